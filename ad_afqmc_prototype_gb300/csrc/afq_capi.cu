@@ -1,0 +1,532 @@
+// extern "C" entry points of libafqmc_gb300.so (declared in afqmc_gb300.h):
+// argument checks, workspace layout, and the host-side orchestration of the
+// step and block.  Nothing here allocates device memory or synchronises,
+// except the set-up call afq_build_prop_ctx (one norm read-back for expm).
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "afq_internal.cuh"
+
+namespace afq {
+
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return AFQ_OK;
+    return fail(AFQ_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+size_t energy_partial_count(int W, int o, int G);
+int launch_sr_scan_dev(int W, const double* weights, const double* zeta_dev, double* levels, int32_t* idx,
+                       double* avg_out, cudaStream_t s);
+
+static int check_dims(const afq_dims* d, bool need_chol = true) {
+    if (!d) return fail(AFQ_E_INVALID_ARGUMENT, "dims is NULL");
+    if (d->n_walkers < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_walkers=%d < 1", d->n_walkers);
+    if (d->norb < 1) return fail(AFQ_E_INVALID_ARGUMENT, "norb=%d < 1", d->norb);
+    if (d->nocc < 1 || d->nocc > d->norb)
+        return fail(AFQ_E_INVALID_ARGUMENT, "nocc=%d outside [1, norb=%d]", d->nocc, d->norb);
+    if (d->nocc > 64) return fail(AFQ_E_UNSUPPORTED, "nocc=%d > 64", d->nocc);
+    if (d->norb > 512) return fail(AFQ_E_UNSUPPORTED, "norb=%d > 512", d->norb);
+    if (need_chol && d->nchol < 1) return fail(AFQ_E_INVALID_ARGUMENT, "nchol=%d < 1", d->nchol);
+    if (d->precision != AFQ_PREC_FP64 && d->precision != AFQ_PREC_MIXED)
+        return fail(AFQ_E_INVALID_ARGUMENT, "unknown precision %d", d->precision);
+    return AFQ_OK;
+}
+
+#define AFQ_NOTNULL(p)                                                      \
+    do {                                                                    \
+        if (!(p)) return fail(AFQ_E_INVALID_ARGUMENT, "%s is NULL", #p);    \
+    } while (0)
+
+static int check_ws(const Arena& a, size_t have) {
+    if (a.used > have) return fail(AFQ_E_WORKSPACE, "workspace of %zu bytes < %zu needed", have, a.used);
+    return AFQ_OK;
+}
+
+// ------------------------------------------------------- workspace layouts
+struct StepWS {
+    double* fields;     // W*G (drawn fields)
+    double2* green;     // W*o*n
+    double2* fb;        // W*G
+    double2* xs;        // W*G
+    double2* V;         // Wc*n*n
+    double2* shift_term, *fb_term, *ovl_new;  // W
+};
+
+static int chunk_size(int W, int n_chunks) { return n_chunks <= 1 ? W : (W + n_chunks - 1) / n_chunks; }
+
+static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
+    const size_t W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const size_t Wc = chunk_size(d->n_walkers, n_chunks);
+    StepWS s;
+    s.fields = a.take<double>(W * G);
+    s.green = a.take<double2>(W * o * n);
+    s.fb = a.take<double2>(W * G);
+    s.xs = a.take<double2>(W * G);
+    s.V = a.take<double2>(Wc * n * n);
+    s.shift_term = a.take<double2>(W);
+    s.fb_term = a.take<double2>(W);
+    s.ovl_new = a.take<double2>(W);
+    return s;
+}
+
+struct BlockWS {
+    StepWS step;
+    double2* energy;     // W
+    double* partial;     // energy partials
+    double* levels;      // comb scan
+    int32_t* idx;        // W
+    double* avg;         // 1
+    double* zeta;        // 1
+    double2* wcopy;      // W*n*o
+    double2* ocopy;      // W
+};
+
+static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
+    BlockWS b;
+    b.step = layout_step(a, d, n_chunks);
+    const size_t W = d->n_walkers;
+    b.energy = a.take<double2>(W);
+    b.partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
+    b.levels = a.take<double>(sr_levels_size(d->n_walkers));
+    b.idx = a.take<int32_t>(W);
+    b.avg = a.take<double>(1);
+    b.zeta = a.take<double>(1);
+    b.wcopy = a.take<double2>(W * d->norb * d->nocc);
+    b.ocopy = a.take<double2>(W);
+    return b;
+}
+
+// ------------------------------------------------------------ step pieces
+static int force_bias_from_green(const afq_dims* d, const double2* green, const double* rot_chol,
+                                 double2* fb, cudaStream_t s) {
+    const int on = d->nocc * d->norb;
+    return launch_zgemm(d->n_walkers, d->nchol, on, 2.0, green, on, rot_chol, on, !d->trial_is_real, true, fb,
+                        d->nchol, s);
+}
+
+static int trotter_chunked(const afq_dims* d, int n_terms, double sqrt_dt, int n_chunks, const double* chol,
+                           const double* E, const double2* win, const double2* xs, double2* wout, double2* V,
+                           cudaStream_t s) {
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const int Wc = chunk_size(W, n_chunks);
+    for (int w0 = 0; w0 < W; w0 += Wc) {
+        const int wc = W - w0 < Wc ? W - w0 : Wc;
+        // V (wc x n^2) = x~ (wc x G) . chol (G x n^2)   (prop/chol_afqmc_ops.py:70-74)
+        AFQ_TRY(launch_zgemm(wc, n * n, G, 1.0, xs + (size_t)w0 * G, G, chol, (int64_t)n * n, false, false, V,
+                             (int64_t)n * n, s));
+        AFQ_TRY(launch_trotter(wc, n, o, n_terms, sqrt_dt, E, V, win + (size_t)w0 * n * o,
+                               wout + (size_t)w0 * n * o, s));
+    }
+    return AFQ_OK;
+}
+
+static int check_problem(const afq_problem* pb) {
+    if (!pb) return fail(AFQ_E_INVALID_ARGUMENT, "problem is NULL");
+    AFQ_TRY(check_dims(&pb->dims));
+    AFQ_NOTNULL(pb->chol);
+    AFQ_NOTNULL(pb->mo_coeff);
+    AFQ_NOTNULL(pb->exp_h1_half);
+    AFQ_NOTNULL(pb->mf_shifts);
+    AFQ_NOTNULL(pb->rot_h1);
+    AFQ_NOTNULL(pb->rot_chol);
+    if (!(pb->dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", pb->dt);
+    if (pb->dims.precision == AFQ_PREC_MIXED)
+        return fail(AFQ_E_UNSUPPORTED, "precision MIXED is not available in this build");
+    return AFQ_OK;
+}
+
+static int check_state(const afq_state* st) {
+    if (!st) return fail(AFQ_E_INVALID_ARGUMENT, "state is NULL");
+    AFQ_NOTNULL(st->walkers);
+    AFQ_NOTNULL(st->weights);
+    AFQ_NOTNULL(st->overlaps);
+    AFQ_NOTNULL(st->pop_control_ene_shift);
+    AFQ_NOTNULL(st->e_estimate);
+    return AFQ_OK;
+}
+
+static int check_params(const afq_params* p) {
+    if (!p) return fail(AFQ_E_INVALID_ARGUMENT, "params is NULL");
+    if (p->n_exp_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_exp_terms=%d < 0", p->n_exp_terms);
+    if (p->n_prop_steps < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_prop_steps=%d < 0", p->n_prop_steps);
+    if (!(p->dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", p->dt);
+    return AFQ_OK;
+}
+
+static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
+                     uint64_t seed, uint64_t counter, const StepWS& ws, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const double2* mo = (const double2*)pb->mo_coeff;
+    double2* walk = (double2*)st->walkers;
+    if (!fields) {
+        AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
+        fields = ws.fields;
+    }
+    // force bias (prop/afqmc.py:90-95)
+    AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s));
+    AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s));
+    // shifts (prop/afqmc.py:97-101)
+    AFQ_TRY(launch_field_shift(W, G, pb->sqrt_dt, fields, ws.fb, (const double2*)pb->mf_shifts, ws.xs,
+                               ws.shift_term, ws.fb_term, s));
+    // propagation (prop/afqmc.py:103-110)
+    AFQ_TRY(trotter_chunked(d, p->n_exp_terms, pb->sqrt_dt, p->n_chunks, pb->chol, pb->exp_h1_half, walk, ws.xs,
+                            walk, ws.V, s));
+    // overlaps (prop/afqmc.py:112-114)
+    AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, ws.ovl_new, nullptr, s));
+    // weights (prop/afqmc.py:116-138)
+    return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
+                                ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
+                                st->pop_control_ene_shift, st->e_estimate, s);
+}
+
+static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    double2* walk = (double2*)st->walkers;
+    AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+    return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
+                        (double2*)st->overlaps, nullptr, s);
+}
+
+}  // namespace afq
+
+using namespace afq;
+
+extern "C" {
+
+int afq_abi_version(void) { return AFQ_ABI_VERSION; }
+
+const char* afq_status_string(int status) {
+    switch (status) {
+        case AFQ_OK: return "ok";
+        case AFQ_E_INVALID_ARGUMENT: return "invalid argument";
+        case AFQ_E_UNSUPPORTED: return "unsupported size or mode";
+        case AFQ_E_CUDA: return "CUDA error";
+        case AFQ_E_WORKSPACE: return "workspace too small";
+        case AFQ_E_DEVICE_CHECK: return "device-side check failed";
+        default: return "unknown status";
+    }
+}
+
+const char* afq_last_error(void) { return g_err; }
+
+// ------------------------------------------------------------------ set-up
+size_t afq_build_prop_ctx_workspace(int32_t norb, int32_t nchol) {
+    (void)nchol;
+    Arena a;
+    a.take<double2>((size_t)norb * norb);  // dm
+    a.take<double>((size_t)norb * norb);   // h1_eff
+    for (int k = 0; k < 3; ++k) a.take<double>((size_t)norb * norb);
+    a.take<double>(1);
+    return a.used;
+}
+
+int afq_build_prop_ctx(int32_t norb, int32_t nchol, double h0, double dt, const double* h1, const double* chol,
+                       const double* rdm1, int32_t rdm1_spin_blocks, double* exp_h1_half, double* mf_shifts,
+                       double* h0_prop, void* workspace, size_t workspace_bytes, void* stream) {
+    if (norb < 1 || nchol < 1) return fail(AFQ_E_INVALID_ARGUMENT, "norb=%d nchol=%d", norb, nchol);
+    AFQ_NOTNULL(h1); AFQ_NOTNULL(chol); AFQ_NOTNULL(rdm1);
+    AFQ_NOTNULL(exp_h1_half); AFQ_NOTNULL(mf_shifts); AFQ_NOTNULL(h0_prop); AFQ_NOTNULL(workspace);
+    if (!(dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", dt);
+    cudaStream_t s = as_stream(stream);
+    const int n = norb;
+    Arena a(workspace, workspace_bytes);
+    double2* dm = a.take<double2>((size_t)n * n);
+    double* h1e = a.take<double>((size_t)n * n);
+    double* t0 = a.take<double>((size_t)n * n);
+    double* t1 = a.take<double>((size_t)n * n);
+    double* t2 = a.take<double>((size_t)n * n);
+    double* nrm = a.take<double>(1);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    const double2* dmp = (const double2*)rdm1;
+    if (rdm1_spin_blocks) {
+        AFQ_TRY(launch_sum_spin_blocks(n, (const double2*)rdm1, dm, s));
+        dmp = dm;
+    }
+    AFQ_TRY(launch_mf_shifts(n, nchol, chol, dmp, (double2*)mf_shifts, s));
+    AFQ_TRY(launch_h0_prop(nchol, h0, (const double2*)mf_shifts, (double2*)h0_prop, s));
+    AFQ_TRY(launch_h1_eff(n, nchol, h1, chol, (const double2*)mf_shifts, h1e, s));
+    AFQ_TRY(launch_expm(n, -0.5 * dt, h1e, exp_h1_half, t0, t1, t2, nrm, s));
+    return AFQ_OK;
+}
+
+int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* h1, const double* chol,
+                       const double* mo_coeff, int32_t trial_is_real, double* rot_h1, double* rot_chol,
+                       void* stream) {
+    if (norb < 1 || nocc < 1 || nocc > norb || nchol < 1)
+        return fail(AFQ_E_INVALID_ARGUMENT, "norb=%d nocc=%d nchol=%d", norb, nocc, nchol);
+    AFQ_NOTNULL(h1); AFQ_NOTNULL(chol); AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rot_h1); AFQ_NOTNULL(rot_chol);
+    return launch_rot(norb, nocc, nchol, h1, chol, (const double2*)mo_coeff, trial_is_real, (double2*)rot_h1,
+                      rot_chol, as_stream(stream));
+}
+
+size_t afq_lowp_bytes(const afq_dims* d) {
+    (void)d;
+    return 0;
+}
+
+int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_chol, void* out, size_t out_bytes,
+                     void* stream) {
+    (void)d; (void)chol; (void)rot_chol; (void)out; (void)out_bytes; (void)stream;
+    return fail(AFQ_E_UNSUPPORTED, "precision MIXED is not available in this build");
+}
+
+// ----------------------------------------------------------- walker kernels
+int afq_overlap(const afq_dims* d, const double* mo_coeff, const double* walkers, double* overlaps, void* stream) {
+    AFQ_TRY(check_dims(d, false));
+    AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(walkers); AFQ_NOTNULL(overlaps);
+    return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)mo_coeff, d->trial_is_real,
+                        (const double2*)walkers, (double2*)overlaps, nullptr, as_stream(stream));
+}
+
+int afq_half_green(const afq_dims* d, const double* mo_coeff, const double* walkers, double* green,
+                   double* overlaps, void* stream) {
+    AFQ_TRY(check_dims(d, false));
+    AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(walkers); AFQ_NOTNULL(green);
+    return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)mo_coeff, d->trial_is_real,
+                        (const double2*)walkers, (double2*)overlaps, (double2*)green, as_stream(stream));
+}
+
+size_t afq_force_bias_workspace(const afq_dims* d) {
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
+    return a.used;
+}
+
+int afq_force_bias(const afq_dims* d, const double* mo_coeff, const double* rot_chol, const double* walkers,
+                   double* force_bias, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_dims(d));
+    AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rot_chol); AFQ_NOTNULL(walkers); AFQ_NOTNULL(force_bias);
+    AFQ_NOTNULL(workspace);
+    Arena a(workspace, workspace_bytes);
+    double2* green = a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    cudaStream_t s = as_stream(stream);
+    AFQ_TRY(launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)mo_coeff, d->trial_is_real,
+                         (const double2*)walkers, nullptr, green, s));
+    return force_bias_from_green(d, green, rot_chol, (double2*)force_bias, s);
+}
+
+size_t afq_energy_workspace(const afq_dims* d) {
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
+    a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
+    return a.used;
+}
+
+int afq_energy(const afq_dims* d, double h0, const double* mo_coeff, const double* rot_h1, const double* rot_chol,
+               const double* walkers, double* energy, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_dims(d));
+    AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rot_h1); AFQ_NOTNULL(rot_chol); AFQ_NOTNULL(walkers); AFQ_NOTNULL(energy);
+    AFQ_NOTNULL(workspace);
+    Arena a(workspace, workspace_bytes);
+    double2* green = a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
+    double* partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    cudaStream_t s = as_stream(stream);
+    AFQ_TRY(launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)mo_coeff, d->trial_is_real,
+                         (const double2*)walkers, nullptr, green, s));
+    return launch_energy(d->n_walkers, d->norb, d->nocc, d->nchol, h0, green, rot_chol, d->trial_is_real,
+                         (const double2*)rot_h1, partial, (double2*)energy, s);
+}
+
+size_t afq_apply_trotter_workspace(const afq_dims* d, int32_t n_chunks) {
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    a.take<double2>((size_t)chunk_size(d->n_walkers, n_chunks) * d->norb * d->norb);
+    return a.used;
+}
+
+int afq_apply_trotter(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_t n_chunks, const double* chol,
+                      const double* exp_h1_half, const double* walkers, const double* shifted_fields,
+                      double* walkers_out, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_dims(d));
+    AFQ_NOTNULL(chol); AFQ_NOTNULL(exp_h1_half); AFQ_NOTNULL(walkers); AFQ_NOTNULL(shifted_fields);
+    AFQ_NOTNULL(walkers_out); AFQ_NOTNULL(workspace);
+    if (n_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_terms=%d < 0", n_terms);
+    Arena a(workspace, workspace_bytes);
+    double2* V = a.take<double2>((size_t)chunk_size(d->n_walkers, n_chunks) * d->norb * d->norb);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    return trotter_chunked(d, n_terms, sqrt_dt, n_chunks, chol, exp_h1_half, (const double2*)walkers,
+                           (const double2*)shifted_fields, (double2*)walkers_out, V, as_stream(stream));
+}
+
+int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_out, double* det_r, void* stream) {
+    AFQ_TRY(check_dims(d, false));
+    AFQ_NOTNULL(walkers); AFQ_NOTNULL(walkers_out);
+    return launch_qr(d->n_walkers, d->norb, d->nocc, (const double2*)walkers, (double2*)walkers_out,
+                     (double2*)det_r, as_stream(stream));
+}
+
+size_t afq_sr_workspace(int32_t n_walkers) {
+    Arena a;
+    a.take<double>(sr_levels_size(n_walkers));
+    a.take<int32_t>(n_walkers);
+    a.take<double>(1);
+    return a.used;
+}
+
+int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_t* idx, double* cumsum,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+    if (n_walkers < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_walkers=%d < 1", n_walkers);
+    AFQ_NOTNULL(weights); AFQ_NOTNULL(idx); AFQ_NOTNULL(workspace);
+    Arena a(workspace, workspace_bytes);
+    double* lv = a.take<double>(sr_levels_size(n_walkers));
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    return launch_sr_scan(n_walkers, weights, zeta, lv, idx, cumsum, nullptr, as_stream(stream));
+}
+
+int afq_stochastic_reconfiguration(const afq_dims* d, const double* weights, double zeta, const double* walkers,
+                                   double* walkers_out, double* weights_out, int32_t* idx, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_dims(d, false));
+    AFQ_NOTNULL(weights); AFQ_NOTNULL(walkers); AFQ_NOTNULL(walkers_out); AFQ_NOTNULL(weights_out);
+    AFQ_NOTNULL(workspace);
+    if (walkers == walkers_out) return fail(AFQ_E_INVALID_ARGUMENT, "walkers_out must not alias walkers");
+    Arena a(workspace, workspace_bytes);
+    double* lv = a.take<double>(sr_levels_size(d->n_walkers));
+    int32_t* id = a.take<int32_t>(d->n_walkers);
+    double* avg = a.take<double>(1);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    cudaStream_t s = as_stream(stream);
+    AFQ_TRY(launch_sr_scan(d->n_walkers, weights, zeta, lv, id, nullptr, avg, s));
+    AFQ_TRY(launch_gather(d->n_walkers, (int64_t)d->norb * d->nocc, id, (const double2*)walkers,
+                          (double2*)walkers_out, avg, weights_out, s));
+    if (idx) AFQ_CUDA(cudaMemcpyAsync(idx, id, sizeof(int32_t) * d->n_walkers, cudaMemcpyDeviceToDevice, s));
+    return AFQ_OK;
+}
+
+// ------------------------------------------------------------- step pieces
+int afq_fill_normal(int64_t count, uint64_t seed, uint64_t counter, double* out, void* stream) {
+    AFQ_NOTNULL(out);
+    return launch_philox(count, seed, counter, 1, out, as_stream(stream));
+}
+
+int afq_fill_uniform(int64_t count, uint64_t seed, uint64_t counter, double* out, void* stream) {
+    AFQ_NOTNULL(out);
+    return launch_philox(count, seed, counter, 0, out, as_stream(stream));
+}
+
+int afq_field_shift(const afq_dims* d, double sqrt_dt, const double* fields, const double* force_bias,
+                    const double* mf_shifts, double* shifted_fields, double* shift_term, double* fb_term,
+                    void* stream) {
+    AFQ_TRY(check_dims(d));
+    AFQ_NOTNULL(fields); AFQ_NOTNULL(force_bias); AFQ_NOTNULL(mf_shifts); AFQ_NOTNULL(shifted_fields);
+    AFQ_NOTNULL(shift_term); AFQ_NOTNULL(fb_term);
+    return launch_field_shift(d->n_walkers, d->nchol, sqrt_dt, fields, (const double2*)force_bias,
+                              (const double2*)mf_shifts, (double2*)shifted_fields, (double2*)shift_term,
+                              (double2*)fb_term, as_stream(stream));
+}
+
+int afq_weight_update(const afq_dims* d, const afq_params* p, const afq_problem* pb, const double* shift_term,
+                      const double* fb_term, const double* overlaps_new, const afq_state* st, void* stream) {
+    AFQ_TRY(check_dims(d, false));
+    AFQ_TRY(check_params(p));
+    if (!pb) return fail(AFQ_E_INVALID_ARGUMENT, "problem is NULL");
+    AFQ_TRY(check_state(st));
+    AFQ_NOTNULL(shift_term); AFQ_NOTNULL(fb_term); AFQ_NOTNULL(overlaps_new);
+    return launch_weight_update(d->n_walkers, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
+                                (const double2*)shift_term, (const double2*)fb_term, (const double2*)overlaps_new,
+                                st->weights, (double2*)st->overlaps, st->pop_control_ene_shift, st->e_estimate,
+                                as_stream(stream));
+}
+
+int afq_block_measure(int32_t n_walkers, double dt, double shift_ema, const double* weights, const double* energy,
+                      const double* e_estimate, double* pop_control_ene_shift, double* block_energy,
+                      double* block_weight, void* stream) {
+    if (n_walkers < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_walkers=%d < 1", n_walkers);
+    if (!(dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", dt);
+    AFQ_NOTNULL(weights); AFQ_NOTNULL(energy); AFQ_NOTNULL(e_estimate); AFQ_NOTNULL(pop_control_ene_shift);
+    AFQ_NOTNULL(block_energy); AFQ_NOTNULL(block_weight);
+    return launch_block_measure(n_walkers, dt, shift_ema, weights, (const double2*)energy, e_estimate,
+                                pop_control_ene_shift, block_energy, block_weight, as_stream(stream));
+}
+
+// ----------------------------------------------------------- step / block
+size_t afq_step_workspace(const afq_dims* d, int32_t n_chunks) {
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    layout_step(a, d, n_chunks);
+    return a.used;
+}
+
+int afq_step(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields, uint64_t seed,
+             uint64_t counter, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_problem(pb));
+    AFQ_TRY(check_params(p));
+    AFQ_TRY(check_state(st));
+    AFQ_NOTNULL(workspace);
+    Arena a(workspace, workspace_bytes);
+    StepWS ws = layout_step(a, &pb->dims, p->n_chunks);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    return step_impl(pb, p, st, fields, seed, counter, ws, as_stream(stream));
+}
+
+size_t afq_block_workspace(const afq_dims* d, int32_t n_chunks) {
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    layout_block(a, d, n_chunks);
+    return a.used;
+}
+
+int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields, double zeta,
+              uint64_t seed, uint64_t counter, double* block_energy, double* block_weight, int32_t* sr_idx,
+              void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_problem(pb));
+    AFQ_TRY(check_params(p));
+    AFQ_TRY(check_state(st));
+    AFQ_NOTNULL(block_energy); AFQ_NOTNULL(block_weight); AFQ_NOTNULL(workspace);
+    const afq_dims* d = &pb->dims;
+    Arena a(workspace, workspace_bytes);
+    BlockWS ws = layout_block(a, d, p->n_chunks);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    cudaStream_t s = as_stream(stream);
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const size_t fstride = (size_t)W * G;
+    // prop/blocks.py:38-51
+    for (int st_i = 0; st_i < p->n_prop_steps; ++st_i) {
+        AFQ_TRY(step_impl(pb, p, st, fields ? fields + st_i * fstride : nullptr, seed, counter + st_i, ws.step, s));
+        if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps)
+            AFQ_TRY(orthonormalize_refresh(pb, st, s));
+    }
+    // prop/blocks.py:53-57
+    AFQ_TRY(orthonormalize_refresh(pb, st, s));
+    // prop/blocks.py:59-79
+    AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
+                         nullptr, ws.step.green, s));
+    AFQ_TRY(launch_energy(W, n, o, G, pb->h0, ws.step.green, pb->rot_chol, d->trial_is_real,
+                          (const double2*)pb->rot_h1, ws.partial, ws.energy, s));
+    AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
+                                 st->pop_control_ene_shift, block_energy, block_weight, s));
+    // prop/blocks.py:81-92
+    if (zeta < 0.0) {
+        AFQ_TRY(launch_philox(1, seed, counter + p->n_prop_steps, 0, ws.zeta, s));
+        AFQ_TRY(launch_sr_scan_dev(W, st->weights, ws.zeta, ws.levels, ws.idx, ws.avg, s));
+    } else {
+        AFQ_TRY(launch_sr_scan(W, st->weights, zeta, ws.levels, ws.idx, nullptr, ws.avg, s));
+    }
+    AFQ_CUDA(cudaMemcpyAsync(ws.wcopy, st->walkers, sizeof(double2) * (size_t)W * n * o, cudaMemcpyDeviceToDevice, s));
+    AFQ_CUDA(cudaMemcpyAsync(ws.ocopy, st->overlaps, sizeof(double2) * (size_t)W, cudaMemcpyDeviceToDevice, s));
+    AFQ_TRY(launch_gather(W, (int64_t)n * o, ws.idx, ws.wcopy, (double2*)st->walkers, ws.avg, st->weights, s));
+    // overlaps of the copied walkers: a copy of the source walker's overlap is
+    // bit-identical to recomputing det(C^H W)^2 on the copied data
+    AFQ_TRY(launch_gather(W, 1, ws.idx, ws.ocopy, (double2*)st->overlaps, ws.avg, nullptr, s));
+    if (sr_idx) AFQ_CUDA(cudaMemcpyAsync(sr_idx, ws.idx, sizeof(int32_t) * W, cudaMemcpyDeviceToDevice, s));
+    return AFQ_OK;
+}
+
+}  // extern "C"

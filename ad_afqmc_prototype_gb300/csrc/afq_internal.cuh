@@ -1,0 +1,131 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "afqmc_gb300.h"
+
+namespace afq {
+
+// ---------------------------------------------------------------- errors --
+// Records a thread-local message and returns `code`.
+int fail(int code, const char* fmt, ...);
+// Checks the last launch / a runtime call.
+int check_cuda(cudaError_t e, const char* what);
+#define AFQ_TRY(expr)            \
+    do {                         \
+        int _rc = (expr);        \
+        if (_rc != AFQ_OK) return _rc; \
+    } while (0)
+#define AFQ_CUDA(expr) AFQ_TRY(::afq::check_cuda((expr), #expr))
+#define AFQ_LAUNCHED(name) AFQ_TRY(::afq::check_cuda(cudaGetLastError(), name))
+
+// --------------------------------------------------------- complex maths --
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // conj(a) * b
+    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// acc += a * b
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += r * b  (r real)
+__device__ __forceinline__ void rfma(double2& acc, double r, double2 b) {
+    acc.x = fma(r, b.x, acc.x);
+    acc.y = fma(r, b.y, acc.y);
+}
+__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+// complex division a / b (Smith's method)
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    if (fabs(b.x) >= fabs(b.y)) {
+        double r = b.y / b.x, den = b.x + b.y * r;
+        return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+    } else {
+        double r = b.x / b.y, den = b.x * r + b.y;
+        return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------- workspace --
+// Bump allocator over a caller-provided workspace; every region is aligned
+// to 256 bytes.  With base == nullptr it only measures.
+struct Arena {
+    char* base;
+    size_t cap;
+    size_t used;
+    explicit Arena(void* b = nullptr, size_t c = 0) : base((char*)b), cap(c), used(0) {}
+    template <class T>
+    T* take(size_t count) {
+        size_t off = (used + 255) & ~(size_t)255;
+        used = off + count * sizeof(T);
+        return base ? (T*)(base + off) : nullptr;
+    }
+    bool ok() const { return base == nullptr || used <= cap; }
+};
+
+inline cudaStream_t as_stream(void* s) { return (cudaStream_t)s; }
+
+// --------------------------------------------------- launch entry points --
+// k_setup.cu
+int launch_mf_shifts(int n, int G, const double* chol, const double2* dm, double2* mf,
+                     cudaStream_t s);
+int launch_h1_eff(int n, int G, const double* h1, const double* chol, const double2* mf,
+                  double* h1_eff, cudaStream_t s);
+int launch_expm(int n, double scale, const double* a, double* out, double* tmp0, double* tmp1,
+                double* tmp2, double* norm_dev, cudaStream_t s);
+int launch_rot(int n, int o, int G, const double* h1, const double* chol, const double2* mo,
+               int trial_real, double2* rot_h1, void* rot_chol, cudaStream_t s);
+int launch_h0_prop(int G, double h0, const double2* mf, double2* h0_prop, cudaStream_t s);
+int launch_sum_spin_blocks(int n, const double2* rdm1, double2* dm, cudaStream_t s);
+
+// k_gemm.cu : C (M x N complex) = alpha * A (M x K complex, lda) * B
+//   B real or complex; B_TRANS: B(k, n) at B[n*ldb + k] else B[k*ldb + n]
+int launch_zgemm(int M, int N, int K, double alpha, const double2* A, int64_t lda,
+                 const void* B, int64_t ldb, bool b_complex, bool b_trans, double2* C,
+                 int64_t ldc, cudaStream_t s);
+
+// k_walker.cu
+int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                 double2* ovlp_out, double2* green_out, cudaStream_t s);
+int launch_trotter(int W, int n, int o, int n_terms, double sqrt_dt, const double* E,
+                   const double2* V, const double2* win, double2* wout, cudaStream_t s);
+int launch_field_shift(int W, int G, double sqrt_dt, const double* x, const double2* fb,
+                       const double2* mf, double2* xs, double2* shift_term, double2* fb_term,
+                       cudaStream_t s);
+int launch_weight_update(int W, const afq_params* p, double sqrt_dt, double dt,
+                         double2 h0_prop, const double2* shift_term, const double2* fb_term,
+                         const double2* ovlp_new, double* weights, double2* overlaps,
+                         double* pop_shift, const double* e_est, cudaStream_t s);
+int launch_energy(int W, int n, int o, int G, double h0, const double2* green,
+                  const void* rot_chol, int trial_real, const double2* rot_h1,
+                  double* partial, double2* energy, cudaStream_t s);
+int launch_qr(int W, int n, int o, const double2* win, double2* wout, double2* det_r,
+              cudaStream_t s);
+int launch_sr_scan(int W, const double* weights, double zeta, double* levels, int32_t* idx,
+                   double* cumsum_out, double* avg_out, cudaStream_t s);
+int launch_gather(int W, int64_t row, const int32_t* idx, const double2* src, double2* dst,
+                  const double* avg, double* weights_out, cudaStream_t s);
+int launch_block_measure(int W, double dt, double shift_ema, const double* weights,
+                         const double2* energy, const double* e_est, double* pop_shift,
+                         double* block_energy, double* block_weight, cudaStream_t s);
+int launch_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, double* out,
+                  cudaStream_t s);
+size_t sr_levels_size(int W);
+
+}  // namespace afq

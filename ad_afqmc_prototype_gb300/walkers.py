@@ -1,0 +1,126 @@
+"""Walker batches and population operations (walkers.py:1-265 of the
+reference), restricted walkers on the CUDA engine."""
+from __future__ import annotations
+
+from typing import Any, Callable
+
+import torch
+
+from . import engine
+from .core.system import system
+
+
+def _natorbs(dm: torch.Tensor, n_occ: int) -> torch.Tensor:
+    """walkers.py:13-16."""
+    dm = 0.5 * (dm + dm.conj().T)
+    vecs = torch.linalg.eigh(dm)[1].flip(-1)
+    return vecs[:, :n_occ]
+
+
+def init_walkers(sys: system, rdm1, n_walkers: int):
+    """Walkers from natural orbitals of the total rdm1 (walkers.py:19-77)."""
+    wk = sys.walker_kind.lower()
+    rdm1 = torch.as_tensor(rdm1)
+    if wk == "restricted":
+        if rdm1.dim() == 2:
+            raise ValueError(
+                "For walker_kind in {'restricted','unrestricted'}, rdm1 must be spin-block (2, norb, norb).")
+        if rdm1.dim() != 3 or rdm1.shape[0] != 2:
+            raise ValueError("Expected rdm1 with shape (2, norb, norb).")
+        dm_tot = engine.as_device(rdm1[0] + rdm1[1], engine.C128)
+        w0 = _natorbs(dm_tot, sys.nup).to(engine.C128)
+        return w0.unsqueeze(0).expand(n_walkers, *w0.shape).contiguous()
+    if wk in ("unrestricted", "generalized"):
+        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    raise ValueError(f"unknown walker_kind: {wk}")
+
+
+def is_unrestricted(w) -> bool:
+    return isinstance(w, tuple) and len(w) == 2
+
+
+def n_walkers(w) -> int:
+    return w[0].shape[0] if is_unrestricted(w) else w.shape[0]
+
+
+def _chunk_size(nw: int, n_chunks: int) -> int:
+    if nw % n_chunks != 0:
+        raise ValueError(f"n_walkers={nw} is not divisible into n_chunks={n_chunks}")
+    return nw // n_chunks
+
+
+def _run(fn: Callable, chunk_args, extra_args, kwargs):
+    batched = getattr(fn, "batched", None)
+    if batched is not None:
+        return batched(*chunk_args, *extra_args, **kwargs)
+    return torch.func.vmap(lambda *xs: fn(*xs, *extra_args, **kwargs))(*chunk_args)
+
+
+def apply_chunked(w, apply_fn: Callable, n_chunks: int, *args, **kwargs):
+    """apply_fn(walker_i, *args) over all walkers, in n_chunks sequential
+    chunks (walkers.py:94-127).  Engine kernels run a chunk per launch."""
+    nw = n_walkers(w)
+    if n_chunks == 1:
+        return _run(apply_fn, (w,), args, kwargs)
+    cs = _chunk_size(nw, n_chunks)
+    outs = [_run(apply_fn, (w[i * cs:(i + 1) * cs],), args, kwargs) for i in range(n_chunks)]
+    return torch.cat(outs, dim=0)
+
+
+def apply_chunked_prop(w, fields, prop_fn: Callable, n_chunks: int, *args, **kwargs):
+    """prop_fn(walker_i, fields_i, *args) in chunks (walkers.py:130-166)."""
+    nw = n_walkers(w)
+    if n_chunks == 1:
+        return _run(prop_fn, (w, fields), args, kwargs)
+    cs = _chunk_size(nw, n_chunks)
+    outs = [_run(prop_fn, (w[i * cs:(i + 1) * cs], fields[i * cs:(i + 1) * cs]), args, kwargs)
+            for i in range(n_chunks)]
+    return torch.cat(outs, dim=0)
+
+
+def orthogonalize(w, walker_kind: str):
+    """QR with diag(R) >= 0; returns (Q, det(R)^2) for restricted walkers
+    (walkers.py:183-203)."""
+    wk = walker_kind.lower()
+    if wk == "restricted":
+        q, det_r = engine.orthogonalize(w)
+        return q, det_r * det_r
+    if wk in ("unrestricted", "generalized"):
+        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    raise ValueError(f"unknown walker_kind: {walker_kind}")
+
+
+def orthonormalize(w, walker_kind: str):
+    """walkers.py:206-211."""
+    return orthogonalize(w, walker_kind)[0]
+
+
+def multiply_constants(w, constants: Any):
+    """walkers.py:214-230."""
+    if is_unrestricted(w):
+        wu, wd = w
+        if isinstance(constants, (tuple, list)) and len(constants) == 2:
+            cu, cd = constants
+            return (wu * torch.as_tensor(cu).reshape(-1, 1, 1), wd * torch.as_tensor(cd).reshape(-1, 1, 1))
+        c = torch.as_tensor(constants).reshape(-1, 1, 1)
+        return (wu * c, wd * c)
+    return w * torch.as_tensor(constants).to(w.device).reshape(-1, 1, 1)
+
+
+def _sr_indices(weights, zeta: float, n_walkers: int):
+    """Comb indices (walkers.py:233-240)."""
+    idx, _ = engine.sr_indices(weights, float(zeta))
+    if idx.shape[0] != n_walkers:
+        raise ValueError("n_walkers must equal len(weights)")
+    return idx
+
+
+def stochastic_reconfiguration(w, weights, zeta: float, walker_kind: str):
+    """walkers.py:243-265: returns (walkers, weights)."""
+    wk = walker_kind.lower()
+    if wk != "restricted":
+        if wk in ("unrestricted", "generalized"):
+            raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+        raise ValueError(f"unknown walker_kind: {walker_kind}")
+    w_new, weights_new, _ = engine.stochastic_reconfiguration(w, weights, float(zeta))
+    return w_new, weights_new

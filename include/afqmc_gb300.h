@@ -1,0 +1,243 @@
+/*
+ * afqmc_gb300.h -- C ABI of the GB300 phaseless-AFQMC step engine.
+ *
+ * Restricted walkers, RHF trial, Cholesky-factorised Hamiltonian.  Every
+ * entry point replaces one call of the reference package
+ * (ad_afqmc_prototype, a JAX program; citations are file:line inside that
+ * project).  The reference has no native FFI of its own: its plug points are
+ * Python callables (core/ops.py:11-90, prop/chol_afqmc_ops.py:45-50,
+ * driver.py:39-47 block_fn), so these functions are what a ctypes / cffi /
+ * torch-extension binding of that Python surface calls.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers owned by the caller, C-contiguous.
+ *    "complex" arrays are interleaved complex128 (re, im) passed as double*.
+ *  - Walkers are (n_walkers, norb, nocc) complex128, as in walkers.py:64-68.
+ *  - Every call is asynchronous on `stream` (a cudaStream_t passed as void*;
+ *    NULL = legacy default stream) except the ones documented as set-up.
+ *  - Hot calls allocate nothing: scratch comes from `workspace`, whose size
+ *    the matching afq_*_workspace() query returns.  Too small -> AFQ_E_WORKSPACE.
+ *  - Return 0 on success or a negative AFQ_E_* code; no call aborts, traps or
+ *    throws across the ABI.  afq_last_error() gives a thread-local message.
+ *  - Numerical trouble (zero overlap, overflowing importance weight) is
+ *    absorbed the way the reference absorbs it (weights set to zero,
+ *    prop/afqmc.py:127-134), not reported as an error.
+ */
+#ifndef AFQMC_GB300_H
+#define AFQMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AFQ_ABI_VERSION 1
+
+#define AFQ_OK 0
+#define AFQ_E_INVALID_ARGUMENT (-1) /* bad shape, null pointer, bad value */
+#define AFQ_E_UNSUPPORTED (-2)      /* size outside what the kernels handle */
+#define AFQ_E_CUDA (-3)             /* a CUDA runtime call failed */
+#define AFQ_E_WORKSPACE (-4)        /* workspace smaller than the query says */
+#define AFQ_E_DEVICE_CHECK (-5)     /* a device-side bounded wait or check failed */
+
+#define AFQ_PREC_FP64 0  /* every product in binary64 */
+#define AFQ_PREC_MIXED 1 /* tensor-core / FP32 products, FP64 overlaps, QR, weights */
+
+/* Sizes of one batch.  trial_is_real selects the real-trial fast path:
+ * mo_coeff is still passed as complex128 but its imaginary parts must be 0,
+ * and rot_chol is then real (G, o, n) float64 instead of complex. */
+typedef struct afq_dims {
+    int32_t n_walkers;
+    int32_t norb;
+    int32_t nocc;
+    int32_t nchol;
+    int32_t trial_is_real;
+    int32_t precision; /* AFQ_PREC_* */
+} afq_dims;
+
+/* afqmc_params (prop/types.py:19-32) plus the in-block QR cadence. */
+typedef struct afq_params {
+    double dt;
+    double pop_control_damping;
+    double weight_floor;
+    double weight_cap;
+    double shift_ema;
+    int32_t n_exp_terms;
+    int32_t n_prop_steps;
+    int32_t qr_every;  /* 0: orthonormalise only at block end (prop/blocks.py:53) */
+    int32_t n_chunks;  /* walker chunks for the V workspace (walkers.py:94-166) */
+} afq_params;
+
+/* Hamiltonian, trial and the two contexts, all device pointers.
+ * prop ctx = chol_afqmc_ctx (prop/chol_afqmc_ops.py:15-42),
+ * meas ctx = rhf_meas_ctx (meas/rhf.py:133-138). */
+typedef struct afq_problem {
+    afq_dims dims;
+    double h0;
+    const double* chol;        /* (G, n, n) float64 */
+    const double* mo_coeff;    /* (n, o) complex128 */
+    double dt;
+    double sqrt_dt;
+    const double* exp_h1_half; /* (n, n) float64 */
+    const double* mf_shifts;   /* (G,) complex128 */
+    double h0_prop_re;
+    double h0_prop_im;
+    const double* rot_h1;      /* (o, n) complex128 */
+    const double* rot_chol;    /* (G, o, n) float64 or complex128 */
+    const void* lowp;          /* afq_prepare_lowp() output; NULL for FP64 */
+} afq_problem;
+
+/* prop_state (prop/types.py:10-16) without the rng key; device pointers. */
+typedef struct afq_state {
+    double* walkers;               /* (W, n, o) complex128 */
+    double* weights;               /* (W,) float64 */
+    double* overlaps;              /* (W,) complex128 */
+    double* pop_control_ene_shift; /* (1,) float64 */
+    double* e_estimate;            /* (1,) float64 */
+} afq_state;
+
+int afq_abi_version(void);
+const char* afq_status_string(int status);
+const char* afq_last_error(void);
+
+/* ---- set-up (synchronises `stream`; allocates nothing) ------------------ */
+
+/* _build_prop_ctx, prop/chol_afqmc_ops.py:77-103 (+ _mf_shifts :59-63,
+ * _build_exp_h1_half_from_h1 :66-67).  rdm1 is complex (2, n, n) when
+ * rdm1_spin_blocks = 1 (summed as at :53-56) or a total (n, n) when 0.
+ * Outputs: exp_h1_half (n,n) f64, mf_shifts (G,) c128, h0_prop (1,) c128. */
+size_t afq_build_prop_ctx_workspace(int32_t norb, int32_t nchol);
+int afq_build_prop_ctx(int32_t norb, int32_t nchol, double h0, double dt,
+                       const double* h1, const double* chol, const double* rdm1,
+                       int32_t rdm1_spin_blocks, double* exp_h1_half, double* mf_shifts,
+                       double* h0_prop, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* build_meas_ctx, meas/rhf.py:141-150.  rot_h1 (o,n) c128; rot_chol (G,o,n)
+ * f64 when trial_is_real else c128. */
+int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* h1,
+                       const double* chol, const double* mo_coeff, int32_t trial_is_real,
+                       double* rot_h1, double* rot_chol, void* stream);
+
+/* Low-precision copies of chol / rot_chol for AFQ_PREC_MIXED (bf16 hi+lo
+ * splits in tensor-core tile order).  `out` must hold afq_lowp_bytes(). */
+size_t afq_lowp_bytes(const afq_dims* d);
+int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_chol,
+                     void* out, size_t out_bytes, void* stream);
+
+/* ---- per-walker kernels, batched over walkers --------------------------- */
+
+/* overlap_r: det(C^H W)^2.  meas/rhf.py:22-24 = trial/rhf.py:35-37. */
+int afq_overlap(const afq_dims* d, const double* mo_coeff, const double* walkers,
+                double* overlaps, void* stream);
+
+/* _half_green_from_overlap_matrix: G_half = solve((C^H W)^T, W^T), (W,o,n)
+ * c128 (meas/rhf.py:15-19).  `overlaps` (optional, may be NULL) receives
+ * det(C^H W)^2 from the same factorisation. */
+int afq_half_green(const afq_dims* d, const double* mo_coeff, const double* walkers,
+                   double* green, double* overlaps, void* stream);
+
+/* force_bias_kernel_r: 2 L~_flat vec(G_half), (W, G) c128 (meas/rhf.py:27-33). */
+size_t afq_force_bias_workspace(const afq_dims* d);
+int afq_force_bias(const afq_dims* d, const double* mo_coeff, const double* rot_chol,
+                   const double* walkers, double* force_bias, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* energy_kernel_r: h0 + e1 + 2 sum_g c_g^2 - exc, (W,) c128 (meas/rhf.py:36-50). */
+size_t afq_energy_workspace(const afq_dims* d);
+int afq_energy(const afq_dims* d, double h0, const double* mo_coeff, const double* rot_h1,
+               const double* rot_chol, const double* walkers, double* energy,
+               void* workspace, size_t workspace_bytes, void* stream);
+
+/* apply_trotter (restricted): E_half exp(i sqrt_dt V(x)) E_half W with a
+ * n_terms Taylor series, V(x) = sum_g x_g L_g built from complex
+ * shifted_fields (W, G).  prop/chol_afqmc_ops.py:173-183 (+ :70-74, :106-107,
+ * :127-137, prop/utils.py:20-31).  walkers_out may equal walkers. */
+size_t afq_apply_trotter_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_apply_trotter(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_t n_chunks,
+                      const double* chol, const double* exp_h1_half, const double* walkers,
+                      const double* shifted_fields, double* walkers_out, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* orthogonalize / orthonormalize (restricted): Householder QR with diag(R)
+ * real >= 0 (walkers.py:169-211).  det_r (optional) receives prod diag(R)
+ * (W,) c128; the restricted normalisation is det_r^2.  walkers_out may equal
+ * walkers. */
+int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_out,
+                      double* det_r, void* stream);
+
+/* _sr_indices (walkers.py:233-240): comb indices (int32) and the inclusive
+ * prefix sum of |w| (optional, may be NULL) in the engine's association
+ * order (32-wide Hillis-Steele segments, recursive on segment totals). */
+size_t afq_sr_workspace(int32_t n_walkers);
+int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_t* idx,
+                   double* cumsum, void* workspace, size_t workspace_bytes, void* stream);
+
+/* stochastic_reconfiguration (walkers.py:243-265): walkers_out[k] =
+ * walkers[idx[k]], weights_out = sum|w| / W.  walkers_out must not alias
+ * walkers.  idx (optional) receives the indices. */
+int afq_stochastic_reconfiguration(const afq_dims* d, const double* weights, double zeta,
+                                   const double* walkers, double* walkers_out,
+                                   double* weights_out, int32_t* idx, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
+/* ---- the step pieces (prop/afqmc.py:86-138) ----------------------------- */
+
+/* Philox4x32-10 (Salmon et al., SC'11) normals by Box-Muller, and uniforms
+ * in [0, 1); element i depends only on (seed, counter, i). */
+int afq_fill_normal(int64_t count, uint64_t seed, uint64_t counter, double* out,
+                    void* stream);
+int afq_fill_uniform(int64_t count, uint64_t seed, uint64_t counter, double* out,
+                     void* stream);
+
+/* prop/afqmc.py:97-101: field shifts, shifted fields (W,G) c128 and the
+ * per-walker shift_term, fb_term (W,) c128. */
+int afq_field_shift(const afq_dims* d, double sqrt_dt, const double* fields,
+                    const double* force_bias, const double* mf_shifts, double* shifted_fields,
+                    double* shift_term, double* fb_term, void* stream);
+
+/* prop/afqmc.py:116-138: importance weights with the phaseless cut, floor and
+ * cap, population-control shift.  Updates st->weights, st->overlaps (copied
+ * from overlaps_new) and st->pop_control_ene_shift in place. */
+int afq_weight_update(const afq_dims* d, const afq_params* p, const afq_problem* pb,
+                      const double* shift_term, const double* fb_term,
+                      const double* overlaps_new, const afq_state* st, void* stream);
+
+/* prop/blocks.py:59-79: clip |Re E - e_est| > sqrt(2/dt) to e_est, weighted
+ * block energy (w_sum == 0 -> e_est), shift <- (1-a) shift + a E_blk.
+ * energy (W,) c128; block_energy, block_weight (1,) f64 outputs;
+ * pop_control_ene_shift (1,) updated in place. */
+int afq_block_measure(int32_t n_walkers, double dt, double shift_ema, const double* weights,
+                      const double* energy, const double* e_estimate,
+                      double* pop_control_ene_shift, double* block_energy, double* block_weight,
+                      void* stream);
+
+/* ---- fused step and block ------------------------------------------------ */
+
+/* afqmc_step (prop/afqmc.py:74-147).  fields (W,G) f64 injected, or NULL to
+ * draw them with afq_fill_normal(seed, counter). */
+size_t afq_step_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_step(const afq_problem* pb, const afq_params* p, const afq_state* st,
+             const double* fields, uint64_t seed, uint64_t counter, void* workspace,
+             size_t workspace_bytes, void* stream);
+
+/* afqmc_block (prop/blocks.py:22-95): n_prop_steps steps (with an extra
+ * orthonormalisation after every qr_every-th step when qr_every > 0), QR,
+ * mixed energy with clip, weighted block energy, shift EMA, comb
+ * reconfiguration.  fields: (n_prop_steps, W, G) f64 or NULL (step s draws
+ * with counter + s); zeta: the comb uniform, or a negative value to draw it
+ * with afq_fill_uniform(seed, counter + n_prop_steps).  block_energy and
+ * block_weight are device (1,) f64 outputs; sr_idx (optional) (W,) int32. */
+size_t afq_block_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st,
+              const double* fields, double zeta, uint64_t seed, uint64_t counter,
+              double* block_energy, double* block_weight, int32_t* sr_idx,
+              void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AFQMC_GB300_H */
