@@ -83,7 +83,24 @@ _SIGS = {
     "afq_block_workspace": (c_size_t, [POINTER(afq_dims), c_int32]),
     "afq_block": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_double,
                             c_uint64, c_uint64, P, P, P, P, c_size_t, P]),
+    "afq_launch_count": (ctypes.c_longlong, []),
+    "afq_timing_enable": (c_int32, [c_int32]),
+    "afq_timing_report": (c_int32, [ctypes.c_char_p, c_size_t]),
+    "afq_timing_reset": (c_int32, []),
+    "afq_probe_fma_peak": (c_int32, [c_int32, POINTER(c_double)]),
 }
+
+
+def timing_report() -> dict:
+    """{phase: (calls, total_ms)} accumulated since the last reset."""
+    lib = load()
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib.afq_timing_report(buf, len(buf)), "afq_timing_report")
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, calls, ms = line.split()
+        out[name] = (int(calls), float(ms))
+    return out
 
 _lib = None
 

@@ -124,10 +124,12 @@ static int trotter_chunked(const afq_dims* d, int n_terms, double sqrt_dt, int n
     for (int w0 = 0; w0 < W; w0 += Wc) {
         const int wc = W - w0 < Wc ? W - w0 : Wc;
         // V (wc x n^2) = x~ (wc x G) . chol (G x n^2)   (prop/chol_afqmc_ops.py:70-74)
+        { AFQ_PHASE("vbuild_gemm", s);
         AFQ_TRY(launch_zgemm(wc, n * n, G, 1.0, xs + (size_t)w0 * G, G, chol, (int64_t)n * n, false, false, V,
-                             (int64_t)n * n, s));
+                             (int64_t)n * n, s)); }
+        { AFQ_PHASE("trotter", s);
         AFQ_TRY(launch_trotter(wc, n, o, n_terms, sqrt_dt, E, V, win + (size_t)w0 * n * o,
-                               wout + (size_t)w0 * n * o, s));
+                               wout + (size_t)w0 * n * o, s)); }
     }
     return AFQ_OK;
 }
@@ -172,20 +174,23 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
     const double2* mo = (const double2*)pb->mo_coeff;
     double2* walk = (double2*)st->walkers;
     if (!fields) {
+        AFQ_PHASE("philox", s);
         AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
         fields = ws.fields;
     }
     // force bias (prop/afqmc.py:90-95)
-    AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s));
-    AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s));
+    { AFQ_PHASE("green", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s)); }
+    { AFQ_PHASE("fb_gemm", s); AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s)); }
     // shifts (prop/afqmc.py:97-101)
+    { AFQ_PHASE("field_shift", s);
     AFQ_TRY(launch_field_shift(W, G, pb->sqrt_dt, fields, ws.fb, (const double2*)pb->mf_shifts, ws.xs,
-                               ws.shift_term, ws.fb_term, s));
+                               ws.shift_term, ws.fb_term, s)); }
     // propagation (prop/afqmc.py:103-110)
     AFQ_TRY(trotter_chunked(d, p->n_exp_terms, pb->sqrt_dt, p->n_chunks, pb->chol, pb->exp_h1_half, walk, ws.xs,
                             walk, ws.V, s));
     // overlaps (prop/afqmc.py:112-114)
-    AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, ws.ovl_new, nullptr, s));
+    { AFQ_PHASE("overlap", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, ws.ovl_new, nullptr, s)); }
+    AFQ_PHASE("weight_update", s);
     // weights (prop/afqmc.py:116-138)
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
@@ -195,7 +200,8 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
 static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
-    AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+    { AFQ_PHASE("qr", s); AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s)); }
+    AFQ_PHASE("overlap", s);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
                         (double2*)st->overlaps, nullptr, s);
 }
@@ -506,12 +512,16 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
     // prop/blocks.py:53-57
     AFQ_TRY(orthonormalize_refresh(pb, st, s));
     // prop/blocks.py:59-79
+    { AFQ_PHASE("green", s);
     AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
-                         nullptr, ws.step.green, s));
+                         nullptr, ws.step.green, s)); }
+    { AFQ_PHASE("energy", s);
     AFQ_TRY(launch_energy(W, n, o, G, pb->h0, ws.step.green, pb->rot_chol, d->trial_is_real,
-                          (const double2*)pb->rot_h1, ws.partial, ws.energy, s));
+                          (const double2*)pb->rot_h1, ws.partial, ws.energy, s)); }
+    { AFQ_PHASE("block_measure", s);
     AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
-                                 st->pop_control_ene_shift, block_energy, block_weight, s));
+                                 st->pop_control_ene_shift, block_energy, block_weight, s)); }
+    AFQ_PHASE("comb", s);
     // prop/blocks.py:81-92
     if (zeta < 0.0) {
         AFQ_TRY(launch_philox(1, seed, counter + p->n_prop_steps, 0, ws.zeta, s));

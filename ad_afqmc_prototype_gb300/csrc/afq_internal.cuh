@@ -20,7 +20,27 @@ int check_cuda(cudaError_t e, const char* what);
         if (_rc != AFQ_OK) return _rc; \
     } while (0)
 #define AFQ_CUDA(expr) AFQ_TRY(::afq::check_cuda((expr), #expr))
-#define AFQ_LAUNCHED(name) AFQ_TRY(::afq::check_cuda(cudaGetLastError(), name))
+#define AFQ_LAUNCHED(name)                                        \
+    do {                                                          \
+        ::afq::count_launch();                                    \
+        AFQ_TRY(::afq::check_cuda(cudaGetLastError(), name));     \
+    } while (0)
+
+// ---------------------------------------------------------------- tracing --
+// afq_trace.cu: a process-wide count of kernel launches, and (when enabled
+// with afq_timing_enable) CUDA events recorded on the launching stream around
+// each named phase of the step and block.
+void count_launch();
+struct Phase {
+    const char* name;
+    cudaStream_t stream;
+    cudaEvent_t start;
+    Phase(const char* n, cudaStream_t s);
+    ~Phase();
+};
+#define AFQ_PHASE_CAT2(a, b) a##b
+#define AFQ_PHASE_CAT(a, b) AFQ_PHASE_CAT2(a, b)
+#define AFQ_PHASE(name, s) ::afq::Phase AFQ_PHASE_CAT(afq_phase_, __LINE__)(name, s)
 
 // --------------------------------------------------------- complex maths --
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }

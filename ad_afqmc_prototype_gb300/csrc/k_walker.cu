@@ -593,13 +593,15 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
         }
         __syncthreads();
     }
-    // Q[:, k] *= conj(alpha_k / |alpha_k|)
+    // R~_kk = alpha_k is complex here (the reference's LAPACK R has a real
+    // diagonal, hence its conj(phase) fix); Q[:, k] *= alpha_k / |alpha_k|
+    // gives the same unique Q with diag(R) real and >= 0.
     double2* Wo = wout + (size_t)w * n * o;
     for (int e = tid; e < n * o; e += blockDim.x) {
         int i = e / o, j = e % o;
         double2 a = s_alpha[j];
         double aa = sqrt(cabs2(a));
-        double2 cph = aa == 0.0 ? make_double2(1.0, 0.0) : make_double2(a.x / aa, -a.y / aa);
+        double2 cph = aa == 0.0 ? make_double2(1.0, 0.0) : make_double2(a.x / aa, a.y / aa);
         Wo[e] = cmul(A[j * ld + i], cph);
     }
     if (det_out && tid == 0) {

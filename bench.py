@@ -1,0 +1,392 @@
+"""Throughput benchmark of the AFQMC block on GB300.
+
+One bench step = one AFQMC block of the benchmark workload: 10 propagation
+steps with a QR after step 5, then QR, mixed energy, shift update and comb
+reconfiguration (QR every 5 steps, energy and comb every 10).  The metric is
+walker-steps/s = n_walkers * 10 / (seconds per block), summed over ranks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp64|mixed] [--workload NAME]
+
+--impl reference times the CPU restatement of the reference's algorithm
+(the JAX reference cannot be installed here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "walker-steps/s at |ΔE|≤0.1 mHa vs FP64 oracle: chosen form vs plain FP64 GPU"
+UNIT = "walker-steps/s"
+STEPS_PER_BLOCK = 10
+QR_EVERY = 5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="c4_n200_o30_g1000_w4096")
+    ap.add_argument("--walkers", type=int, default=0, help="override the workload's walker count")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+# ----------------------------------------------------------------- clocks ---
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------- algorithmic work model ---
+def phase_work(n, o, G, W, trial_real=True):
+    """Algorithmic FLOPs per launch of each timed phase (real-flop units)."""
+    cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
+    return {
+        "vbuild_gemm": 4.0 * G * n * n * W,
+        "trotter": (48.0 + 8.0) * n * n * o * W,
+        "fb_gemm": cm * G * o * n * W,
+        "green": (cm * o * o * n + 16.0 * o ** 3 + 8.0 * n * o * o) * W,
+        "overlap": (cm * o * o * n + 16.0 * o ** 3) * W,
+        "energy": (cm * G * o * o * n + 8.0 * G * o * o) * W,
+        "qr": (32.0 * n * o * o - 10.7 * o ** 3) * W,
+    }
+
+
+# ------------------------------------------------------------ our engine ---
+def make_engine_state(wl, W, precision):
+    import torch
+    from ad_afqmc_prototype_gb300 import synth
+    from ad_afqmc_prototype_gb300.core.system import system
+    from ad_afqmc_prototype_gb300.ham.chol import ham_chol
+    from ad_afqmc_prototype_gb300.meas.rhf import make_rhf_meas_ops
+    from ad_afqmc_prototype_gb300.prop.afqmc import engine_problem, init_prop_state
+    from ad_afqmc_prototype_gb300.prop.chol_afqmc_ops import make_chol_afqmc_ops
+    from ad_afqmc_prototype_gb300.prop.types import afqmc_params
+    from ad_afqmc_prototype_gb300.trial.rhf import get_rdm1, make_rhf_trial_ops, rhf_trial
+
+    H = synth.make_workload(wl)
+    n, o = wl.nbasis, wl.nocc
+    sys_ = system(norb=n, nelec=(o, o), walker_kind="restricted")
+    ham = ham_chol(h0=H["h0"], h1=H["h1"], chol=H["chol"])
+    trial = rhf_trial(H["mo_coeff"])
+    t_ops, m_ops = make_rhf_trial_ops(sys_), make_rhf_meas_ops(sys_)
+    p_ops = make_chol_afqmc_ops(ham, "restricted")
+    params = afqmc_params(dt=0.005, n_prop_steps=STEPS_PER_BLOCK, qr_every=QR_EVERY, n_walkers=W, seed=2024,
+                          precision=precision)
+    pctx = p_ops.build_prop_ctx(get_rdm1(trial), params.dt)
+    mctx = m_ops.build_meas_ctx(ham, trial)
+    state = init_prop_state(sys=sys_, n_walkers=W, seed=params.seed, ham_data=ham, trial_ops_=t_ops,
+                            trial_data=trial, meas_ops=m_ops,
+                            initial_walkers=synth.trial_walkers(H["mo_coeff"], W))
+    kw = dict(params=params, ham_data=ham, trial_data=trial, meas_ops=m_ops, prop_ops=p_ops, prop_ctx=pctx,
+              meas_ctx=mctx)
+    prob = engine_problem(n_walkers=W, need_energy=True, **kw)
+    torch.cuda.synchronize()
+    return dict(H=H, sys=sys_, kw=kw, prob=prob, state=state, params=params)
+
+
+def run_ours(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    from ad_afqmc_prototype_gb300 import _lib, engine, synth
+    from ad_afqmc_prototype_gb300.prop.afqmc import device_state
+    from ad_afqmc_prototype_gb300.prop.blocks import afqmc_block
+
+    wl = synth.WORKLOADS[args.workload]
+    W = args.walkers or wl.n_walkers
+    n, o, G = wl.nbasis, wl.nocc, wl.nchol
+    env = make_engine_state(wl, W, args.precision)
+    prob, params = env["prob"], env["params"]
+    st = device_state(env["state"], inplace=True)
+    lib = _lib.load()
+    seed = 1000 + rank
+    ctr = 0
+
+    def one_block():
+        nonlocal ctr
+        engine.block(prob, params, st, seed, ctr)
+        ctr += STEPS_PER_BLOCK + 1
+
+    for _ in range(args.warmup):
+        one_block()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    lib.afq_timing_reset()
+    lib.afq_timing_enable(1)
+    launches0 = lib.afq_launch_count()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        one_block()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.afq_launch_count() - launches0
+    lib.afq_timing_enable(0)
+    phases = _lib.timing_report()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * W * STEPS_PER_BLOCK / (ms / 1000.0)
+
+    # dominant kernel and its roofline
+    work = phase_work(n, o, G, W, trial_real=prob.trial_is_real)
+    dom = max(phases.items(), key=lambda kv: kv[1][1])
+    dname, (dcalls, dms) = dom
+    roof = None
+    if dname in work:
+        avg_ms = dms / dcalls
+        achieved = work[dname] / (avg_ms / 1000.0) / 1e12
+        peak, src = fp64_peak(lib) if args.precision == "fp64" else (None, None)
+        roof = {"kernel": dname, "bound": "fp64" if args.precision == "fp64" else "tensor",
+                "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
+                "peak_source": src, "avg_launch_ms": round(avg_ms, 4),
+                "share_of_step": round(dms / sum(v[1] for v in phases.values()), 4)}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, env, afqmc_block, W)
+
+    out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3/f32+f64",
+           "data": "synthetic (seeded Cholesky Hamiltonian, see ad_afqmc_prototype_gb300/synth.py)",
+           "config": {"workload": args.workload, "norb": n, "nocc": o, "nchol": G, "n_walkers_per_gpu": W,
+                      "precision": args.precision, "parallelism": f"replicas{world}",
+                      "step": "one block: 10 propagation steps, QR after step 5, QR + energy + comb at the end",
+                      "l2": "inputs larger than L2 (walkers %d MB, V %d MB per step)"
+                            % (W * n * o * 16 >> 20, W * n * n * 16 >> 20)},
+           "roofline": roof, "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
+           "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+    return out
+
+
+_FP64_PEAK = None
+
+
+def fp64_peak(lib):
+    """FP64 FMA throughput of this GPU, measured once in-process (the pool's
+    MEASURED_PEAKS.json has HBM and bf16 peaks only)."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        import ctypes
+        v = ctypes.c_double(0.0)
+        rc = lib.afq_probe_fma_peak(1, ctypes.byref(v))
+        _FP64_PEAK = (round(v.value, 4), "measured in-process (FMA chains)") if rc == 0 else (None, None)
+    return _FP64_PEAK
+
+
+def run_e2e(args, env, afqmc_block, W):
+    """The same metric through the public API with host buffers: each step
+    copies walkers, weights and overlaps from pinned host memory, runs
+    afqmc_block, and reads walkers, weights, overlaps and the block energy
+    back to pinned host memory."""
+    import torch
+    st0 = env["state"]
+    hw = torch.empty(st0.walkers.shape, dtype=torch.complex128, pin_memory=True)
+    hwt = torch.empty(st0.weights.shape, dtype=torch.float64, pin_memory=True)
+    hov = torch.empty(st0.overlaps.shape, dtype=torch.complex128, pin_memory=True)
+    he = torch.empty((), dtype=torch.float64, pin_memory=True)
+    hw.copy_(st0.walkers)
+    hwt.copy_(st0.weights)
+    hov.copy_(st0.overlaps)
+    dw, dwt, dov = torch.empty_like(st0.walkers), torch.empty_like(st0.weights), torch.empty_like(st0.overlaps)
+    state = st0
+
+    def one(state):
+        dw.copy_(hw, non_blocking=True)
+        dwt.copy_(hwt, non_blocking=True)
+        dov.copy_(hov, non_blocking=True)
+        s_in = state._replace(walkers=dw, weights=dwt, overlaps=dov)
+        s_out, obs = afqmc_block(s_in, sys=env["sys"], inplace=True, **env["kw"])
+        hw.copy_(s_out.walkers, non_blocking=True)
+        hwt.copy_(s_out.weights, non_blocking=True)
+        hov.copy_(s_out.overlaps, non_blocking=True)
+        he.copy_(obs.scalars["energy"], non_blocking=True)
+        return s_out
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        state = one(state)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        state = one(state)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    bi = hw.numel() * 16 + hwt.numel() * 8 + hov.numel() * 16
+    return {"value": round(W * STEPS_PER_BLOCK / (ms / 1000.0), 3), "unit": UNIT, "h2d_bytes_per_step": bi,
+            "d2h_bytes_per_step": bi + 8, "ms_per_step": round(ms, 3), "api": "prop.blocks.afqmc_block"}
+
+
+# --------------------------------------------------------- CPU baselines ---
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_block_rate(wl, budget_s, warm=False):
+    """Times the CPU oracle on a bounded sample of the workload: blocks of
+    10 steps (QR after step 5) on a few walkers until `budget_s` is spent.
+    Returns (walker-steps/s, sample description)."""
+    from oracle import afqmc_oracle as O
+    from ad_afqmc_prototype_gb300 import synth
+    H = synth.make_workload(wl)
+    prob = O.make_problem(H["h0"], H["h1"], H["chol"], H["mo_coeff"], 0.005)
+    P = O.Params(dt=0.005, n_prop_steps=STEPS_PER_BLOCK, qr_every=QR_EVERY)
+    ws = min(wl.n_walkers, 32 if wl.nbasis >= 120 else 256)
+    st = O.init_prop_state(prob, ws, synth.trial_walkers(H["mo_coeff"], ws))
+    rng = np.random.default_rng(0)
+    if warm:
+        st, _, _ = O.afqmc_block(prob, P, st, rng.standard_normal((STEPS_PER_BLOCK, ws, wl.nchol)), 0.5)
+    t0 = time.perf_counter()
+    nblk = 0
+    while True:
+        f = rng.standard_normal((STEPS_PER_BLOCK, ws, wl.nchol))
+        st, _, _ = O.afqmc_block(prob, P, st, f, float(rng.random()))
+        nblk += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return ws * STEPS_PER_BLOCK * nblk / dt, f"{nblk} block(s) of 10 steps on {ws} walkers, {dt:.1f} s"
+
+
+def cpu_baseline(wl, budget_s):
+    rate, sample = cpu_block_rate(wl, budget_s)
+    return {"value": round(rate, 3), "unit": UNIT, "cores": cpu_cores(), "kind": "port", "sample": sample,
+            "what": "NumPy FP64 restatement of the reference algorithm (oracle/afqmc_oracle.py), BLAS threads = all"}
+
+
+def run_reference(args, rank, world):
+    from ad_afqmc_prototype_gb300 import synth
+    wl = synth.WORKLOADS[args.workload]
+    for _ in range(args.warmup):
+        cpu_block_rate(wl, 0.0)
+    rates = []
+    sample = ""
+    for _ in range(args.steps):
+        r, sample = cpu_block_rate(wl, 0.0)
+        rates.append(r)
+    value = float(np.mean(rates))
+    ms = 1000.0 * STEPS_PER_BLOCK * (32 if wl.nbasis >= 120 else 256) / value
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "precision": "fp64",
+                       "step": "one block: 10 propagation steps, QR after step 5, QR + energy + comb at the end"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                             "sample": sample + " per step",
+                             "what": "the JAX reference cannot be installed (no jax wheel); its algorithm "
+                                     "restated in NumPy FP64 (oracle/afqmc_oracle.py)"},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, rank, world)), flush=True)
+        return
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+    g.build()
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -236,6 +236,23 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st,
               double* block_energy, double* block_weight, int32_t* sr_idx,
               void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- tracing (no counterpart in the reference, which only times blocks
+ * with time.perf_counter, driver.py:83-147) --------------------------------- */
+
+/* Number of kernels this library has launched since it was loaded. */
+long long afq_launch_count(void);
+/* Process-wide switch: when on, the step and block record CUDA events
+ * around each named phase on the launching stream.  Off by default. */
+int afq_timing_enable(int on);
+/* Waits for recorded events and writes "phase calls total_ms\n" lines of the
+ * accumulated per-phase device time into buf. */
+int afq_timing_report(char* buf, size_t len);
+int afq_timing_reset(void);
+/* Calibration (synchronises the device; allocates a small scratch buffer):
+ * SIMT FMA throughput of the current GPU in TFLOP/s, binary64 when fp64 != 0
+ * else binary32 -- the ceiling of the binary64 kernels' roofline. */
+int afq_probe_fma_peak(int fp64, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif
