@@ -278,6 +278,28 @@ int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* 
                       rot_chol, as_stream(stream));
 }
 
+int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B, int64_t ldb,
+                     float* C, int64_t ldc, int32_t* err, void* stream) {
+    AFQ_NOTNULL(A); AFQ_NOTNULL(B); AFQ_NOTNULL(C); AFQ_NOTNULL(err);
+    if (M < 0 || N < 0 || lda < K || ldb < K || ldc < N)
+        return fail(AFQ_E_INVALID_ARGUMENT, "lowp gemm: bad sizes M=%d N=%d K=%d", M, N, K);
+    return launch_tc_gemm_tn(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
+}
+
+int afq_workspace_status(void* workspace, int32_t* status, void* stream) {
+    AFQ_NOTNULL(workspace); AFQ_NOTNULL(status);
+    cudaStream_t s = as_stream(stream);
+    int32_t v = 0;
+    AFQ_CUDA(cudaMemcpyAsync(&v, workspace, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    AFQ_CUDA(cudaStreamSynchronize(s));
+    *status = v;
+    if (v != 0) {
+        AFQ_CUDA(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));
+        return fail(AFQ_E_DEVICE_CHECK, "a bounded device-side wait expired (status %d)", v);
+    }
+    return AFQ_OK;
+}
+
 size_t afq_lowp_bytes(const afq_dims* d) {
     (void)d;
     return 0;

@@ -148,4 +148,8 @@ int launch_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, do
                   cudaStream_t s);
 size_t sr_levels_size(int W);
 
+// k_tc_gemm.cu : C (M x N fp32) = A (M x K bf16) . B (N x K bf16)^T on tcgen05
+int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                      long long ldc, int* err, cudaStream_t s);
+
 }  // namespace afq

@@ -1,0 +1,339 @@
+// Tensor-core GEMM for sm_103a: C[M x N] (fp32) = A[M x K] . B[N x K]^T with
+// bf16 operands, both K-major (row-major with K contiguous).
+//
+// Blackwell path: TMA (cp.async.bulk.tensor, 128-byte swizzle) stages
+// 128x64 A and 256x64 B tiles through a 4-deep shared-memory ring guarded by
+// mbarriers; one thread issues tcgen05.mma (kind::f16, M=128, N=256, K=16)
+// into a double-buffered fp32 accumulator in tensor memory; four epilogue
+// warps read the accumulator back with tcgen05.ld and store it.  The kernel
+// is persistent (one CTA per SM, static round-robin over tiles, M-tiles
+// fastest so CTAs working at the same time share B tiles in L2).
+//
+// Mixed-precision products use the operand layout, not the kernel: a split
+// x = hi + lo (both bf16) is written along K in sections, A = [a_hi a_hi a_lo]
+// and B = [b_hi b_lo b_hi], so one GEMM returns a_hi b_hi + a_hi b_lo +
+// a_lo b_hi (relative error ~2^-17 instead of 2^-9).
+//
+// Every mbarrier wait is bounded (1 s of %globaltimer); on a timeout the CTA
+// raises *err, every role leaves its loop, the producer waits (bounded) for
+// the copies it issued, and the tensor memory is freed before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "afq_internal.cuh"
+
+namespace afq {
+namespace tc {
+
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;
+constexpr int B_BYTES = BN * BK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int ACC_COLS = BN;
+constexpr int TMEM_COLS = 2 * ACC_COLS;
+constexpr int THREADS = 192;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-5: epilogue
+constexpr unsigned long long WAIT_NS = 1000000000ull;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+
+// instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16 (7-9 = 1),
+// B bf16 (10-12 = 1), both K-major (bits 15, 16 = 0), N>>3 at 17, M>>4 at 24
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with `parity`; false on timeout or abort.
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (abort_flag && *abort_flag) return false;
+        if (now_ns() - t0 > WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand tile with 128-byte swizzle: 128-byte rows, 8-row atoms
+// 1024 bytes apart (stride byte offset), descriptor version 1 (bit 46),
+// swizzle mode 2 (bits 61-63).  The leading byte offset is unused for this
+// layout.  Advancing K by 16 bf16 (32 bytes) inside the 128-byte row moves the
+// start address; the tile base is 1024-byte aligned so the swizzle phase is 0.
+__device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, float* __restrict__ C,
+              int M, int N, int K, long long ldc, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + STAGES * A_BYTES;
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+    const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
+    const uint32_t drain = smem_u32(bars + 2 * STAGES + 4);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = (M + BM - 1) / BM, nt = (N + BN - 1) / BN, kt = K / BK;
+    const int ntiles = mt * nt;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 128);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmA) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
+            int stage = 0;
+            uint32_t phase = 0;
+            int issued[STAGES];
+            uint32_t issued_par[STAGES];
+            for (int s = 0; s < STAGES; ++s) issued[s] = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                const int mb = t % mt, nb = t / mt;
+                for (int kb = 0; kb < kt; ++kb) {
+                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
+                    issued[stage] = 0;  // the consumer released it: its copy had landed
+                    mbar_expect_tx(full0 + 8 * stage, STAGE_BYTES);
+                    tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
+                    tma_load_2d(smem_u32(sB + stage * B_BYTES), &tmB, kb * BK, nb * BN, full0 + 8 * stage);
+                    issued[stage] = 1;
+                    issued_par[stage] = phase;
+                    if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                // let the copies this thread issued land before the CTA exits
+                for (int s = 0; s < STAGES; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0, acc = 0;
+            uint32_t phase = 0, acc_phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                if (!mbar_wait(tempty0 + 8 * acc, acc_phase ^ 1, abort_flag)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t d = tmem + acc * ACC_COLS;
+                for (int kb = 0; kb < kt; ++kb) {
+                    if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + stage * A_BYTES), b0 = smem_u32(sB + stage * B_BYTES);
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k)
+                        umma_bf16(d, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), (kb | k) != 0);
+                    umma_commit(empty0 + 8 * stage);
+                    if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                }
+                if (!ok) break;
+                umma_commit(tfull0 + 8 * acc);
+                if (++acc == 2) { acc = 0; acc_phase ^= 1; }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                // MMAs already issued must finish before the tensor memory is freed
+                umma_commit(drain);
+                mbar_wait(drain, 0, nullptr);
+            }
+        }
+    } else {
+        const int q = warp & 3;  // TMEM lane quarter this warp may access
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        const bool vec = (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int mb = t % mt, nb = t / mt;
+            if (!mbar_wait(tfull0 + 8 * acc, acc_phase, abort_flag)) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const int row = mb * BM + q * 32 + lane;
+            float* dst_row = C + (long long)row * ldc;
+#pragma unroll 1
+            for (int c = 0; c < BN; c += 32) {
+                uint32_t r[32];
+                tmem_ld32(tmem + acc * ACC_COLS + c + ((uint32_t)(q * 32) << 16), r);
+                const int col0 = nb * BN + c;
+                if (row < M && col0 < N) {
+                    float* dst = dst_row + col0;
+                    if (vec && col0 + 32 <= N) {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 4)
+                            *(float4*)(dst + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                              __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (col0 + j < N) dst[j] = __uint_as_float(r[j]);
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(tempty0 + 8 * acc);
+            if (++acc == 2) { acc = 0; acc_phase ^= 1; }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ------------------------------------------------------------------- host --
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static int get_encode() {
+    if (g_encode) return AFQ_OK;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    return AFQ_OK;
+}
+
+// rows x cols bf16 matrix, row stride ld elements, box = box_rows x BK
+static int make_map(CUtensorMap* m, const void* base, long long rows, long long cols, long long ld, int box_rows) {
+    if (((uintptr_t)base) & 15) return fail(AFQ_E_INVALID_ARGUMENT, "tensor base not 16-byte aligned");
+    if ((ld * 2) % 16) return fail(AFQ_E_INVALID_ARGUMENT, "tensor row stride not a multiple of 16 bytes");
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return AFQ_OK;
+}
+
+}  // namespace tc
+
+static int g_num_sms = 0;
+
+int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                      long long ldc, int* err, cudaStream_t s) {
+    using namespace tc;
+    if (M <= 0 || N <= 0) return AFQ_OK;
+    if (K <= 0 || K % BK) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: K=%d must be a positive multiple of %d", K, BK);
+    AFQ_TRY(get_encode());
+    CUtensorMap ma, mb;
+    AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
+    AFQ_TRY(make_map(&mb, B, N, K, ldb, BN));
+    if (!g_num_sms) {
+        int dev = 0;
+        AFQ_CUDA(cudaGetDevice(&dev));
+        AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    }
+    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+    k_gemm_tn<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, M, N, K, ldc, err);
+    AFQ_LAUNCHED("k_gemm_tn");
+    return AFQ_OK;
+}
+
+}  // namespace afq

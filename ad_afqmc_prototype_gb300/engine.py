@@ -67,6 +67,7 @@ class _Arena:
         if b is None or b.numel() < nbytes:
             self.buf.pop(dev, None)
             b = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+            b[:256].zero_()  # the step / block status word lives at offset 0
             self.buf[dev] = b
         return b
 

@@ -127,6 +127,20 @@ size_t afq_lowp_bytes(const afq_dims* d);
 int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_chol,
                      void* out, size_t out_bytes, void* stream);
 
+/* The tensor-core GEMM under the mixed-precision V-build and force bias
+ * (prop/chol_afqmc_ops.py:70-74, meas/rhf.py:33): C (M x N, fp32, row stride
+ * ldc) = A (M x K) . B (N x K)^T with bf16 A and B, row-major, K contiguous,
+ * K a multiple of 64, lda / ldb multiples of 8, 16-byte aligned bases.
+ * `err` (device int32, required) is set to 1 if a bounded pipeline wait
+ * expired (the kernel then stops early instead of hanging). */
+int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B,
+                     int64_t ldb, float* C, int64_t ldc, int32_t* err, void* stream);
+
+/* Device status word of a step / block workspace: synchronises `stream`,
+ * copies the word to *status (0 = fine, 1 = a bounded device wait expired)
+ * and clears it.  Returns AFQ_E_DEVICE_CHECK when the word was set. */
+int afq_workspace_status(void* workspace, int32_t* status, void* stream);
+
 /* ---- per-walker kernels, batched over walkers --------------------------- */
 
 /* overlap_r: det(C^H W)^2.  meas/rhf.py:22-24 = trial/rhf.py:35-37. */
