@@ -55,34 +55,100 @@ static int check_ws(const Arena& a, size_t have) {
 }
 
 // ------------------------------------------------------- workspace layouts
+static int chunk_size(int W, int n_chunks) { return n_chunks <= 1 ? W : (W + n_chunks - 1) / n_chunks; }
+
+// Split-operand geometry of the mixed-precision GEMMs: section stride S and
+// row length Kt (a multiple of the GEMM's K tile).
+struct LowpDims {
+    int S_V, Kt_V;   // V-build:    x~ (2W x G)       . L   (n^2 x G)
+    int S_F, Kt_F;   // force bias: G_half (2W x o n) . L~  (G x o n)
+    int S_E, Kt_E;   // energy:     L~ (G o x n)      . G_half rows (2 o W x n)
+    long long ldv;   // row stride of V (fp32)
+};
+
+static LowpDims lowp_dims(const afq_dims* d) {
+    LowpDims L;
+    const int n = d->norb, o = d->nocc, G = d->nchol;
+    L.S_V = G;
+    L.Kt_V = (int)round_up(3LL * G, 64);
+    L.S_F = o * n;
+    L.Kt_F = (int)round_up(3LL * o * n, 64);
+    L.S_E = n;
+    L.Kt_E = (int)round_up(3LL * n, 64);
+    L.ldv = round_up((long long)n * n, 4);
+    return L;
+}
+
+struct LowpBufs {
+    __nv_bfloat16* Bv;  // n^2 x Kt_V   right operand [hi lo hi] of chol^T
+    __nv_bfloat16* Bf;  // G x Kt_F     right operand of rot_chol_flat
+    __nv_bfloat16* Le;  // G o x Kt_E   left operand [hi hi lo] of rot_chol
+};
+
+static LowpBufs layout_lowp(Arena& a, const afq_dims* d) {
+    const LowpDims L = lowp_dims(d);
+    const size_t n = d->norb, o = d->nocc, G = d->nchol;
+    LowpBufs b;
+    b.Bv = a.take<__nv_bfloat16>(n * n * L.Kt_V);
+    b.Bf = a.take<__nv_bfloat16>(G * L.Kt_F);
+    b.Le = a.take<__nv_bfloat16>(G * o * L.Kt_E);
+    return b;
+}
+
 struct StepWS {
+    int* status;        // device status word (offset 0 of every step / block workspace)
     double* fields;     // W*G (drawn fields)
+    double2 *shift_term, *fb_term, *ovl_new;  // W
+    // binary64 form
     double2* green;     // W*o*n
     double2* fb;        // W*G
     double2* xs;        // W*G
     double2* V;         // Wc*n*n
-    double2* shift_term, *fb_term, *ovl_new;  // W
+    // mixed form
+    __nv_bfloat16* Ag;  // 2W x Kt_F
+    float* fbm;         // 2W x G
+    __nv_bfloat16* Av;  // 2W x Kt_V
+    float* Vm;          // 2Wc x ldv
+    float* emi;         // n*n
 };
-
-static int chunk_size(int W, int n_chunks) { return n_chunks <= 1 ? W : (W + n_chunks - 1) / n_chunks; }
 
 static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
     const size_t W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const size_t Wc = chunk_size(d->n_walkers, n_chunks);
-    StepWS s;
+    StepWS s = {};
+    s.status = a.take<int>(64);
     s.fields = a.take<double>(W * G);
-    s.green = a.take<double2>(W * o * n);
-    s.fb = a.take<double2>(W * G);
-    s.xs = a.take<double2>(W * G);
-    s.V = a.take<double2>(Wc * n * n);
     s.shift_term = a.take<double2>(W);
     s.fb_term = a.take<double2>(W);
     s.ovl_new = a.take<double2>(W);
+    if (d->precision == AFQ_PREC_MIXED) {
+        const LowpDims L = lowp_dims(d);
+        s.Ag = a.take<__nv_bfloat16>(2 * W * L.Kt_F);
+        s.fbm = a.take<float>(2 * W * G);
+        s.Av = a.take<__nv_bfloat16>(2 * W * L.Kt_V);
+        s.Vm = a.take<float>(2 * Wc * L.ldv);
+        s.emi = a.take<float>(n * n);
+    } else {
+        s.green = a.take<double2>(W * o * n);
+        s.fb = a.take<double2>(W * G);
+        s.xs = a.take<double2>(W * G);
+        s.V = a.take<double2>(Wc * n * n);
+    }
     return s;
+}
+
+// walkers per energy GEMM in the mixed form: F (G o x 2 o We fp32) <= 2 GiB
+static int energy_chunk(const afq_dims* d) {
+    const long long per = (long long)d->nchol * d->nocc * 2 * d->nocc * 4;
+    long long we = (2LL << 30) / (per > 0 ? per : 1);
+    if (we < 1) we = 1;
+    if (we > d->n_walkers) we = d->n_walkers;
+    return (int)we;
 }
 
 struct BlockWS {
     StepWS step;
+    double2* green;      // W*o*n (energy)
     double2* energy;     // W
     double* partial;     // energy partials
     double* levels;      // comb scan
@@ -91,14 +157,25 @@ struct BlockWS {
     double* zeta;        // 1
     double2* wcopy;      // W*n*o
     double2* ocopy;      // W
+    __nv_bfloat16* Bg;   // mixed energy: 2 o We x Kt_E
+    float* F;            // mixed energy: G o x 2 o We
 };
 
 static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
-    BlockWS b;
+    BlockWS b = {};
     b.step = layout_step(a, d, n_chunks);
     const size_t W = d->n_walkers;
+    b.green = d->precision == AFQ_PREC_MIXED ? a.take<double2>(W * d->nocc * d->norb) : b.step.green;
     b.energy = a.take<double2>(W);
-    b.partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
+    if (d->precision == AFQ_PREC_MIXED) {
+        const LowpDims L = lowp_dims(d);
+        const size_t we = energy_chunk(d);
+        b.partial = (double*)a.take<double2>(W * exchange_chunks(d->nchol) * 2);
+        b.Bg = a.take<__nv_bfloat16>(2 * d->nocc * we * L.Kt_E);
+        b.F = a.take<float>((size_t)d->nchol * d->nocc * 2 * d->nocc * we);
+    } else {
+        b.partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
+    }
     b.levels = a.take<double>(sr_levels_size(d->n_walkers));
     b.idx = a.take<int32_t>(W);
     b.avg = a.take<double>(1);
@@ -144,9 +221,83 @@ static int check_problem(const afq_problem* pb) {
     AFQ_NOTNULL(pb->rot_h1);
     AFQ_NOTNULL(pb->rot_chol);
     if (!(pb->dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", pb->dt);
-    if (pb->dims.precision == AFQ_PREC_MIXED)
-        return fail(AFQ_E_UNSUPPORTED, "precision MIXED is not available in this build");
+    if (pb->dims.precision == AFQ_PREC_MIXED) {
+        if (!pb->lowp) return fail(AFQ_E_INVALID_ARGUMENT, "precision MIXED needs afq_prepare_lowp() output in lowp");
+        if (!pb->dims.trial_is_real)
+            return fail(AFQ_E_UNSUPPORTED, "precision MIXED supports real trial orbitals only");
+    }
     return AFQ_OK;
+}
+
+// The mixed-precision step (AFQ_PREC_MIXED): same sequence as step_impl,
+// with the force bias and V-build on tensor cores and the Taylor series in
+// fp32 products accumulated into the binary64 walkers.
+static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
+                      const StepWS& ws, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const LowpDims L = lowp_dims(d);
+    Arena la((void*)pb->lowp, (size_t)-1);
+    const LowpBufs lb = layout_lowp(la, d);
+    const double2* mo = (const double2*)pb->mo_coeff;
+    double2* walk = (double2*)st->walkers;
+    // force bias: G_half split straight from the Green's function kernel
+    {
+        AFQ_PHASE("green", s);
+        SplitOut so;
+        so.ptr = ws.Ag;
+        so.W = W;
+        so.ld = L.Kt_F;
+        so.S = L.S_F;
+        AFQ_TRY(launch_green_split(W, n, o, mo, 1, walk, nullptr, nullptr, so, s));
+    }
+    { AFQ_PHASE("fb_gemm", s);
+      AFQ_TRY(launch_tc_gemm_tn(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s)); }
+    const int Wc = chunk_size(W, p->n_chunks);
+    { AFQ_PHASE("field_shift", s);
+      AFQ_TRY(launch_field_shift_mixed(W, G, Wc, pb->sqrt_dt, fields, ws.fbm, G, (const double2*)pb->mf_shifts, ws.Av,
+                                       L.S_V, L.Kt_V, ws.shift_term, ws.fb_term, s)); }
+    AFQ_TRY(launch_e_minus_i(n, pb->exp_h1_half, ws.emi, s));
+    for (int w0 = 0; w0 < W; w0 += Wc) {
+        const int wc = W - w0 < Wc ? W - w0 : Wc;
+        { AFQ_PHASE("vbuild_gemm", s);
+          AFQ_TRY(launch_tc_gemm_tn(2 * wc, n * n, L.Kt_V, ws.Av + (size_t)2 * w0 * L.Kt_V, L.Kt_V, lb.Bv, L.Kt_V,
+                                    ws.Vm, L.ldv, ws.status, s)); }
+        { AFQ_PHASE("trotter", s);
+          AFQ_TRY(launch_trotter_mixed(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.emi, ws.Vm, L.ldv,
+                                       walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, s)); }
+    }
+    { AFQ_PHASE("overlap", s); AFQ_TRY(launch_green(W, n, o, mo, 1, walk, ws.ovl_new, nullptr, s)); }
+    AFQ_PHASE("weight_update", s);
+    return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
+                                ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
+                                st->pop_control_ene_shift, st->e_estimate, s);
+}
+
+// Local energies of all walkers into ws.energy (meas/rhf.py:36-50).
+static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS& ws, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    { AFQ_PHASE("green", s);
+      AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
+                           nullptr, ws.green, s)); }
+    AFQ_PHASE("energy", s);
+    if (d->precision != AFQ_PREC_MIXED)
+        return launch_energy(W, n, o, G, pb->h0, ws.green, pb->rot_chol, d->trial_is_real,
+                             (const double2*)pb->rot_h1, ws.partial, ws.energy, s);
+    const LowpDims L = lowp_dims(d);
+    Arena la((void*)pb->lowp, (size_t)-1);
+    const LowpBufs lb = layout_lowp(la, d);
+    const int We = energy_chunk(d), nch = exchange_chunks(G);
+    double2* partial = (double2*)ws.partial;
+    for (int w0 = 0; w0 < W; w0 += We) {
+        const int wc = W - w0 < We ? W - w0 : We;
+        AFQ_TRY(launch_green_rows(wc, n, o, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, s));
+        AFQ_TRY(launch_tc_gemm_tn(G * o, 2 * o * wc, L.Kt_E, lb.Le, L.Kt_E, ws.Bg, L.Kt_E, ws.F, 2LL * o * wc,
+                                  ws.step.status, s));
+        AFQ_TRY(launch_exchange_reduce(wc, G, o, ws.F, 2LL * o * wc, partial + (size_t)w0 * nch * 2, s));
+    }
+    return launch_energy_finish(W, n, o, nch, pb->h0, ws.green, (const double2*)pb->rot_h1, partial, ws.energy, s);
 }
 
 static int check_state(const afq_state* st) {
@@ -178,6 +329,7 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
         AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
         fields = ws.fields;
     }
+    if (d->precision == AFQ_PREC_MIXED) return step_mixed(pb, p, st, fields, ws, s);
     // force bias (prop/afqmc.py:90-95)
     { AFQ_PHASE("green", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s)); }
     { AFQ_PHASE("fb_gemm", s); AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s)); }
@@ -232,6 +384,7 @@ const char* afq_last_error(void) { return g_err; }
 size_t afq_build_prop_ctx_workspace(int32_t norb, int32_t nchol) {
     (void)nchol;
     Arena a;
+    a.take<int>(64);  // status word: offset 0 of every workspace
     a.take<double2>((size_t)norb * norb);  // dm
     a.take<double>((size_t)norb * norb);   // h1_eff
     for (int k = 0; k < 3; ++k) a.take<double>((size_t)norb * norb);
@@ -249,6 +402,7 @@ int afq_build_prop_ctx(int32_t norb, int32_t nchol, double h0, double dt, const 
     cudaStream_t s = as_stream(stream);
     const int n = norb;
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double2* dm = a.take<double2>((size_t)n * n);
     double* h1e = a.take<double>((size_t)n * n);
     double* t0 = a.take<double>((size_t)n * n);
@@ -301,14 +455,31 @@ int afq_workspace_status(void* workspace, int32_t* status, void* stream) {
 }
 
 size_t afq_lowp_bytes(const afq_dims* d) {
-    (void)d;
-    return 0;
+    if (check_dims(d) != AFQ_OK) return 0;
+    Arena a;
+    layout_lowp(a, d);
+    return a.used + 256;
 }
 
 int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_chol, void* out, size_t out_bytes,
                      void* stream) {
-    (void)d; (void)chol; (void)rot_chol; (void)out; (void)out_bytes; (void)stream;
-    return fail(AFQ_E_UNSUPPORTED, "precision MIXED is not available in this build");
+    AFQ_TRY(check_dims(d));
+    AFQ_NOTNULL(chol); AFQ_NOTNULL(rot_chol); AFQ_NOTNULL(out);
+    if (!d->trial_is_real) return fail(AFQ_E_UNSUPPORTED, "precision MIXED supports real trial orbitals only");
+    if (((uintptr_t)out) & 255) return fail(AFQ_E_INVALID_ARGUMENT, "lowp buffer must be 256-byte aligned");
+    Arena a(out, out_bytes);
+    const LowpBufs b = layout_lowp(a, d);
+    AFQ_TRY(check_ws(a, out_bytes));
+    const LowpDims L = lowp_dims(d);
+    const long long n = d->norb, o = d->nocc, G = d->nchol;
+    cudaStream_t s = as_stream(stream);
+    // chol^T: row j = (i, k) of L_g[i, k] over g   (right operand of the V-build)
+    AFQ_TRY(launch_split_rows(n * n, (int)G, L.S_V, L.Kt_V, chol, 1, n * n, b.Bv, 0, s));
+    // rot_chol_flat: row g over (p, j)              (right operand of the force bias)
+    AFQ_TRY(launch_split_rows(G, (int)(o * n), L.S_F, L.Kt_F, rot_chol, o * n, 1, b.Bf, 0, s));
+    // rot_chol rows (g, p) over j                   (left operand of the energy)
+    AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, s));
+    return AFQ_OK;
 }
 
 // ----------------------------------------------------------- walker kernels
@@ -330,6 +501,7 @@ int afq_half_green(const afq_dims* d, const double* mo_coeff, const double* walk
 size_t afq_force_bias_workspace(const afq_dims* d) {
     if (check_dims(d) != AFQ_OK) return 0;
     Arena a;
+    a.take<int>(64);  // status word: offset 0 of every workspace
     a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
     return a.used;
 }
@@ -340,6 +512,7 @@ int afq_force_bias(const afq_dims* d, const double* mo_coeff, const double* rot_
     AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rot_chol); AFQ_NOTNULL(walkers); AFQ_NOTNULL(force_bias);
     AFQ_NOTNULL(workspace);
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double2* green = a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
     AFQ_TRY(check_ws(a, workspace_bytes));
     cudaStream_t s = as_stream(stream);
@@ -351,6 +524,7 @@ int afq_force_bias(const afq_dims* d, const double* mo_coeff, const double* rot_
 size_t afq_energy_workspace(const afq_dims* d) {
     if (check_dims(d) != AFQ_OK) return 0;
     Arena a;
+    a.take<int>(64);  // status word: offset 0 of every workspace
     a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
     a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
     return a.used;
@@ -362,6 +536,7 @@ int afq_energy(const afq_dims* d, double h0, const double* mo_coeff, const doubl
     AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rot_h1); AFQ_NOTNULL(rot_chol); AFQ_NOTNULL(walkers); AFQ_NOTNULL(energy);
     AFQ_NOTNULL(workspace);
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double2* green = a.take<double2>((size_t)d->n_walkers * d->nocc * d->norb);
     double* partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
     AFQ_TRY(check_ws(a, workspace_bytes));
@@ -375,6 +550,7 @@ int afq_energy(const afq_dims* d, double h0, const double* mo_coeff, const doubl
 size_t afq_apply_trotter_workspace(const afq_dims* d, int32_t n_chunks) {
     if (check_dims(d) != AFQ_OK) return 0;
     Arena a;
+    a.take<int>(64);  // status word: offset 0 of every workspace
     a.take<double2>((size_t)chunk_size(d->n_walkers, n_chunks) * d->norb * d->norb);
     return a.used;
 }
@@ -387,6 +563,7 @@ int afq_apply_trotter(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_
     AFQ_NOTNULL(walkers_out); AFQ_NOTNULL(workspace);
     if (n_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_terms=%d < 0", n_terms);
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double2* V = a.take<double2>((size_t)chunk_size(d->n_walkers, n_chunks) * d->norb * d->norb);
     AFQ_TRY(check_ws(a, workspace_bytes));
     return trotter_chunked(d, n_terms, sqrt_dt, n_chunks, chol, exp_h1_half, (const double2*)walkers,
@@ -402,6 +579,7 @@ int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_
 
 size_t afq_sr_workspace(int32_t n_walkers) {
     Arena a;
+    a.take<int>(64);  // status word: offset 0 of every workspace
     a.take<double>(sr_levels_size(n_walkers));
     a.take<int32_t>(n_walkers);
     a.take<double>(1);
@@ -413,6 +591,7 @@ int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_
     if (n_walkers < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_walkers=%d < 1", n_walkers);
     AFQ_NOTNULL(weights); AFQ_NOTNULL(idx); AFQ_NOTNULL(workspace);
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double* lv = a.take<double>(sr_levels_size(n_walkers));
     AFQ_TRY(check_ws(a, workspace_bytes));
     return launch_sr_scan(n_walkers, weights, zeta, lv, idx, cumsum, nullptr, as_stream(stream));
@@ -426,6 +605,7 @@ int afq_stochastic_reconfiguration(const afq_dims* d, const double* weights, dou
     AFQ_NOTNULL(workspace);
     if (walkers == walkers_out) return fail(AFQ_E_INVALID_ARGUMENT, "walkers_out must not alias walkers");
     Arena a(workspace, workspace_bytes);
+    a.take<int>(64);  // status word: offset 0 of every workspace
     double* lv = a.take<double>(sr_levels_size(d->n_walkers));
     int32_t* id = a.take<int32_t>(d->n_walkers);
     double* avg = a.take<double>(1);
@@ -534,12 +714,7 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
     // prop/blocks.py:53-57
     AFQ_TRY(orthonormalize_refresh(pb, st, s));
     // prop/blocks.py:59-79
-    { AFQ_PHASE("green", s);
-    AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
-                         nullptr, ws.step.green, s)); }
-    { AFQ_PHASE("energy", s);
-    AFQ_TRY(launch_energy(W, n, o, G, pb->h0, ws.step.green, pb->rot_chol, d->trial_is_real,
-                          (const double2*)pb->rot_h1, ws.partial, ws.energy, s)); }
+    AFQ_TRY(energy_impl(pb, st, ws, s));
     { AFQ_PHASE("block_measure", s);
     AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
                                  st->pop_control_ene_shift, block_energy, block_weight, s)); }

@@ -1,6 +1,7 @@
 // Internal declarations shared by the engine's translation units.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -82,6 +83,29 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// -------------------------------------------- bf16 hi/lo split operands --
+// x = hi + lo with hi = bf16(x), lo = bf16(x - hi).  A row of a split
+// operand holds three K sections starting at 0, S and 2S (S >= K), zero
+// after 3S up to the row length Kt (a multiple of 64): a left (A) operand
+// stores [hi hi lo], a right (B) operand [hi lo hi], so that A . B^T sums
+// a_hi b_hi + a_hi b_lo + a_lo b_hi.
+__device__ __forceinline__ void split_store3(__nv_bfloat16* row, int S, int k, double x, bool left) {
+    const __nv_bfloat16 hi = __double2bfloat16(x);
+    const __nv_bfloat16 lo = __double2bfloat16(x - (double)__bfloat162float(hi));
+    row[k] = hi;
+    row[S + k] = left ? hi : lo;
+    row[2 * S + k] = left ? lo : hi;
+}
+
+// Destination of a split left operand written by a per-walker kernel: walker
+// w's real parts go to row w, its imaginary parts to row W + w.
+struct SplitOut {
+    __nv_bfloat16* ptr = nullptr;
+    int W = 0;
+    long long ld = 0;  // row length Kt
+    int S = 0;         // section stride
+};
+
 // ------------------------------------------------------------- workspace --
 // Bump allocator over a caller-provided workspace; every region is aligned
 // to 256 bytes.  With base == nullptr it only measures.
@@ -151,5 +175,27 @@ size_t sr_levels_size(int W);
 // k_tc_gemm.cu : C (M x N fp32) = A (M x K bf16) . B (N x K bf16)^T on tcgen05
 int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                       long long ldc, int* err, cudaStream_t s);
+
+// k_walker.cu : Green's function with an optional split (bf16) output
+int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s);
+size_t energy_partial_count(int W, int o, int G);
+int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const double2* green, const double2* rot_h1,
+                         const double2* partial, double2* energy, cudaStream_t s);
+
+// k_mixed.cu
+int launch_split_rows(long long rows, int K, int S, int Kt, const double* src, long long rs, long long ks,
+                      __nv_bfloat16* dst, int left, cudaStream_t s);
+int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s);
+int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
+                             const double2* mf, __nv_bfloat16* av, int S, int Kt, double2* shift_term,
+                             double2* fb_term, cudaStream_t s);
+int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
+                         long long ldv, const double2* win, double2* wout, cudaStream_t s);
+int exchange_chunks(int G);
+int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
+int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, cudaStream_t s);
+
+inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 
 }  // namespace afq

@@ -25,7 +25,7 @@ template <bool CR>
 __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __restrict__ mo,
                                                const double2* __restrict__ walkers,
                                                double2* __restrict__ ovlp_out,
-                                               double2* __restrict__ green_out) {
+                                               double2* __restrict__ green_out, SplitOut split) {
     extern __shared__ double2 sm[];
     double2* m = sm;          // o x o
     double2* inv = sm + o * o;  // o x o
@@ -107,30 +107,51 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
         __syncthreads();
     }
     if (ovlp_out && tid == 0) ovlp_out[w] = cmul(s_det, s_det);
-    if (!green_out) return;
+    if (!green_out && !split.ptr) return;
     // G_half[b, i] = sum_a W[i, a] inv[a, b]
-    double2* Gp = green_out + (size_t)w * o * n;
+    double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
+    __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
+    __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
     for (int e = tid; e < n * o; e += blockDim.x) {
         int b = e / n, i = e % n;
         double2 acc = make_double2(0.0, 0.0);
         for (int a = 0; a < o; ++a) cfma(acc, Wp[i * o + a], inv[a * o + b]);
-        Gp[e] = acc;
+        if (Gp) Gp[e] = acc;
+        if (re_row) {
+            split_store3(re_row, split.S, e, acc.x, true);
+            split_store3(im_row, split.S, e, acc.y, true);
+        }
+    }
+    if (re_row) {  // zero the section gaps and the tail of the row
+        for (int e = n * o + tid; e < split.S; e += blockDim.x) {
+            split_store3(re_row, split.S, e, 0.0, true);
+            split_store3(im_row, split.S, e, 0.0, true);
+        }
+        for (long long e = 3LL * split.S + tid; e < split.ld; e += blockDim.x) {
+            re_row[e] = __double2bfloat16(0.0);
+            im_row[e] = __double2bfloat16(0.0);
+        }
     }
 }
 
-int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
-                 double2* ovlp_out, double2* green_out, cudaStream_t s) {
+int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     size_t smem = 2 * (size_t)o * o * sizeof(double2);
     if (trial_real) {
         AFQ_TRY(set_smem(k_green<true>, smem));
-        k_green<true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out);
+        k_green<true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split);
     } else {
         AFQ_TRY(set_smem(k_green<false>, smem));
-        k_green<false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out);
+        k_green<false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split);
     }
     AFQ_LAUNCHED("k_green");
     return AFQ_OK;
+}
+
+int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                 double2* ovlp_out, double2* green_out, cudaStream_t s) {
+    return launch_green_split(W, n, o, mo, trial_real, walkers, ovlp_out, green_out, SplitOut{}, s);
 }
 
 // =====================================================================
@@ -501,6 +522,11 @@ int launch_energy(int W, int n, int o, int G, double h0, const double2* green, c
         k_energy_partial<false><<<grid, EN_THREADS, smem, s>>>(n, o, G, ng, green, rot_chol, partial);
     }
     AFQ_LAUNCHED("k_energy_partial");
+    return launch_energy_finish(W, n, o, nchunk, h0, green, rot_h1, partial, energy, s);
+}
+
+int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const double2* green, const double2* rot_h1,
+                         const double2* partial, double2* energy, cudaStream_t s) {
     k_energy_finish<<<(W + 7) / 8, 256, 0, s>>>(W, n, o, nchunk, h0, green, rot_h1, partial, energy);
     AFQ_LAUNCHED("k_energy_finish");
     return AFQ_OK;

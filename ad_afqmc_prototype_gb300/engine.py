@@ -297,6 +297,31 @@ class Problem:
                            ptr(self.lowp) if self.lowp is not None else None)
 
 
+def prepare_lowp(n_walkers: int, norb: int, nocc: int, nchol: int, chol: torch.Tensor,
+                 rot_chol: torch.Tensor) -> torch.Tensor:
+    """bf16 hi/lo split copies of chol and rot_chol in tensor-core operand
+    order, for the mixed-precision step (real trial orbitals only)."""
+    if rot_chol.is_complex():
+        raise ValueError("the mixed-precision form supports real trial orbitals only")
+    d = make_dims(n_walkers, norb, nocc, nchol, True, _lib.AFQ_PREC_MIXED)
+    lib = _lib.load()
+    nb = int(lib.afq_lowp_bytes(ctypes.byref(d)))
+    buf = torch.empty((nb,), dtype=torch.uint8, device=chol.device)
+    _lib.call("afq_prepare_lowp", ctypes.byref(d), ptr(chol), ptr(rot_chol), ptr(buf), nb, stream_ptr())
+    return buf
+
+
+def workspace_status():
+    """Reads and clears the device status word of the step / block workspace
+    (synchronises the stream); raises EngineError if a bounded wait expired."""
+    b = _arena.buf.get(torch.cuda.current_device())
+    if b is None:
+        return 0
+    v = ctypes.c_int32(0)
+    _lib.call("afq_workspace_status", ptr(b), ctypes.byref(v), stream_ptr())
+    return v.value
+
+
 def make_params(params, n_prop_steps: Optional[int] = None) -> afq_params:
     return afq_params(float(params.dt), float(params.pop_control_damping), float(params.weight_floor),
                       float(params.weight_cap), float(params.shift_ema), int(params.n_exp_terms),

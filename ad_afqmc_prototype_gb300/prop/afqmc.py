@@ -65,12 +65,22 @@ def engine_problem(*, params, ham_data, trial_data, meas_ops, prop_ops, prop_ctx
     prec = _PREC.get(str(getattr(params, "precision", "fp64")).lower())
     if prec is None:
         raise ValueError(f"unknown precision {params.precision!r}; expected 'fp64' or 'mixed'")
+    lowp = None
+    if prec == _lib.AFQ_PREC_MIXED:
+        # cached on the measurement context: it depends on chol and rot_chol only
+        cached = getattr(meas_ctx, "_lowp", None)
+        if cached is None or cached[0] is not ham_data.chol or cached[1] < n_walkers:
+            buf = engine.prepare_lowp(n_walkers, trial_data.norb, trial_data.nocc, int(ham_data.chol.shape[0]),
+                                      ham_data.chol, meas_ctx.rot_chol)
+            cached = (ham_data.chol, n_walkers, buf)
+            object.__setattr__(meas_ctx, "_lowp", cached)
+        lowp = cached[2]
     return engine.Problem(
         n_walkers=n_walkers, norb=trial_data.norb, nocc=trial_data.nocc, nchol=int(ham_data.chol.shape[0]),
         trial_is_real=trial_data.is_real, h0=ham_data.h0, chol=ham_data.chol, mo=trial_data.mo_coeff,
         dt=float(prop_ctx.dt), sqrt_dt=float(prop_ctx.sqrt_dt), exp_h1_half=prop_ctx.exp_h1_half,
         mf_shifts=prop_ctx.mf_shifts, h0_prop=complex(prop_ctx.h0_prop.item()), rot_h1=meas_ctx.rot_h1,
-        rot_chol=meas_ctx.rot_chol, precision=prec)
+        rot_chol=meas_ctx.rot_chol, precision=prec, lowp=lowp)
 
 
 def device_state(state: prop_state, inplace: bool) -> engine.DeviceState:

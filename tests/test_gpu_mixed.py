@@ -1,0 +1,101 @@
+"""The mixed-precision form against the binary64 form, through the same API,
+from identical states and fields.  Tolerances: one step moves walkers by
+<= 1e-4 relative (bf16 hi/lo split products, ~2^-16); block energies agree
+to 1e-4 Ha (0.1 mHa, the accuracy target of the mixed form) and the
+energy kernel alone (a block of zero steps) to 1e-4 Ha as well."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(wl_name, W, precision, **pkw):
+    from ad_afqmc_prototype_gb300 import synth
+    from ad_afqmc_prototype_gb300.core.system import system
+    from ad_afqmc_prototype_gb300.ham.chol import ham_chol
+    from ad_afqmc_prototype_gb300.meas.rhf import make_rhf_meas_ops
+    from ad_afqmc_prototype_gb300.prop.afqmc import engine_problem, init_prop_state
+    from ad_afqmc_prototype_gb300.prop.chol_afqmc_ops import make_chol_afqmc_ops
+    from ad_afqmc_prototype_gb300.prop.types import afqmc_params
+    from ad_afqmc_prototype_gb300.trial.rhf import get_rdm1, make_rhf_trial_ops, rhf_trial
+    wl = synth.WORKLOADS[wl_name]
+    H = synth.make_workload(wl)
+    n, o = wl.nbasis, wl.nocc
+    sys_ = system(norb=n, nelec=(o, o), walker_kind="restricted")
+    ham = ham_chol(h0=H["h0"], h1=H["h1"], chol=H["chol"])
+    trial = rhf_trial(H["mo_coeff"])
+    t_ops, m_ops = make_rhf_trial_ops(sys_), make_rhf_meas_ops(sys_)
+    p_ops = make_chol_afqmc_ops(ham, "restricted")
+    params = afqmc_params(dt=0.005, precision=precision, **pkw)
+    pctx = p_ops.build_prop_ctx(get_rdm1(trial), params.dt)
+    mctx = m_ops.build_meas_ctx(ham, trial)
+    st = init_prop_state(sys=sys_, n_walkers=W, seed=1, ham_data=ham, trial_ops_=t_ops, trial_data=trial,
+                         meas_ops=m_ops, initial_walkers=synth.trial_walkers(H["mo_coeff"], W))
+    kw = dict(params=params, ham_data=ham, trial_data=trial, meas_ops=m_ops, prop_ops=p_ops, prop_ctx=pctx,
+              meas_ctx=mctx)
+    return engine_problem(n_walkers=W, need_energy=True, **kw), params, st
+
+
+def _dstate(st):
+    from ad_afqmc_prototype_gb300.prop.afqmc import device_state
+    return device_state(st, inplace=False)
+
+
+@pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 64), ("c1_n12_o6_g48_w256", 100)])
+def test_mixed_step_close_to_fp64(cuda, wl, W):
+    from ad_afqmc_prototype_gb300 import engine
+    pa, pra, st = _setup(wl, W, "fp64")
+    pb, prb, _ = _setup(wl, W, "mixed")
+    a, b = _dstate(st), _dstate(st)
+    G = pa.nchol
+    for k in range(3):
+        f = engine.fill_normal((W, G), 3, k)
+        engine.step(pa, pra, a, 0, 0, fields=f)
+        engine.step(pb, prb, b, 0, 0, fields=f)
+    assert engine.workspace_status() == 0
+    rel = float(((a.walkers - b.walkers).abs().max() / a.walkers.abs().max()).item())
+    assert rel < 1e-4, rel
+    relw = float(((a.weights - b.weights).abs() / a.weights.abs().clamp_min(1e-300)).max().item())
+    assert relw < 1e-4, relw
+    relo = float(((a.overlaps - b.overlaps).abs() / a.overlaps.abs()).max().item())
+    assert relo < 1e-3, relo
+
+
+@pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 128), ("c4_n200_o30_g1000_w4096", 256)])
+def test_mixed_energy_kernel_close_to_fp64(cuda, wl, W):
+    """A block of zero steps is QR + energy + comb: isolates the energy GEMM."""
+    from ad_afqmc_prototype_gb300 import engine
+    pa, pra, st = _setup(wl, W, "fp64", n_prop_steps=3)
+    pb, prb, _ = _setup(wl, W, "mixed", n_prop_steps=3)
+    a = _dstate(st)
+    engine.block(pa, pra, a, 5, 0)  # move the walkers off the trial
+    z0a = pra.__class__(**{**pra.__dict__, "n_prop_steps": 0})
+    z0b = prb.__class__(**{**prb.__dict__, "n_prop_steps": 0})
+    x, y = engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)]), \
+        engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)])
+    ea, _ = engine.block(pa, z0a, x, 5, 100, zeta=0.5)
+    eb, _ = engine.block(pb, z0b, y, 5, 100, zeta=0.5)
+    assert engine.workspace_status() == 0
+    assert abs(float(ea) - float(eb)) < 1e-4, (float(ea), float(eb))
+
+
+def test_mixed_block_energy_error_per_block(cuda):
+    """From identical block-start states and fields: |E_mixed - E_fp64| per
+    10-step block (QR after step 5) within 0.1 mHa."""
+    from ad_afqmc_prototype_gb300 import engine
+    W = 512
+    pa, pra, st = _setup("c4_n200_o30_g1000_w4096", W, "fp64", n_prop_steps=10, qr_every=5)
+    pb, prb, _ = _setup("c4_n200_o30_g1000_w4096", W, "mixed", n_prop_steps=10, qr_every=5)
+    ref = _dstate(st)
+    errs = []
+    for blk in range(3):
+        f = engine.fill_normal((10, W, pa.nchol), 9, blk)
+        b = engine.DeviceState(*[t.clone() for t in (ref.walkers, ref.weights, ref.overlaps, ref.pop_shift,
+                                                      ref.e_estimate)])
+        ea, wa = engine.block(pa, pra, ref, 0, 0, fields=f, zeta=0.25)
+        eb, wb = engine.block(pb, prb, b, 0, 0, fields=f, zeta=0.25)
+        errs.append(abs(float(ea) - float(eb)))
+    assert engine.workspace_status() == 0
+    print("per-block |dE| (Ha):", errs)
+    assert max(errs) < 1e-4, errs
