@@ -71,6 +71,7 @@ _SIGS = {
     "afq_orthogonalize": (c_int32, [POINTER(afq_dims), P, P, P, P]),
     "afq_sr_workspace": (c_size_t, [c_int32]),
     "afq_sr_indices": (c_int32, [c_int32, P, c_double, P, P, P, c_size_t, P]),
+    "afq_sr_indices_static": (c_int32, [c_int32, P, c_double, P, P, P]),
     "afq_stochastic_reconfiguration": (c_int32, [POINTER(afq_dims), P, c_double, P, P, P, P, P,
                                                  c_size_t, P]),
     "afq_fill_normal": (c_int32, [c_int64, c_uint64, c_uint64, P, P]),

@@ -189,6 +189,19 @@ size_t afq_sr_workspace(int32_t n_walkers);
 int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_t* idx,
                    double* cumsum, void* workspace, size_t workspace_bytes, void* stream);
 
+/* afq_sr_indices without a workspace.  No counterpart in the reference: it is
+ * for callers that cannot give this library device memory -- a plug-in
+ * inside a process whose runtime already reserved the GPU's memory for its own
+ * pool (JAX does so by default), or a thin FFI binding with no device
+ * allocator.  The scan's scratch is a file-scope device array of 1 MiB per GPU
+ * (held until the process exits); at most 65536 walkers, larger calls return
+ * AFQ_E_UNSUPPORTED.  All calls on a device share that array: calls that
+ * overlap on the GPU race, so order them on one stream.  The first call on
+ * each device looks the array up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  Allocates nothing. */
+int afq_sr_indices_static(int32_t n_walkers, const double* weights, double zeta, int32_t* idx,
+                          double* cumsum, void* stream);
+
 /* stochastic_reconfiguration (walkers.py:243-265): walkers_out[k] =
  * walkers[idx[k]], weights_out = sum|w| / W.  walkers_out must not alias
  * walkers.  idx (optional) receives the indices. */
