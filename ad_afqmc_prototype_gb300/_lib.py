@@ -57,7 +57,7 @@ _SIGS = {
     "afq_build_meas_ctx": (c_int32, [c_int32, c_int32, c_int32, P, P, P, c_int32, P, P, P]),
     "afq_lowp_bytes": (c_size_t, [POINTER(afq_dims)]),
     "afq_prepare_lowp": (c_int32, [POINTER(afq_dims), P, P, P, c_size_t, P]),
-    "afq_lowp_gemm_tn": (c_int32, [c_int32, c_int32, c_int32, P, c_int64, P, c_int64, P, c_int64, P, P]),
+    "afq_lowp_gemm_tn": (c_int32, [c_int32, c_int32, c_int32, P, c_int64, P, c_int64, P, c_int64, P, c_int32, P]),
     "afq_workspace_status": (c_int32, [P, POINTER(c_int32), P]),
     "afq_overlap": (c_int32, [POINTER(afq_dims), P, P, P, P]),
     "afq_half_green": (c_int32, [POINTER(afq_dims), P, P, P, P, P]),

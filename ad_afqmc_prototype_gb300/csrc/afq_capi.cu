@@ -70,11 +70,11 @@ static LowpDims lowp_dims(const afq_dims* d) {
     LowpDims L;
     const int n = d->norb, o = d->nocc, G = d->nchol;
     L.S_V = G;
-    L.Kt_V = (int)round_up(3LL * G, 64);
+    L.Kt_V = (int)round_up((long long)kSplit * G, 64);
     L.S_F = o * n;
-    L.Kt_F = (int)round_up(3LL * o * n, 64);
+    L.Kt_F = (int)round_up((long long)kSplit * o * n, 64);
     L.S_E = n;
-    L.Kt_E = (int)round_up(3LL * n, 64);
+    L.Kt_E = (int)round_up((long long)kSplit * n, 64);
     L.ldv = round_up((long long)n * n, 4);
     return L;
 }
@@ -232,8 +232,22 @@ static int check_problem(const afq_problem* pb) {
 // The mixed-precision step (AFQ_PREC_MIXED): same sequence as step_impl,
 // with the force bias and V-build on tensor cores and the Taylor series in
 // fp32 products accumulated into the binary64 walkers.
+// Destination of the force-bias operand (split G_half) in a mixed workspace.
+static SplitOut fb_split(const afq_dims* d, const StepWS& ws) {
+    const LowpDims L = lowp_dims(d);
+    SplitOut so;
+    so.ptr = ws.Ag;
+    so.W = d->n_walkers;
+    so.ld = L.Kt_F;
+    so.S = L.S_F;
+    return so;
+}
+
+// green_ready: ws.Ag already holds the split G_half of the current walkers
+// (written by the previous step's overlap kernel or by the overlap refresh
+// after a QR inside the same block).
 static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
-                      const StepWS& ws, cudaStream_t s) {
+                      const StepWS& ws, bool green_ready, cudaStream_t s) {
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const LowpDims L = lowp_dims(d);
@@ -242,17 +256,12 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     const double2* mo = (const double2*)pb->mo_coeff;
     double2* walk = (double2*)st->walkers;
     // force bias: G_half split straight from the Green's function kernel
-    {
+    if (!green_ready) {
         AFQ_PHASE("green", s);
-        SplitOut so;
-        so.ptr = ws.Ag;
-        so.W = W;
-        so.ld = L.Kt_F;
-        so.S = L.S_F;
-        AFQ_TRY(launch_green_split(W, n, o, mo, 1, walk, nullptr, nullptr, so, s));
+        AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, nullptr, fb_split(d, ws), s));
     }
     { AFQ_PHASE("fb_gemm", s);
-      AFQ_TRY(launch_tc_gemm_tn(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s)); }
+      AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s)); }
     const int Wc = chunk_size(W, p->n_chunks);
     { AFQ_PHASE("field_shift", s);
       AFQ_TRY(launch_field_shift_mixed(W, G, Wc, pb->sqrt_dt, fields, ws.fbm, G, (const double2*)pb->mf_shifts, ws.Av,
@@ -261,13 +270,15 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     for (int w0 = 0; w0 < W; w0 += Wc) {
         const int wc = W - w0 < Wc ? W - w0 : Wc;
         { AFQ_PHASE("vbuild_gemm", s);
-          AFQ_TRY(launch_tc_gemm_tn(2 * wc, n * n, L.Kt_V, ws.Av + (size_t)2 * w0 * L.Kt_V, L.Kt_V, lb.Bv, L.Kt_V,
+          AFQ_TRY(launch_tc_gemm_tn_drain(2 * wc, n * n, L.Kt_V, ws.Av + (size_t)2 * w0 * L.Kt_V, L.Kt_V, lb.Bv, L.Kt_V,
                                     ws.Vm, L.ldv, ws.status, s)); }
         { AFQ_PHASE("trotter", s);
           AFQ_TRY(launch_trotter_mixed(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.emi, ws.Vm, L.ldv,
                                        walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, s)); }
     }
-    { AFQ_PHASE("overlap", s); AFQ_TRY(launch_green(W, n, o, mo, 1, walk, ws.ovl_new, nullptr, s)); }
+    // overlaps, and the next step's force-bias operand from the same factorisation
+    { AFQ_PHASE("overlap", s);
+      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s)); }
     AFQ_PHASE("weight_update", s);
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
@@ -293,9 +304,11 @@ static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS
     for (int w0 = 0; w0 < W; w0 += We) {
         const int wc = W - w0 < We ? W - w0 : We;
         AFQ_TRY(launch_green_rows(wc, n, o, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, s));
-        AFQ_TRY(launch_tc_gemm_tn(G * o, 2 * o * wc, L.Kt_E, lb.Le, L.Kt_E, ws.Bg, L.Kt_E, ws.F, 2LL * o * wc,
+        // F[(w, part, k), (g, i)]: the sections of Bg ([hi lo hi]) and Le
+        // ([hi hi lo]) still pair up as hi.hi + lo.hi + hi.lo
+        AFQ_TRY(launch_tc_gemm_tn_drain(2 * o * wc, G * o, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.F, (long long)G * o,
                                   ws.step.status, s));
-        AFQ_TRY(launch_exchange_reduce(wc, G, o, ws.F, 2LL * o * wc, partial + (size_t)w0 * nch * 2, s));
+        AFQ_TRY(launch_exchange_reduce(wc, G, o, ws.F, (long long)G * o, partial + (size_t)w0 * nch * 2, s));
     }
     return launch_energy_finish(W, n, o, nch, pb->h0, ws.green, (const double2*)pb->rot_h1, partial, ws.energy, s);
 }
@@ -319,7 +332,7 @@ static int check_params(const afq_params* p) {
 }
 
 static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
-                     uint64_t seed, uint64_t counter, const StepWS& ws, cudaStream_t s) {
+                     uint64_t seed, uint64_t counter, const StepWS& ws, cudaStream_t s, bool green_ready = false) {
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const double2* mo = (const double2*)pb->mo_coeff;
@@ -329,7 +342,7 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
         AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
         fields = ws.fields;
     }
-    if (d->precision == AFQ_PREC_MIXED) return step_mixed(pb, p, st, fields, ws, s);
+    if (d->precision == AFQ_PREC_MIXED) return step_mixed(pb, p, st, fields, ws, green_ready, s);
     // force bias (prop/afqmc.py:90-95)
     { AFQ_PHASE("green", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s)); }
     { AFQ_PHASE("fb_gemm", s); AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s)); }
@@ -349,11 +362,17 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
                                 st->pop_control_ene_shift, st->e_estimate, s);
 }
 
-static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s) {
+// QR and overlap refresh (prop/blocks.py:53-57); in the mixed form the same
+// kernel also writes the next step's force-bias operand into ws->Ag.
+static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s,
+                                  const StepWS* ws = nullptr) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
     { AFQ_PHASE("qr", s); AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s)); }
     AFQ_PHASE("overlap", s);
+    if (ws && d->precision == AFQ_PREC_MIXED)
+        return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
+                                    (double2*)st->overlaps, fb_split(d, *ws), s);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
                         (double2*)st->overlaps, nullptr, s);
 }
@@ -433,10 +452,12 @@ int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* 
 }
 
 int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B, int64_t ldb,
-                     float* C, int64_t ldc, int32_t* err, void* stream) {
+                     float* C, int64_t ldc, int32_t* err, int32_t accumulate, void* stream) {
     AFQ_NOTNULL(A); AFQ_NOTNULL(B); AFQ_NOTNULL(C); AFQ_NOTNULL(err);
     if (M < 0 || N < 0 || lda < K || ldb < K || ldc < N)
         return fail(AFQ_E_INVALID_ARGUMENT, "lowp gemm: bad sizes M=%d N=%d K=%d", M, N, K);
+    if (accumulate == 1) return launch_tc_gemm_tn_drain(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
+    if (accumulate != 0) return fail(AFQ_E_INVALID_ARGUMENT, "accumulate=%d must be 0 or 1", accumulate);
     return launch_tc_gemm_tn(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
 }
 
@@ -707,9 +728,11 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
     const size_t fstride = (size_t)W * G;
     // prop/blocks.py:38-51
     for (int st_i = 0; st_i < p->n_prop_steps; ++st_i) {
-        AFQ_TRY(step_impl(pb, p, st, fields ? fields + st_i * fstride : nullptr, seed, counter + st_i, ws.step, s));
+        // from the second step on, the previous overlap kernel left the force-bias operand
+        AFQ_TRY(step_impl(pb, p, st, fields ? fields + st_i * fstride : nullptr, seed, counter + st_i, ws.step, s,
+                          st_i > 0));
         if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps)
-            AFQ_TRY(orthonormalize_refresh(pb, st, s));
+            AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));
     }
     // prop/blocks.py:53-57
     AFQ_TRY(orthonormalize_refresh(pb, st, s));

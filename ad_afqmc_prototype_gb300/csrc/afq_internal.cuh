@@ -84,17 +84,51 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // -------------------------------------------- bf16 hi/lo split operands --
-// x = hi + lo with hi = bf16(x), lo = bf16(x - hi).  A row of a split
-// operand holds three K sections starting at 0, S and 2S (S >= K), zero
-// after 3S up to the row length Kt (a multiple of 64): a left (A) operand
-// stores [hi hi lo], a right (B) operand [hi lo hi], so that A . B^T sums
-// a_hi b_hi + a_hi b_lo + a_lo b_hi.
-__device__ __forceinline__ void split_store3(__nv_bfloat16* row, int S, int k, double x, bool left) {
-    const __nv_bfloat16 hi = __double2bfloat16(x);
-    const __nv_bfloat16 lo = __double2bfloat16(x - (double)__bfloat162float(hi));
-    row[k] = hi;
-    row[S + k] = left ? hi : lo;
-    row[2 * S + k] = left ? lo : hi;
+// x = h + m + l with h = bf16(x), m = bf16(x - h), l = bf16(x - h - m):
+// three bf16 pieces carry 24 significant bits (an fp32 value exactly).  A row
+// of a split operand holds kSplit K sections starting at 0, S, 2S, ... (S >= K)
+// and is zero from kSplit*S up to its length Kt (a multiple of 64): a left (A)
+// operand stores [h h m h l m], a right (B) operand [h m h l h m], so that
+// A . B^T sums hh + hm + mh + hl + lh + mm -- every product above 2^-24
+// relative.  (bf16 has 8 significant bits, so a two-piece split would keep
+// only ~16 bits.)
+constexpr int kSplit = 6;
+
+template <class T>
+__device__ __forceinline__ void split_pieces(T x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l);
+template <>
+__device__ __forceinline__ void split_pieces<double>(double x, __nv_bfloat16& h, __nv_bfloat16& m,
+                                                     __nv_bfloat16& l) {
+    h = __double2bfloat16(x);
+    const double r1 = x - (double)__bfloat162float(h);
+    m = __double2bfloat16(r1);
+    l = __double2bfloat16(r1 - (double)__bfloat162float(m));
+}
+template <>
+__device__ __forceinline__ void split_pieces<float>(float x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+    h = __float2bfloat16(x);
+    const float r1 = x - __bfloat162float(h);  // exact
+    m = __float2bfloat16(r1);
+    l = __float2bfloat16(r1 - __bfloat162float(m));  // exact
+}
+
+template <class T>
+__device__ __forceinline__ void split_store_t(__nv_bfloat16* row, int S, int k, T x, bool left) {
+    __nv_bfloat16 h, m, l;
+    split_pieces<T>(x, h, m, l);
+    row[k] = h;
+    row[S + k] = left ? h : m;
+    row[2 * S + k] = left ? m : h;
+    row[3 * S + k] = left ? h : l;
+    row[4 * S + k] = left ? l : h;
+    row[5 * S + k] = m;
+}
+__device__ __forceinline__ void split_store(__nv_bfloat16* row, int S, int k, double x, bool left) {
+    split_store_t<double>(row, S, k, x, left);
+}
+// Same split of an fp32 value, on the fp32 pipe.
+__device__ __forceinline__ void split_storef(__nv_bfloat16* row, int S, int k, float x, bool left) {
+    split_store_t<float>(row, S, k, x, left);
 }
 
 // Destination of a split left operand written by a per-walker kernel: walker
@@ -175,6 +209,10 @@ size_t sr_levels_size(int W);
 // k_tc_gemm.cu : C (M x N fp32) = A (M x K bf16) . B (N x K bf16)^T on tcgen05
 int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                       long long ldc, int* err, cudaStream_t s);
+// Same product with the K sum formed in fp32 registers per 64-wide K block
+// (round-to-nearest) instead of in the tensor cores' truncating accumulator.
+int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                            long long ldc, int* err, cudaStream_t s);
 
 // k_walker.cu : Green's function with an optional split (bf16) output
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
@@ -192,6 +230,8 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
                              double2* fb_term, cudaStream_t s);
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
                          long long ldv, const double2* win, double2* wout, cudaStream_t s);
+int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
+                         SplitOut split, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
 int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, cudaStream_t s);

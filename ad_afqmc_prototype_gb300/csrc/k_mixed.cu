@@ -25,8 +25,8 @@ __global__ void k_split_rows(long long rows, int K, int S, int Kt, const double*
         __nv_bfloat16* row = dst + r * Kt;
         if (kk < S) {
             const double x = kk < K ? src[r * rs + (long long)kk * ks] : 0.0;
-            split_store3(row, S, kk, x, left != 0);
-        } else if (kk >= 3 * S) {
+            split_store(row, S, kk, x, left != 0);
+        } else if (kk >= kSplit * S) {
             row[kk] = __double2bfloat16(0.0);
         }
     }
@@ -79,18 +79,18 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
             const double xv = x[(size_t)w * G + g];
             const double2 fs = make_double2(-sqrt_dt * (-f.y - m.x), -sqrt_dt * (f.x - m.y));
             const double2 xt = make_double2(xv - fs.x, -fs.y);
-            split_store3(re_row, S, g, xt.x, true);
-            split_store3(im_row, S, g, xt.y, true);
+            split_store(re_row, S, g, xt.x, true);
+            split_store(im_row, S, g, xt.y, true);
             sr += xt.x * m.x - xt.y * m.y;
             si += xt.x * m.y + xt.y * m.x;
             br += xv * fs.x - 0.5 * (fs.x * fs.x - fs.y * fs.y);
             bi += xv * fs.y - 0.5 * (2.0 * fs.x * fs.y);
         } else {
-            split_store3(re_row, S, g, 0.0, true);
-            split_store3(im_row, S, g, 0.0, true);
+            split_store(re_row, S, g, 0.0, true);
+            split_store(im_row, S, g, 0.0, true);
         }
     }
-    for (int k = 3 * S + lane; k < Kt; k += 32) {
+    for (int k = kSplit * S + lane; k < Kt; k += 32) {
         re_row[k] = __double2bfloat16(0.0);
         im_row[k] = __double2bfloat16(0.0);
     }
@@ -118,7 +118,10 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
 // only at its own entries (so walkers_out may alias walkers_in):
 //   W1 = W + (E-I) W;  out = W1 + sum_k (i sqrt_dt V)^k / k! W1;
 //   W' = out + (E-I) out.
-constexpr int TM_THREADS = 256, TM_CC = 4, TM_BJ = 16;
+constexpr int TM_THREADS = 512, TM_CC = 4, TM_BJ = 16;
+// Row stride of the staged operand: odd, so the four row groups of a warp
+// read four different banks.
+constexpr int TM_MS = TM_BJ + 1;
 
 template <int OC, int NR, bool REAL_M>
 __device__ __forceinline__ void tm_matmul(int n, const float* __restrict__ Mr, const float* __restrict__ Mi,
@@ -135,8 +138,8 @@ __device__ __forceinline__ void tm_matmul(int n, const float* __restrict__ Mr, c
         for (int e = threadIdx.x; e < n * TM_BJ; e += TM_THREADS) {
             const int i = e / TM_BJ, jj = e % TM_BJ;
             const size_t src = (size_t)i * n + j0 + jj;
-            if (REAL_M) Msr[e] = jj < jn ? Mr[src] : 0.f;
-            else Ms[e] = jj < jn ? make_float2(Mr[src], Mi[src]) : make_float2(0.f, 0.f);
+            if (REAL_M) Msr[i * TM_MS + jj] = jj < jn ? Mr[src] : 0.f;
+            else Ms[i * TM_MS + jj] = jj < jn ? make_float2(Mr[src], Mi[src]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
         for (int jj = 0; jj < jn; ++jj) {
@@ -149,14 +152,14 @@ __device__ __forceinline__ void tm_matmul(int n, const float* __restrict__ Mr, c
                 const int i = rg + RG * q;
                 if (i < n) {
                     if (REAL_M) {
-                        const float m = Msr[i * TM_BJ + jj];
+                        const float m = Msr[i * TM_MS + jj];
 #pragma unroll
                         for (int j = 0; j < TM_CC; ++j) {
                             acc[q][j].x = fmaf(m, t[j].x, acc[q][j].x);
                             acc[q][j].y = fmaf(m, t[j].y, acc[q][j].y);
                         }
                     } else {
-                        const float2 m = Ms[i * TM_BJ + jj];
+                        const float2 m = Ms[i * TM_MS + jj];
 #pragma unroll
                         for (int j = 0; j < TM_CC; ++j) {
                             acc[q][j].x = fmaf(m.x, t[j].x, acc[q][j].x);
@@ -280,7 +283,7 @@ static int trotter_mixed_oc(int wc, int n, int o, int n_terms, double sqrt_dt, c
                             long long ldv, const double2* win, double2* wout, cudaStream_t s) {
     constexpr int RG = TM_THREADS / (OC / TM_CC);
     const int nr = (n + RG - 1) / RG;
-    const size_t smem = (size_t)n * (OC + TM_BJ) * sizeof(float2);
+    const size_t smem = (size_t)n * (OC + TM_MS) * sizeof(float2);
     dim3 grid((o + OC - 1) / OC, wc);
 #define AFQ_TM(NRV)                                                                                    \
     do {                                                                                               \
@@ -291,8 +294,6 @@ static int trotter_mixed_oc(int wc, int n, int o, int n_terms, double sqrt_dt, c
     if (nr <= 1) AFQ_TM(1);
     else if (nr <= 2) AFQ_TM(2);
     else if (nr <= 4) AFQ_TM(4);
-    else if (nr <= 8) AFQ_TM(8);
-    else if (nr <= 16) AFQ_TM(16);
     else return fail(AFQ_E_UNSUPPORTED, "mixed trotter: norb=%d too large", n);
 #undef AFQ_TM
     AFQ_LAUNCHED("k_trotter_mixed");
@@ -303,26 +304,262 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
                          long long ldv, const double2* win, double2* wout, cudaStream_t s) {
     if (wc <= 0) return AFQ_OK;
     if (wc > 65535) return fail(AFQ_E_UNSUPPORTED, "mixed trotter: chunk of %d walkers > 65535", wc);
-    if (o <= 16) return trotter_mixed_oc<16>(wc, n, o, n_terms, sqrt_dt, emi, vm, ldv, win, wout, s);
+    // 32 columns per CTA keep a walker's V read once per term; above 256
+    // orbitals 16 columns keep the per-thread tile at <= 4 rows (no spills)
+    if (o <= 16 || n > 256) return trotter_mixed_oc<16>(wc, n, o, n_terms, sqrt_dt, emi, vm, ldv, win, wout, s);
     return trotter_mixed_oc<32>(wc, n, o, n_terms, sqrt_dt, emi, vm, ldv, win, wout, s);
+}
+
+// ------------------------------------------- overlap + force-bias operand
+// Mixed-form replacement of k_green for the overlap (meas/rhf.py:22-24) and
+// the next step's force-bias operand (meas/rhf.py:15-19, 27-33):
+//   m = C^H W in binary64; LU with partial pivoting in binary64 gives
+//   det(m) and the overlap det(m)^2 -- the only binary64 work;
+//   m^-1 by fp32 Gauss-Jordan on a float copy of m, and
+//   G_half^T = W m^-1 in fp32, written as the bf16 hi/lo split operand
+//   (which resolves ~2^-17, so fp32 here costs no accuracy downstream).
+// Pivot reciprocals are computed once per pivot and shared through shared
+// memory.  Real trial orbitals (the mixed form requires them).
+template <int MA, bool STAGE_W>
+__global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const double2* __restrict__ mo,
+                                                       const double2* __restrict__ walkers,
+                                                       double2* __restrict__ ovlp_out, SplitOut split) {
+    extern __shared__ double2 smd[];
+    double2* m = smd;                              // o x o binary64 (LU in place)
+    float2* mf = (float2*)(m + o * o);             // o x o fp32 copy -> Gauss-Jordan
+    float2* invf = mf + o * o;                     // o x o fp32 inverse
+    float2* wf = invf + o * o;                     // n x o fp32 copy of W
+    __shared__ int s_piv;
+    __shared__ double2 s_rp;
+    __shared__ float2 s_rpf;
+    __shared__ double2 s_det;
+    const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const double2* Wp = walkers + (size_t)w * n * o;
+
+    {  // m (binary64) and the fp32 copy of W
+        const int AG = blockDim.x / o;
+        const int b = tid % o, ag = tid / o;
+        double2 acc[MA];
+#pragma unroll
+        for (int k = 0; k < MA; ++k) acc[k] = make_double2(0.0, 0.0);
+        if (ag < AG) {
+            for (int i = 0; i < n; ++i) {
+                const double2 x = Wp[(size_t)i * o + b];
+                if (STAGE_W && ag == 0) wf[i * o + b] = make_float2((float)x.x, (float)x.y);
+#pragma unroll
+                for (int k = 0; k < MA; ++k) {
+                    const int a = ag + AG * k;
+                    if (a < o) rfma(acc[k], mo[i * o + a].x, x);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < MA; ++k) {
+                const int a = ag + AG * k;
+                if (a < o) {
+                    m[a * o + b] = acc[k];
+                    mf[a * o + b] = make_float2((float)acc[k].x, (float)acc[k].y);
+                }
+            }
+        }
+        for (int e = tid; e < o * o; e += blockDim.x)
+            invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
+    }
+    if (tid == 0) s_det = make_double2(1.0, 0.0);
+    __syncthreads();
+
+    // binary64 LU with partial pivoting: det(m) only
+    for (int k = 0; k < o; ++k) {
+        if (wid == 0) {
+            double best = -1.0;
+            int bi = k;
+            for (int r = k + lane; r < o; r += 32) {
+                const double v = cabs2(m[r * o + k]);
+                if (v > best) { best = v; bi = r; }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) {
+                s_piv = bi;
+                const double2 piv = m[bi * o + k];
+                const double2 d = cmul(s_det, piv);
+                s_det = (bi != k) ? make_double2(-d.x, -d.y) : d;
+                s_rp = cdiv(make_double2(1.0, 0.0), piv);
+            }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (p != k)
+            for (int j = tid; j < o; j += blockDim.x) {
+                const double2 t = m[k * o + j];
+                m[k * o + j] = m[p * o + j];
+                m[p * o + j] = t;
+            }
+        __syncthreads();
+        const double2 rp = s_rp;
+        const int rem = o - k - 1;
+        for (int e = tid; e < rem * rem; e += blockDim.x) {
+            const int r = k + 1 + e / rem, j = k + 1 + e % rem;
+            const double2 l = cmul(m[r * o + k], rp);
+            m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && ovlp_out) ovlp_out[w] = cmul(s_det, s_det);
+
+    // fp32 Gauss-Jordan inverse of the copy
+    for (int k = 0; k < o; ++k) {
+        if (wid == 0) {
+            float best = -1.f;
+            int bi = k;
+            for (int r = k + lane; r < o; r += 32) {
+                const float2 v = mf[r * o + k];
+                const float a = v.x * v.x + v.y * v.y;
+                if (a > best) { best = a; bi = r; }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) {
+                s_piv = bi;
+                const float2 v = mf[bi * o + k];
+                const float den = v.x * v.x + v.y * v.y;
+                s_rpf = make_float2(v.x / den, -v.y / den);
+            }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (p != k)
+            for (int j = tid; j < 2 * o; j += blockDim.x) {
+                float2* X = j < o ? mf : invf;
+                const int jj = j < o ? j : j - o;
+                const float2 t = X[k * o + jj];
+                X[k * o + jj] = X[p * o + jj];
+                X[p * o + jj] = t;
+            }
+        __syncthreads();
+        const float2 rp = s_rpf;
+        for (int j = tid; j < 2 * o; j += blockDim.x) {
+            float2* X = j < o ? mf : invf;
+            const int jj = j < o ? j : j - o;
+            if (j < o && jj <= k) continue;
+            const float2 v = X[k * o + jj];
+            X[k * o + jj] = make_float2(v.x * rp.x - v.y * rp.y, v.x * rp.y + v.y * rp.x);
+        }
+        __syncthreads();
+        for (int e = tid; e < o * 2 * o; e += blockDim.x) {
+            const int r = e / (2 * o), j = e % (2 * o);
+            if (r == k) continue;
+            const float2 f = mf[r * o + k];
+            float2* X = j < o ? mf : invf;
+            const int jj = j < o ? j : j - o;
+            if (j < o && jj <= k) continue;
+            const float2 v = X[k * o + jj], x = X[r * o + jj];
+            X[r * o + jj] = make_float2(x.x - (f.x * v.x - f.y * v.y), x.y - (f.x * v.y + f.y * v.x));
+        }
+        __syncthreads();
+    }
+
+    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand
+    __nv_bfloat16* re_row = split.ptr + (size_t)w * split.ld;
+    __nv_bfloat16* im_row = split.ptr + (size_t)(split.W + w) * split.ld;
+    constexpr int BG = 8;
+    const int nbg = (o + BG - 1) / BG;
+    for (int t = tid; t < n * nbg; t += blockDim.x) {
+        const int i = t % n, bg = t / n;
+        float2 acc[BG];
+#pragma unroll
+        for (int j = 0; j < BG; ++j) acc[j] = make_float2(0.f, 0.f);
+        for (int a = 0; a < o; ++a) {
+            float2 x;
+            if (STAGE_W) {
+                x = wf[i * o + a];
+            } else {
+                const double2 v = Wp[(size_t)i * o + a];
+                x = make_float2((float)v.x, (float)v.y);
+            }
+#pragma unroll
+            for (int j = 0; j < BG; ++j) {
+                const int b = bg * BG + j;
+                if (b < o) {
+                    const float2 v = invf[a * o + b];
+                    acc[j].x = fmaf(x.x, v.x, acc[j].x); acc[j].x = fmaf(-x.y, v.y, acc[j].x);
+                    acc[j].y = fmaf(x.x, v.y, acc[j].y); acc[j].y = fmaf(x.y, v.x, acc[j].y);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < BG; ++j) {
+            const int b = bg * BG + j;
+            if (b < o) {
+                split_storef(re_row, split.S, b * n + i, acc[j].x, true);
+                split_storef(im_row, split.S, b * n + i, acc[j].y, true);
+            }
+        }
+    }
+    for (int e = n * o + tid; e < split.S; e += blockDim.x) {
+        split_storef(re_row, split.S, e, 0.f, true);
+        split_storef(im_row, split.S, e, 0.f, true);
+    }
+    for (long long e = (long long)kSplit * split.S + tid; e < split.ld; e += blockDim.x) {
+        re_row[e] = __float2bfloat16(0.f);
+        im_row[e] = __float2bfloat16(0.f);
+    }
+}
+
+int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
+                         SplitOut split, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
+    const size_t wbytes = (size_t)n * o * sizeof(float2);
+    const bool stage = base + wbytes <= 160 * 1024;  // else read W from global in the last loop
+    const size_t smem = base + (stage ? wbytes : 0);
+    const int ag = 256 / o, ma = (o + ag - 1) / ag;
+#define AFQ_OS(MAV)                                                                               \
+    do {                                                                                          \
+        if (stage) {                                                                              \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, true>, smem));                                 \
+            k_overlap_split<MAV, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split);  \
+        } else {                                                                                  \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, false>, smem));                                \
+            k_overlap_split<MAV, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split); \
+        }                                                                                         \
+    } while (0)
+    if (ma <= 1) AFQ_OS(1);
+    else if (ma <= 2) AFQ_OS(2);
+    else if (ma <= 4) AFQ_OS(4);
+    else if (ma <= 8) AFQ_OS(8);
+    else AFQ_OS(16);
+#undef AFQ_OS
+    AFQ_LAUNCHED("k_overlap_split");
+    return AFQ_OK;
 }
 
 // ------------------------------------------------------------------ energy
 // Mixed energy (meas/rhf.py:36-50) for a chunk of walkers: the tensor-core
-// GEMM produced F[(g, i), (w, part, k)] = sum_j L~[g, i, j] G_part[w, k, j]
-// (part 0 = Re, 1 = Im of G_half); this kernel forms, per walker and chunk of
+// GEMM produced F[(w, part, k), (g, i)] = sum_j G_part[w, k, j] L~[g, i, j]
+// (part 0 = Re, 1 = Im of G_half), so each walker's f_g blocks lie along
+// contiguous runs of a row; this kernel forms, per walker and chunk of
 // Cholesky vectors, sum_g c_g^2 and sum_g sum_ik f_g[i,k] f_g[k,i] in fp64.
 constexpr int EX_G = 8;  // Cholesky vectors per CTA
 __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const float* __restrict__ F, long long ldf,
                                                          double2* __restrict__ partial, int nchunk) {
-    extern __shared__ float2 fs[];  // EX_G x o x o complex
+    extern __shared__ float2 fs[];  // EX_G x o x o complex, fs[(g o + i) o + k] = f_g[i, k]
     const int w = blockIdx.y, g0 = blockIdx.x * EX_G;
     const int ng = min(EX_G, G - g0);
     const int oo = o * o;
     for (int e = threadIdx.x; e < ng * oo; e += blockDim.x) {
-        const int g = e / oo, r = e % oo, i = r / o, k = r % o;
-        const float* row = F + (long long)((g0 + g) * o + i) * ldf + (long long)(2 * w) * o;
-        fs[e] = make_float2(row[k], row[o + k]);
+        const int i = e % o, k = (e / o) % o, g = e / oo;  // i fastest: contiguous columns (g, i)
+        const long long col = (long long)(g0 + g) * o + i;
+        const float re = F[(long long)((2 * w) * o + k) * ldf + col];
+        const float im = F[(long long)((2 * w + 1) * o + k) * ldf + col];
+        fs[(g * o + i) * o + k] = make_float2(re, im);
     }
     __syncthreads();
     double xr = 0.0, xi = 0.0, cr = 0.0, ci = 0.0;
@@ -385,8 +622,8 @@ __global__ void k_green_rows(int wc, int n, int o, const double2* __restrict__ g
                 const double2 v = green[((size_t)w * o + k) * n + kk];
                 x = part ? v.y : v.x;
             }
-            split_store3(row, S, kk, x, false);
-        } else if (kk >= 3 * S) {
+            split_store(row, S, kk, x, false);
+        } else if (kk >= kSplit * S) {
             row[kk] = __double2bfloat16(0.0);
         }
     }

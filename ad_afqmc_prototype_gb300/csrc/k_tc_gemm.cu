@@ -281,6 +281,187 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// ----------------------------------------------------------------- drained --
+// Same pipeline, but the fp32 sum over K is formed outside the tensor cores.
+// The tensor cores' fp32 accumulation truncates: summing K positive terms
+// drifts low by ~K/16 * 2^-25 relative (about -3e-5 at K = 16384, measured),
+// and that drift is coherent across a whole contraction.  Here every 64-wide
+// K block starts a fresh partial in tensor memory (4 MMAs, bias < 2^-23), and
+// the epilogue warps add the partials into fp32 registers with ordinary
+// round-to-nearest adds while the MMA thread fills the next of 4 slots.
+// Tile 128 x 128 so that a thread's running sums (one row, 128 columns) fit
+// in registers.
+constexpr int DBN = 128, DSTAGES = 6, DSLOTS = 4;
+constexpr int DB_BYTES = DBN * BK * 2;
+constexpr int DSTAGE_BYTES = A_BYTES + DB_BYTES;
+constexpr int DTMEM_COLS = DSLOTS * DBN;  // 512
+constexpr int DSMEM_BYTES = DSTAGES * DSTAGE_BYTES + 1024 + 256;
+constexpr uint32_t DIDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(DBN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16_n128(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(DIDESC), "r"(accumulate)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    float* __restrict__ C, int M, int N, int K, long long ldc, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + DSTAGES * A_BYTES;
+    uint64_t* bars = (uint64_t*)(smem + DSTAGES * DSTAGE_BYTES);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * DSTAGES + 2 * DSLOTS + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + DSTAGES);
+    const uint32_t tfull0 = smem_u32(bars + 2 * DSTAGES), tempty0 = smem_u32(bars + 2 * DSTAGES + DSLOTS);
+    const uint32_t drain = smem_u32(bars + 2 * DSTAGES + 2 * DSLOTS);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = (M + BM - 1) / BM, nt = (N + DBN - 1) / DBN, kt = K / BK;
+    const int ntiles = mt * nt;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < DSTAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int a = 0; a < DSLOTS; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 128);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(DTMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmA) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
+            int stage = 0;
+            uint32_t phase = 0;
+            int issued[DSTAGES];
+            uint32_t issued_par[DSTAGES];
+            for (int s = 0; s < DSTAGES; ++s) issued[s] = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                const int mb = t % mt, nb = t / mt;
+                for (int kb = 0; kb < kt; ++kb) {
+                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
+                    issued[stage] = 0;
+                    mbar_expect_tx(full0 + 8 * stage, DSTAGE_BYTES);
+                    tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
+                    tma_load_2d(smem_u32(sB + stage * DB_BYTES), &tmB, kb * BK, nb * DBN, full0 + 8 * stage);
+                    issued[stage] = 1;
+                    issued_par[stage] = phase;
+                    if (++stage == DSTAGES) { stage = 0; phase ^= 1; }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                for (int s = 0; s < DSTAGES; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0, slot = 0;
+            uint32_t phase = 0, slot_phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                for (int kb = 0; kb < kt; ++kb) {
+                    if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(tempty0 + 8 * slot, slot_phase ^ 1, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + stage * A_BYTES), b0 = smem_u32(sB + stage * DB_BYTES);
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k)
+                        umma_bf16_n128(tmem + slot * DBN, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), k != 0);
+                    umma_commit(empty0 + 8 * stage);
+                    umma_commit(tfull0 + 8 * slot);
+                    if (++stage == DSTAGES) { stage = 0; phase ^= 1; }
+                    if (++slot == DSLOTS) { slot = 0; slot_phase ^= 1; }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                umma_commit(drain);
+                mbar_wait(drain, 0, nullptr);
+            }
+        }
+    } else {
+        const int q = warp & 3;
+        int slot = 0;
+        uint32_t slot_phase = 0;
+        const bool vec = (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
+        bool ok = true;
+        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            const int mb = t % mt, nb = t / mt;
+            float acc[DBN];
+#pragma unroll
+            for (int j = 0; j < DBN; ++j) acc[j] = 0.f;
+            for (int kb = 0; kb < kt; ++kb) {
+                if (!mbar_wait(tfull0 + 8 * slot, slot_phase, abort_flag)) {
+                    atomicExch(err, 1);
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+#pragma unroll
+                for (int c = 0; c < DBN; c += 32) {
+                    uint32_t r[32];
+                    tmem_ld32(tmem + slot * DBN + c + ((uint32_t)(q * 32) << 16), r);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) acc[c + j] += __uint_as_float(r[j]);
+                }
+                tc_fence_before();
+                mbar_arrive(tempty0 + 8 * slot);
+                if (++slot == DSLOTS) { slot = 0; slot_phase ^= 1; }
+            }
+            if (!ok) break;
+            const int row = mb * BM + q * 32 + lane;
+            const int col0 = nb * DBN;
+            if (row < M) {
+                float* dst = C + (long long)row * ldc + col0;
+                if (vec && col0 + DBN <= N) {
+#pragma unroll
+                    for (int j = 0; j < DBN; j += 4) *(float4*)(dst + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < DBN; ++j)
+                        if (col0 + j < N) dst[j] = acc[j];
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DTMEM_COLS) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------- host --
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
@@ -333,6 +514,34 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
     k_gemm_tn<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, M, N, K, ldc, err);
     AFQ_LAUNCHED("k_gemm_tn");
+    return AFQ_OK;
+}
+
+static bool g_drain_attr = false;
+
+int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                            long long ldc, int* err, cudaStream_t s) {
+    using namespace tc;
+    if (M <= 0 || N <= 0) return AFQ_OK;
+    if (K <= 0 || K % BK) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: K=%d must be a positive multiple of %d", K, BK);
+    AFQ_TRY(get_encode());
+    CUtensorMap ma, mb;
+    AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
+    AFQ_TRY(make_map(&mb, B, N, K, ldb, DBN));
+    if (!g_num_sms) {
+        int dev = 0;
+        AFQ_CUDA(cudaGetDevice(&dev));
+        AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    }
+    if (!g_drain_attr) {
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain, cudaFuncAttributeMaxDynamicSharedMemorySize, DSMEM_BYTES));
+        g_drain_attr = true;
+    }
+    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + DBN - 1) / DBN);
+    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+    k_gemm_tn_drain<<<grid, THREADS, DSMEM_BYTES, s>>>(ma, mb, C, M, N, K, ldc, err);
+    AFQ_LAUNCHED("k_gemm_tn_drain");
     return AFQ_OK;
 }
 

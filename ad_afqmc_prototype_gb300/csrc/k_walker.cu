@@ -21,7 +21,7 @@ static int set_smem(K kernel, size_t bytes) {
 //   m^-1; overlap = det(m)^2 (meas/rhf.py:22-24); G_half^T = W m^-1, i.e.
 //   G_half = solve(m^T, W^T) (meas/rhf.py:15-19).  One CTA per walker.
 // =====================================================================
-template <bool CR>
+template <bool CR, int MA>
 __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __restrict__ mo,
                                                const double2* __restrict__ walkers,
                                                double2* __restrict__ ovlp_out,
@@ -34,20 +34,42 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
-    for (int e = tid; e < o * o; e += blockDim.x) {
-        int a = e / o, b = e % o;
-        double2 acc = make_double2(0.0, 0.0);
-        for (int i = 0; i < n; ++i) {
-            double2 c = mo[i * o + a], x = Wp[i * o + b];
-            if (CR) {
-                rfma(acc, c.x, x);
-            } else {
-                acc.x = fma(c.x, x.x, acc.x); acc.x = fma(c.y, x.y, acc.x);
-                acc.y = fma(c.x, x.y, acc.y); acc.y = fma(-c.y, x.x, acc.y);
+    // m[a, b] = sum_i conj(C[i, a]) W[i, b]: thread <-> column b and rows
+    // a = ag + AG k, so each thread streams its column of W once (coalesced
+    // across b) and takes C from L1.
+    {
+        // MA >= ceil(o / AG) rows per thread, a template argument so that the
+        // accumulators stay in registers without inflating smaller cases
+        const int AG = blockDim.x / o;
+        const int b = tid % o, ag = tid / o;
+        double2 acc[MA];
+#pragma unroll
+        for (int k = 0; k < MA; ++k) acc[k] = make_double2(0.0, 0.0);
+        if (ag < AG) {
+            for (int i = 0; i < n; ++i) {
+                const double2 x = Wp[(size_t)i * o + b];
+#pragma unroll
+                for (int k = 0; k < MA; ++k) {
+                    const int a = ag + AG * k;
+                    if (a < o) {
+                        const double2 c = mo[i * o + a];
+                        if (CR) {
+                            rfma(acc[k], c.x, x);
+                        } else {
+                            acc[k].x = fma(c.x, x.x, acc[k].x); acc[k].x = fma(c.y, x.y, acc[k].x);
+                            acc[k].y = fma(c.x, x.y, acc[k].y); acc[k].y = fma(-c.y, x.x, acc[k].y);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < MA; ++k) {
+                const int a = ag + AG * k;
+                if (a < o) m[a * o + b] = acc[k];
             }
         }
-        m[e] = acc;
-        inv[e] = make_double2(a == b ? 1.0 : 0.0, 0.0);
+        for (int e = tid; e < o * o; e += blockDim.x)
+            inv[e] = make_double2((e / o) == (e % o) ? 1.0 : 0.0, 0.0);
     }
     if (tid == 0) s_det = make_double2(1.0, 0.0);
     __syncthreads();
@@ -109,25 +131,60 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
     if (ovlp_out && tid == 0) ovlp_out[w] = cmul(s_det, s_det);
     if (!green_out && !split.ptr) return;
     // G_half[b, i] = sum_a W[i, a] inv[a, b]
-    double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
-    __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
-    __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
-    for (int e = tid; e < n * o; e += blockDim.x) {
-        int b = e / n, i = e % n;
-        double2 acc = make_double2(0.0, 0.0);
-        for (int a = 0; a < o; ++a) cfma(acc, Wp[i * o + a], inv[a * o + b]);
-        if (Gp) Gp[e] = acc;
-        if (re_row) {
-            split_store3(re_row, split.S, e, acc.x, true);
-            split_store3(im_row, split.S, e, acc.y, true);
+    if (green_out) {
+        double2* Gp = green_out + (size_t)w * o * n;
+        for (int e = tid; e < n * o; e += blockDim.x) {
+            int b = e / n, i = e % n;
+            double2 acc = make_double2(0.0, 0.0);
+            for (int a = 0; a < o; ++a) cfma(acc, Wp[i * o + a], inv[a * o + b]);
+            Gp[e] = acc;
         }
     }
-    if (re_row) {  // zero the section gaps and the tail of the row
-        for (int e = n * o + tid; e < split.S; e += blockDim.x) {
-            split_store3(re_row, split.S, e, 0.0, true);
-            split_store3(im_row, split.S, e, 0.0, true);
+    if (!split.ptr) return;
+    // Force-bias operand: the same product in fp32 (the bf16 hi/lo split that
+    // consumes it resolves ~2^-17), written as the split left operand.
+    __nv_bfloat16* re_row = split.ptr + (size_t)w * split.ld;
+    __nv_bfloat16* im_row = split.ptr + (size_t)(split.W + w) * split.ld;
+    float2* invf = (float2*)(inv + o * o);
+    for (int e = tid; e < o * o; e += blockDim.x) invf[e] = make_float2((float)inv[e].x, (float)inv[e].y);
+    __syncthreads();
+    {
+        constexpr int BG = 8;
+        const int nbg = (o + BG - 1) / BG;
+        for (int t = tid; t < n * nbg; t += blockDim.x) {
+            const int i = t % n, bg = t / n;
+            float2 acc[BG];
+#pragma unroll
+            for (int j = 0; j < BG; ++j) acc[j] = make_float2(0.f, 0.f);
+            for (int a = 0; a < o; ++a) {
+                const double2 wv = Wp[(size_t)i * o + a];
+                const float2 x = make_float2((float)wv.x, (float)wv.y);
+#pragma unroll
+                for (int j = 0; j < BG; ++j) {
+                    const int b = bg * BG + j;
+                    if (b < o) {
+                        const float2 v = invf[a * o + b];
+                        acc[j].x = fmaf(x.x, v.x, acc[j].x); acc[j].x = fmaf(-x.y, v.y, acc[j].x);
+                        acc[j].y = fmaf(x.x, v.y, acc[j].y); acc[j].y = fmaf(x.y, v.x, acc[j].y);
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < BG; ++j) {
+                const int b = bg * BG + j;
+                if (b < o) {
+                    split_store(re_row, split.S, b * n + i, (double)acc[j].x, true);
+                    split_store(im_row, split.S, b * n + i, (double)acc[j].y, true);
+                }
+            }
         }
-        for (long long e = 3LL * split.S + tid; e < split.ld; e += blockDim.x) {
+    }
+    {  // zero the section gaps and the tail of the row
+        for (int e = n * o + tid; e < split.S; e += blockDim.x) {
+            split_store(re_row, split.S, e, 0.0, true);
+            split_store(im_row, split.S, e, 0.0, true);
+        }
+        for (long long e = (long long)kSplit * split.S + tid; e < split.ld; e += blockDim.x) {
             re_row[e] = __double2bfloat16(0.0);
             im_row[e] = __double2bfloat16(0.0);
         }
@@ -137,14 +194,25 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
                        double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
-    size_t smem = 2 * (size_t)o * o * sizeof(double2);
-    if (trial_real) {
-        AFQ_TRY(set_smem(k_green<true>, smem));
-        k_green<true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split);
-    } else {
-        AFQ_TRY(set_smem(k_green<false>, smem));
-        k_green<false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split);
-    }
+    size_t smem = 2 * (size_t)o * o * sizeof(double2) + (split.ptr ? (size_t)o * o * sizeof(float2) : 0);
+    const int ag = 256 / o, ma = (o + ag - 1) / ag;  // rows of m per thread
+#define AFQ_GREEN(CRV, MAV)                                                                  \
+    do {                                                                                     \
+        AFQ_TRY(set_smem(k_green<CRV, MAV>, smem));                                          \
+        k_green<CRV, MAV><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split); \
+    } while (0)
+#define AFQ_GREEN_MA(CRV)                \
+    do {                                 \
+        if (ma <= 1) AFQ_GREEN(CRV, 1);  \
+        else if (ma <= 2) AFQ_GREEN(CRV, 2); \
+        else if (ma <= 4) AFQ_GREEN(CRV, 4); \
+        else if (ma <= 8) AFQ_GREEN(CRV, 8); \
+        else AFQ_GREEN(CRV, 16);         \
+    } while (0)
+    if (trial_real) AFQ_GREEN_MA(true);
+    else AFQ_GREEN_MA(false);
+#undef AFQ_GREEN_MA
+#undef AFQ_GREEN
     AFQ_LAUNCHED("k_green");
     return AFQ_OK;
 }

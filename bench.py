@@ -30,6 +30,7 @@ METRIC = "walker-steps/s at |ΔE|≤0.1 mHa vs FP64 oracle: chosen form vs plain
 UNIT = "walker-steps/s"
 STEPS_PER_BLOCK = 10
 QR_EVERY = 5
+SPLIT_SECTIONS = 6  # bf16 sections of a split tensor-core operand (kSplit in the CUDA sources)
 
 
 def parse():
@@ -38,12 +39,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="c4_n200_o30_g1000_w4096")
     ap.add_argument("--walkers", type=int, default=0, help="override the workload's walker count")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison block")
     return ap.parse_args()
 
 
@@ -106,18 +108,54 @@ class Clocks:
 
 
 # --------------------------------------------------- algorithmic work model ---
-def phase_work(n, o, G, W, trial_real=True):
-    """Algorithmic FLOPs per launch of each timed phase (real-flop units)."""
+def _r64(x):
+    return (x + 63) // 64 * 64
+
+
+def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
+    """(FLOPs per launch, pipe) of each timed phase.  FP64 form: algorithmic
+    real flops.  Mixed form: the tensor-core phases count the flops the
+    tensor cores execute on the bf16 hi/lo split operands (2 M N K with K the
+    three-section row length), the others algorithmic flops on their pipe."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
-    return {
-        "vbuild_gemm": 4.0 * G * n * n * W,
-        "trotter": (48.0 + 8.0) * n * n * o * W,
-        "fb_gemm": cm * G * o * n * W,
-        "green": (cm * o * o * n + 16.0 * o ** 3 + 8.0 * n * o * o) * W,
-        "overlap": (cm * o * o * n + 16.0 * o ** 3) * W,
-        "energy": (cm * G * o * o * n + 8.0 * G * o * o) * W,
-        "qr": (32.0 * n * o * o - 10.7 * o ** 3) * W,
+    work = {
+        "vbuild_gemm": (4.0 * G * n * n * W, "fp64"),
+        "trotter": ((48.0 + 8.0) * n * n * o * W, "fp64"),
+        "fb_gemm": (cm * G * o * n * W, "fp64"),
+        "green": ((cm * o * o * n + 16.0 * o ** 3 + 8.0 * n * o * o) * W, "fp64"),
+        "overlap": ((cm * o * o * n + 16.0 * o ** 3) * W, "fp64"),
+        "energy": ((cm * G * o * o * n + 8.0 * G * o * o) * W, "fp64"),
+        "qr": ((32.0 * n * o * o - 10.7 * o ** 3) * W, "fp64"),
     }
+    if precision == "mixed":
+        ks = SPLIT_SECTIONS
+        work["vbuild_gemm"] = (2.0 * (2 * W) * n * n * _r64(ks * G), "tensor")
+        work["fb_gemm"] = (2.0 * (2 * W) * G * _r64(ks * o * n), "tensor")
+        work["energy"] = (2.0 * (G * o) * (2 * o * W) * _r64(ks * n), "tensor")
+        work["trotter"] = ((48.0 + 8.0) * n * n * o * W, "fp32")
+    return work
+
+
+def roofline_for(phases, work, lib, steps):
+    """Roofline object of the phase with the largest device time."""
+    dname, (dcalls, dms) = max(phases.items(), key=lambda kv: kv[1][1])
+    if dname not in work:
+        return None
+    flops, pipe = work[dname]
+    avg_ms = dms / dcalls
+    achieved = flops / (avg_ms / 1000.0) / 1e12
+    peaks = load_peaks() or {}
+    if pipe == "tensor":
+        peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
+        src = "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)" if peak else None
+        if not peak:
+            peak, src = 1700.0, "fallback (no MEASURED_PEAKS.json)"
+    else:
+        peak, src = fma_peak(lib, pipe == "fp64")
+    return {"kernel": dname, "bound": pipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4) if peak else None, "traffic": None, "peak_source": src,
+            "avg_launch_ms": round(avg_ms, 4), "launches_per_step": round(dcalls / steps, 2),
+            "share_of_step": round(dms / sum(v[1] for v in phases.values()), 4)}
 
 
 # ------------------------------------------------------------ our engine ---
@@ -206,19 +244,14 @@ def run_ours(args, rank, world):
     value = world * W * STEPS_PER_BLOCK / (ms / 1000.0)
 
     # dominant kernel and its roofline
-    work = phase_work(n, o, G, W, trial_real=prob.trial_is_real)
-    dom = max(phases.items(), key=lambda kv: kv[1][1])
-    dname, (dcalls, dms) = dom
-    roof = None
-    if dname in work:
-        avg_ms = dms / dcalls
-        achieved = work[dname] / (avg_ms / 1000.0) / 1e12
-        peak, src = fp64_peak(lib) if args.precision == "fp64" else (None, None)
-        roof = {"kernel": dname, "bound": "fp64" if args.precision == "fp64" else "tensor",
-                "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
-                "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
-                "peak_source": src, "avg_launch_ms": round(avg_ms, 4),
-                "share_of_step": round(dms / sum(v[1] for v in phases.values()), 4)}
+    work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=args.precision)
+    roof = roofline_for(phases, work, lib, args.steps)
+    tc = {k: roofline_for({k: v}, work, lib, args.steps) for k, v in phases.items()
+          if k in work and work[k][1] == "tensor"}
+
+    compare = None
+    if args.precision == "mixed" and not args.no_fp64:
+        compare = compare_with_fp64(env, st, W)
 
     e2e = None
     if not args.no_e2e:
@@ -233,26 +266,63 @@ def run_ours(args, rank, world):
                       "step": "one block: 10 propagation steps, QR after step 5, QR + energy + comb at the end",
                       "l2": "inputs larger than L2 (walkers %d MB, V %d MB per step)"
                             % (W * n * o * 16 >> 20, W * n * n * 16 >> 20)},
-           "roofline": roof, "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
+           "roofline": roof, "tensor_kernels": tc,
+           "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
            "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
+    if compare:
+        out["plain_fp64"] = compare
+        out["ratio_vs_plain_fp64"] = round(value / compare["value"], 2)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     return out
 
 
-_FP64_PEAK = None
+def compare_with_fp64(env, st_mixed, W):
+    """The metric's denominator and accuracy check, on the same workload:
+    one block of the plain binary64 form and one of the mixed form from the
+    same state with the same fields and comb uniform.  Returns the FP64
+    walker-steps/s and |E_mixed - E_fp64| of that block."""
+    import dataclasses
+
+    import torch
+    from ad_afqmc_prototype_gb300 import engine
+    from ad_afqmc_prototype_gb300.prop.afqmc import engine_problem
+
+    kw = dict(env["kw"])
+    kw["params"] = dataclasses.replace(env["params"], precision="fp64")
+    prob64 = engine_problem(n_walkers=W, need_energy=True, **kw)
+
+    def clone(s):
+        return engine.DeviceState(*[t.clone() for t in (s.walkers, s.weights, s.overlaps, s.pop_shift,
+                                                          s.e_estimate)])
+    a, b = clone(st_mixed), clone(st_mixed)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ea, _ = engine.block(prob64, kw["params"], a, 77, 0, zeta=0.5)
+    e1.record()
+    eb, _ = engine.block(env["prob"], env["params"], b, 77, 0, zeta=0.5)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"value": round(W * STEPS_PER_BLOCK / (ms / 1000.0), 3), "unit": UNIT, "ms_per_step": round(ms, 1),
+            "measured": "one block of the binary64 form on the same workload (no warm-up of its own)",
+            "energy_error_per_block_ha": float(abs(float(ea) - float(eb))),
+            "energy_fp64_ha": float(ea), "energy_mixed_ha": float(eb)}
 
 
-def fp64_peak(lib):
-    """FP64 FMA throughput of this GPU, measured once in-process (the pool's
-    MEASURED_PEAKS.json has HBM and bf16 peaks only)."""
-    global _FP64_PEAK
-    if _FP64_PEAK is None:
+_FMA_PEAK = {}
+
+
+def fma_peak(lib, fp64: bool):
+    """SIMT FMA throughput of this GPU (binary64 or binary32), measured once
+    in-process: the pool's MEASURED_PEAKS.json has HBM and bf16 peaks only."""
+    if fp64 not in _FMA_PEAK:
         import ctypes
         v = ctypes.c_double(0.0)
-        rc = lib.afq_probe_fma_peak(1, ctypes.byref(v))
-        _FP64_PEAK = (round(v.value, 4), "measured in-process (FMA chains)") if rc == 0 else (None, None)
-    return _FP64_PEAK
+        rc = lib.afq_probe_fma_peak(1 if fp64 else 0, ctypes.byref(v))
+        _FMA_PEAK[fp64] = ((round(v.value, 4), "measured in-process (%s FMA chains)" % ("fp64" if fp64 else "fp32"))
+                           if rc == 0 else (None, None))
+    return _FMA_PEAK[fp64]
 
 
 def run_e2e(args, env, afqmc_block, W):

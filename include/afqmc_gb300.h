@@ -132,9 +132,14 @@ int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_ch
  * ldc) = A (M x K) . B (N x K)^T with bf16 A and B, row-major, K contiguous,
  * K a multiple of 64, lda / ldb multiples of 8, 16-byte aligned bases.
  * `err` (device int32, required) is set to 1 if a bounded pipeline wait
- * expired (the kernel then stops early instead of hanging). */
+ * expired (the kernel then stops early instead of hanging).
+ * accumulate: 0 = fp32 accumulation inside the tensor cores (truncating:
+ * a sum of K positive terms drifts low by ~K/16 * 2^-25 relative);
+ * 1 = each 64-wide K block is a fresh tensor-core partial, summed in fp32
+ * registers with round-to-nearest adds (what the mixed step uses). */
 int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B,
-                     int64_t ldb, float* C, int64_t ldc, int32_t* err, void* stream);
+                     int64_t ldb, float* C, int64_t ldc, int32_t* err, int32_t accumulate,
+                     void* stream);
 
 /* Device status word of a step / block workspace: synchronises `stream`,
  * copies the word to *status (0 = fine, 1 = a bounded device wait expired)
