@@ -456,8 +456,9 @@ int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda
     AFQ_NOTNULL(A); AFQ_NOTNULL(B); AFQ_NOTNULL(C); AFQ_NOTNULL(err);
     if (M < 0 || N < 0 || lda < K || ldb < K || ldc < N)
         return fail(AFQ_E_INVALID_ARGUMENT, "lowp gemm: bad sizes M=%d N=%d K=%d", M, N, K);
-    if (accumulate == 1) return launch_tc_gemm_tn_drain(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
-    if (accumulate != 0) return fail(AFQ_E_INVALID_ARGUMENT, "accumulate=%d must be 0 or 1", accumulate);
+    if (accumulate >= 1)
+        return launch_tc_gemm_tn_drain(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream), accumulate);
+    if (accumulate != 0) return fail(AFQ_E_INVALID_ARGUMENT, "accumulate=%d must be >= 0", accumulate);
     return launch_tc_gemm_tn(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
 }
 

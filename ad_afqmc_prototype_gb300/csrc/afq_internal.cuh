@@ -212,7 +212,7 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
 // Same product with the K sum formed in fp32 registers per 64-wide K block
 // (round-to-nearest) instead of in the tensor cores' truncating accumulator.
 int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
-                            long long ldc, int* err, cudaStream_t s);
+                            long long ldc, int* err, cudaStream_t s, int kd = 1);
 
 // k_walker.cu : Green's function with an optional split (bf16) output
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,

@@ -111,124 +111,184 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
 }
 
 // ------------------------------------------------------- Taylor propagation
-// Per CTA: one walker, OC columns.  Thread tile NR rows x CC columns; the
-// current Taylor term T is fp32 in shared memory, the operator (V or
-// E_half - I) is streamed through shared memory BJ columns at a time, and the
-// running sum lives in the binary64 output walker, which each thread updates
-// only at its own entries (so walkers_out may alias walkers_in):
+// One CTA per (walker, 32 columns).  The current Taylor term T (fp32, all n
+// rows x 32 columns) stays in shared memory; the operand (V of this walker,
+// or E_half - I) streams through a two-stage cp.async ring, TR_BJ columns per
+// stage, so the next columns are in flight while the current ones are
+// multiplied.  Thread (rg, cg) owns rows rg + RG q (q < NR) and the complex
+// columns 2cg, 2cg+1, 16+2cg, 16+2cg+1 (so a warp's T reads are contiguous
+// 128-byte rows).  The running sum lives in the binary64 output walker, which
+// each thread updates only at its own entries (walkers_out may alias
+// walkers_in):
 //   W1 = W + (E-I) W;  out = W1 + sum_k (i sqrt_dt V)^k / k! W1;
 //   W' = out + (E-I) out.
-constexpr int TM_THREADS = 512, TM_CC = 4, TM_BJ = 16;
-// Row stride of the staged operand: odd, so the four row groups of a warp
-// read four different banks.
-constexpr int TM_MS = TM_BJ + 1;
+constexpr int TR_CG = 8, TR_OC = 32, TR_BJ = 8;
+// Row stride (floats) of a staged operand plane: 16-byte rows for cp.async,
+// and rows 0..3 of a warp start in different banks.
+constexpr int TR_VS = TR_BJ + 4;
 
-template <int OC, int NR, bool REAL_M>
-__device__ __forceinline__ void tm_matmul(int n, const float* __restrict__ Mr, const float* __restrict__ Mi,
-                                          const float2* __restrict__ T, float2* __restrict__ Ms,
-                                          float2 (&acc)[NR][TM_CC], int cg, int rg) {
-    constexpr int CG = OC / TM_CC, RG = TM_THREADS / CG;
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Columns [j0, j0 + TR_BJ) of rows 0..n-1 of the operand planes (row stride
+// n floats) into a stage; columns past n are zero.
+__device__ __forceinline__ void tr_stage(int n, int j0, const float* __restrict__ re, const float* __restrict__ im,
+                                         float* sr, float* si, bool v16) {
+    const int jn = min(TR_BJ, n - j0);
+    const int planes = im ? 2 : 1;
+    if (v16) {  // n % 4 == 0 and 16-byte aligned planes: jn is a multiple of 4
+        constexpr int CH = TR_BJ / 4;
+        for (int e = threadIdx.x; e < n * CH * planes; e += blockDim.x) {
+            const int i = e / (CH * planes), r = e % (CH * planes), pl = r / CH, h = r % CH;
+            float* dst = (pl ? si : sr) + i * TR_VS + 4 * h;
+            if (4 * h < jn) cp_async16(dst, (pl ? im : re) + (size_t)i * n + j0 + 4 * h);
+            else *(float4*)dst = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    } else {
+        for (int e = threadIdx.x; e < n * TR_BJ * planes; e += blockDim.x) {
+            const int i = e / (TR_BJ * planes), r = e % (TR_BJ * planes), pl = r / TR_BJ, jj = r % TR_BJ;
+            float* dst = (pl ? si : sr) + i * TR_VS + jj;
+            if (jj < jn) cp_async4(dst, (pl ? im : re) + (size_t)i * n + j0 + jj);
+            else *dst = 0.f;
+        }
+    }
+    cp_async_commit();
+}
+
+// acc = M T for the n x n operand M (real when im == nullptr).  stg holds two
+// stages of two planes, rows padded to RG*NR and zero beyond n.  Ends with a
+// barrier, so the caller may overwrite T and the stages.
+template <int NR, bool CPLX>
+__device__ __forceinline__ void tr_matmul(int n, const float* __restrict__ re, const float* __restrict__ im,
+                                          const float4* __restrict__ T4, float* stg, int rows, float2 (&acc)[NR][4],
+                                          int cg, int rg, int RG, bool v16) {
 #pragma unroll
     for (int q = 0; q < NR; ++q)
 #pragma unroll
-        for (int j = 0; j < TM_CC; ++j) acc[q][j] = make_float2(0.f, 0.f);
-    float* Msr = (float*)Ms;
-    for (int j0 = 0; j0 < n; j0 += TM_BJ) {
-        const int jn = min(TM_BJ, n - j0);
-        for (int e = threadIdx.x; e < n * TM_BJ; e += TM_THREADS) {
-            const int i = e / TM_BJ, jj = e % TM_BJ;
-            const size_t src = (size_t)i * n + j0 + jj;
-            if (REAL_M) Msr[i * TM_MS + jj] = jj < jn ? Mr[src] : 0.f;
-            else Ms[i * TM_MS + jj] = jj < jn ? make_float2(Mr[src], Mi[src]) : make_float2(0.f, 0.f);
-        }
+        for (int j = 0; j < 4; ++j) acc[q][j] = make_float2(0.f, 0.f);
+    const int plane = rows * TR_VS;
+    const int nb = (n + TR_BJ - 1) / TR_BJ;
+    tr_stage(n, 0, re, im, stg, stg + plane, v16);
+    for (int b = 0; b < nb; ++b) {
+        cp_async_wait_all();
         __syncthreads();
-        for (int jj = 0; jj < jn; ++jj) {
-            const float4* tp = (const float4*)(T + (j0 + jj) * OC + cg * TM_CC);
-            const float4 t01 = tp[0], t23 = tp[1];
-            const float2 t[TM_CC] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w), make_float2(t23.x, t23.y),
-                                     make_float2(t23.z, t23.w)};
+        const float* sr = stg + (b & 1) * 2 * plane;
+        const float* si = sr + plane;
+        if (b + 1 < nb) {
+            float* nr_ = stg + ((b + 1) & 1) * 2 * plane;
+            tr_stage(n, (b + 1) * TR_BJ, re, im, nr_, nr_ + plane, v16);
+        }
+        const float4* tb = T4 + (size_t)b * TR_BJ * (TR_OC / 2);
+#pragma unroll 1
+        for (int jj = 0; jj < TR_BJ; jj += 2) {
+            float2 mr[NR], mi[NR];
 #pragma unroll
             for (int q = 0; q < NR; ++q) {
                 const int i = rg + RG * q;
-                if (i < n) {
-                    if (REAL_M) {
-                        const float m = Msr[i * TM_MS + jj];
+                mr[q] = *(const float2*)(sr + i * TR_VS + jj);
+                if (CPLX) mi[q] = *(const float2*)(si + i * TR_VS + jj);
+            }
 #pragma unroll
-                        for (int j = 0; j < TM_CC; ++j) {
-                            acc[q][j].x = fmaf(m, t[j].x, acc[q][j].x);
-                            acc[q][j].y = fmaf(m, t[j].y, acc[q][j].y);
-                        }
-                    } else {
-                        const float2 m = Ms[i * TM_MS + jj];
+            for (int h = 0; h < 2; ++h) {
+                const float4 ta = tb[(jj + h) * (TR_OC / 2) + cg], tc = tb[(jj + h) * (TR_OC / 2) + TR_CG + cg];
+                const float2 t[4] = {make_float2(ta.x, ta.y), make_float2(ta.z, ta.w), make_float2(tc.x, tc.y),
+                                     make_float2(tc.z, tc.w)};
 #pragma unroll
-                        for (int j = 0; j < TM_CC; ++j) {
-                            acc[q][j].x = fmaf(m.x, t[j].x, acc[q][j].x);
-                            acc[q][j].x = fmaf(-m.y, t[j].y, acc[q][j].x);
-                            acc[q][j].y = fmaf(m.x, t[j].y, acc[q][j].y);
-                            acc[q][j].y = fmaf(m.y, t[j].x, acc[q][j].y);
+                for (int q = 0; q < NR; ++q) {
+                    const float a = h ? mr[q].y : mr[q].x;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        acc[q][j].x = fmaf(a, t[j].x, acc[q][j].x);
+                        acc[q][j].y = fmaf(a, t[j].y, acc[q][j].y);
+                    }
+                    if (CPLX) {
+                        const float bq = h ? mi[q].y : mi[q].x;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            acc[q][j].x = fmaf(-bq, t[j].y, acc[q][j].x);
+                            acc[q][j].y = fmaf(bq, t[j].x, acc[q][j].y);
                         }
                     }
                 }
             }
         }
-        __syncthreads();
     }
+    __syncthreads();
 }
 
-template <int OC, int NR>
-__global__ void __launch_bounds__(TM_THREADS) k_trotter_mixed(int n, int o, int n_terms, float sqrt_dt,
-                                                              const float* __restrict__ emi, const float* __restrict__ vm,
-                                                              long long ldv, int wc, const double2* win, double2* wout) {
-    constexpr int CG = OC / TM_CC, RG = TM_THREADS / CG;
-    extern __shared__ float2 smf2[];
-    float2* T = smf2;                     // n x OC
-    float2* Ms = smf2 + (size_t)n * OC;   // n x BJ
-    const int w = blockIdx.y, c0 = blockIdx.x * OC;
-    const int cg = threadIdx.x % CG, rg = threadIdx.x / CG;
+__device__ __forceinline__ int tr_col(int cg, int j) { return j < 2 ? 2 * cg + j : TR_OC / 2 + 2 * cg + (j - 2); }
+
+template <int NR>
+__global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms, float sqrt_dt,
+                                                          const float* __restrict__ emi, const float* __restrict__ vm,
+                                                          long long ldv, int wc, const double2* win, double2* wout,
+                                                          int v16) {
+    extern __shared__ float4 smf4[];
+    const int RG = blockDim.x / TR_CG, rows = RG * NR;
+    const int nT = (n + TR_BJ - 1) / TR_BJ * TR_BJ;
+    float4* T4 = smf4;                              // nT x 32 complex, as float4 pairs
+    float2* T = (float2*)smf4;
+    float* stg = (float*)(smf4 + (size_t)nT * (TR_OC / 2));  // 2 stages x 2 planes x rows x TR_VS
+    const int w = blockIdx.y, c0 = blockIdx.x * TR_OC;
+    const int cg = threadIdx.x % TR_CG, rg = threadIdx.x / TR_CG;
     const double2* Wp = win + (size_t)w * n * o;
     double2* Wo = wout + (size_t)w * n * o;
     const float* Vr = vm + (long long)w * ldv;
     const float* Vi = vm + (long long)(wc + w) * ldv;
 
-    for (int e = threadIdx.x; e < n * OC; e += TM_THREADS) {
-        const int i = e / OC, cc = e % OC;
-        if (c0 + cc < o) {
+    for (int e = threadIdx.x; e < 4 * rows * TR_VS; e += blockDim.x) stg[e] = 0.f;
+    for (int e = threadIdx.x; e < nT * TR_OC; e += blockDim.x) {
+        const int i = e / TR_OC, cc = e % TR_OC;
+        float2 t = make_float2(0.f, 0.f);
+        if (i < n && c0 + cc < o) {
             const double2 v = Wp[(size_t)i * o + c0 + cc];
-            T[e] = make_float2((float)v.x, (float)v.y);
-        } else {
-            T[e] = make_float2(0.f, 0.f);
+            t = make_float2((float)v.x, (float)v.y);
         }
+        T[e] = t;
     }
     __syncthreads();
-    float2 acc[NR][TM_CC];
+    float2 acc[NR][4];
+    int rgl;  // rg, opaque to the compiler: entry addresses are recomputed per epilogue, not held in registers
     // W1 = W + (E - I) W
-    tm_matmul<OC, NR, true>(n, emi, nullptr, T, Ms, acc, cg, rg);
+    tr_matmul<NR, false>(n, emi, nullptr, T4, stg, rows, acc, cg, rg, RG, v16);
+    rgl = rg;
+    asm volatile("" : "+r"(rgl));
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-        const int i = rg + RG * q;
+        const int i = rgl + RG * q;
 #pragma unroll
-        for (int j = 0; j < TM_CC; ++j) {
-            const int cl = cg * TM_CC + j, c = c0 + cl;
+        for (int j = 0; j < 4; ++j) {
+            const int cl = tr_col(cg, j), c = c0 + cl;
             if (i < n && c < o) {
                 const double2 v = Wp[(size_t)i * o + c];
                 const double2 w1 = make_double2(v.x + (double)acc[q][j].x, v.y + (double)acc[q][j].y);
                 Wo[(size_t)i * o + c] = w1;
-                T[i * OC + cl] = make_float2((float)w1.x, (float)w1.y);
+                T[i * TR_OC + cl] = make_float2((float)w1.x, (float)w1.y);
             }
         }
     }
     __syncthreads();
     for (int k = 1; k <= n_terms; ++k) {
-        tm_matmul<OC, NR, false>(n, Vr, Vi, T, Ms, acc, cg, rg);
+        tr_matmul<NR, true>(n, Vr, Vi, T4, stg, rows, acc, cg, rg, RG, v16);
         const float sk = sqrt_dt / (float)k;  // (i sqrt_dt / k) z = sk (-z.y, z.x)
+        rgl = rg;
+        asm volatile("" : "+r"(rgl));
 #pragma unroll
         for (int q = 0; q < NR; ++q) {
-            const int i = rg + RG * q;
+            const int i = rgl + RG * q;
 #pragma unroll
-            for (int j = 0; j < TM_CC; ++j) {
-                const int cl = cg * TM_CC + j, c = c0 + cl;
+            for (int j = 0; j < 4; ++j) {
+                const int cl = tr_col(cg, j), c = c0 + cl;
                 const float2 t = make_float2(-sk * acc[q][j].y, sk * acc[q][j].x);
-                if (i < n) T[i * OC + cl] = (c < o) ? t : make_float2(0.f, 0.f);
+                if (i < n) T[i * TR_OC + cl] = (c < o) ? t : make_float2(0.f, 0.f);
                 if (i < n && c < o) {
                     double2 v = Wo[(size_t)i * o + c];
                     v.x += (double)t.x;
@@ -240,26 +300,30 @@ __global__ void __launch_bounds__(TM_THREADS) k_trotter_mixed(int n, int o, int 
         __syncthreads();
     }
     // W' = out + (E - I) out
+    rgl = rg;
+    asm volatile("" : "+r"(rgl));
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-        const int i = rg + RG * q;
+        const int i = rgl + RG * q;
 #pragma unroll
-        for (int j = 0; j < TM_CC; ++j) {
-            const int cl = cg * TM_CC + j, c = c0 + cl;
+        for (int j = 0; j < 4; ++j) {
+            const int cl = tr_col(cg, j), c = c0 + cl;
             if (i < n && c < o) {
                 const double2 v = Wo[(size_t)i * o + c];
-                T[i * OC + cl] = make_float2((float)v.x, (float)v.y);
+                T[i * TR_OC + cl] = make_float2((float)v.x, (float)v.y);
             }
         }
     }
     __syncthreads();
-    tm_matmul<OC, NR, true>(n, emi, nullptr, T, Ms, acc, cg, rg);
+    tr_matmul<NR, false>(n, emi, nullptr, T4, stg, rows, acc, cg, rg, RG, v16);
+    rgl = rg;
+    asm volatile("" : "+r"(rgl));
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-        const int i = rg + RG * q;
+        const int i = rgl + RG * q;
 #pragma unroll
-        for (int j = 0; j < TM_CC; ++j) {
-            const int c = c0 + cg * TM_CC + j;
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tr_col(cg, j);
             if (i < n && c < o) {
                 double2 v = Wo[(size_t)i * o + c];
                 v.x += (double)acc[q][j].x;
@@ -278,36 +342,30 @@ static int smem_attr(K kernel, size_t bytes) {
     return AFQ_OK;
 }
 
-template <int OC>
-static int trotter_mixed_oc(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
-                            long long ldv, const double2* win, double2* wout, cudaStream_t s) {
-    constexpr int RG = TM_THREADS / (OC / TM_CC);
-    const int nr = (n + RG - 1) / RG;
-    const size_t smem = (size_t)n * (OC + TM_MS) * sizeof(float2);
-    dim3 grid((o + OC - 1) / OC, wc);
-#define AFQ_TM(NRV)                                                                                    \
-    do {                                                                                               \
-        AFQ_TRY(smem_attr(k_trotter_mixed<OC, NRV>, smem));                                             \
-        k_trotter_mixed<OC, NRV><<<grid, TM_THREADS, smem, s>>>(n, o, n_terms, (float)sqrt_dt, emi, vm, ldv, wc, \
-                                                              win, wout);                             \
-    } while (0)
-    if (nr <= 1) AFQ_TM(1);
-    else if (nr <= 2) AFQ_TM(2);
-    else if (nr <= 4) AFQ_TM(4);
-    else return fail(AFQ_E_UNSUPPORTED, "mixed trotter: norb=%d too large", n);
-#undef AFQ_TM
-    AFQ_LAUNCHED("k_trotter_mixed");
-    return AFQ_OK;
-}
-
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
                          long long ldv, const double2* win, double2* wout, cudaStream_t s) {
     if (wc <= 0) return AFQ_OK;
     if (wc > 65535) return fail(AFQ_E_UNSUPPORTED, "mixed trotter: chunk of %d walkers > 65535", wc);
-    // 32 columns per CTA keep a walker's V read once per term; above 256
-    // orbitals 16 columns keep the per-thread tile at <= 4 rows (no spills)
-    if (o <= 16 || n > 256) return trotter_mixed_oc<16>(wc, n, o, n_terms, sqrt_dt, emi, vm, ldv, win, wout, s);
-    return trotter_mixed_oc<32>(wc, n, o, n_terms, sqrt_dt, emi, vm, ldv, win, wout, s);
+    // 256 threads (32 row groups) up to 7 rows each, else 512 threads
+    const int threads = n <= 32 * 7 ? 256 : 512, RG = threads / TR_CG;
+    const int nr = (n + RG - 1) / RG;
+    if (nr > 8) return fail(AFQ_E_UNSUPPORTED, "mixed trotter: norb=%d too large", n);
+    const int nT = (n + TR_BJ - 1) / TR_BJ * TR_BJ;
+    const size_t smem = (size_t)nT * TR_OC * sizeof(float2) + (size_t)4 * RG * nr * TR_VS * sizeof(float);
+    const int v16 = (n % 4 == 0) && (ldv % 4 == 0) && ((((uintptr_t)vm) | ((uintptr_t)emi)) & 15) == 0;
+    dim3 grid((o + TR_OC - 1) / TR_OC, wc);
+#define AFQ_TM(NRV)                                                                                      \
+    case NRV:                                                                                            \
+        AFQ_TRY(smem_attr(k_trotter_mixed<NRV>, smem));                                                  \
+        k_trotter_mixed<NRV><<<grid, threads, smem, s>>>(n, o, n_terms, (float)sqrt_dt, emi, vm, ldv, wc, win, \
+                                                         wout, v16);                                     \
+        break;
+    switch (nr) {
+        AFQ_TM(1) AFQ_TM(2) AFQ_TM(3) AFQ_TM(4) AFQ_TM(5) AFQ_TM(6) AFQ_TM(7) AFQ_TM(8)
+    }
+#undef AFQ_TM
+    AFQ_LAUNCHED("k_trotter_mixed");
+    return AFQ_OK;
 }
 
 // ------------------------------------------- overlap + force-bias operand

@@ -287,53 +287,82 @@ __global__ void __launch_bounds__(THREADS, 1)
 // drifts low by ~K/16 * 2^-25 relative (about -3e-5 at K = 16384, measured),
 // and that drift is coherent across a whole contraction.  Here every 64-wide
 // K block starts a fresh partial in tensor memory (4 MMAs, bias < 2^-23), and
-// the epilogue warps add the partials into fp32 registers with ordinary
-// round-to-nearest adds while the MMA thread fills the next of 4 slots.
-// Tile 128 x 128 so that a thread's running sums (one row, 128 columns) fit
-// in registers.
-constexpr int DBN = 128, DSTAGES = 6, DSLOTS = 4;
-constexpr int DB_BYTES = DBN * BK * 2;
-constexpr int DSTAGE_BYTES = A_BYTES + DB_BYTES;
-constexpr int DTMEM_COLS = DSLOTS * DBN;  // 512
-constexpr int DSMEM_BYTES = DSTAGES * DSTAGE_BYTES + 1024 + 256;
-constexpr uint32_t DIDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(DBN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// eight epilogue warps add the partials into fp32 registers with
+// round-to-nearest adds (two lanes per instruction) while the MMA thread
+// fills the next slot.  Warp w may only read TMEM lanes 32*(w%4)..+31, so
+// warps 2-5 and 6-9 each cover all 128 rows, one column half each.
+constexpr int DTHREADS = 320;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-9: epilogue
+constexpr int DTMEM_COLS = 512;
 
-__device__ __forceinline__ void umma_bf16_n128(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+template <int BNT>
+struct Drain {
+    static constexpr int SLOTS = DTMEM_COLS / BNT;
+    static constexpr int STG = BNT == 128 ? 6 : 4;
+    static constexpr int B_BYTES = BNT * BK * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int SMEM = STG * STAGE + 1024 + 256;
+    static constexpr int CW = BNT / 2;  // columns per epilogue warp
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BNT >> 3) << 17) |
+                                      ((uint32_t)(BM >> 4) << 24);
+};
+
+__device__ __forceinline__ void umma_bf16_i(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(DIDESC), "r"(accumulate)
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
+#define AFQ_R8(i)                                                                                              \
+    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
+        "=r"(r[i + 7])
+// 64 consecutive fp32 columns of this warp's 32 lanes; returns after the load completed.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, "
+        "%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, "
+        "%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : AFQ_R8(0), AFQ_R8(8), AFQ_R8(16), AFQ_R8(24), AFQ_R8(32), AFQ_R8(40), AFQ_R8(48), AFQ_R8(56)
+        : "r"(taddr)
+        : "memory");
+}
+#undef AFQ_R8
+
+template <int BNT>
+__global__ void __launch_bounds__(DTHREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    float* __restrict__ C, int M, int N, int K, long long ldc, int* __restrict__ err) {
+                    float* __restrict__ C, int M, int N, int K, long long ldc, int kd, int* __restrict__ err) {
+    using D = Drain<BNT>;
+    constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
-    uint8_t* sB = smem + DSTAGES * A_BYTES;
-    uint64_t* bars = (uint64_t*)(smem + DSTAGES * DSTAGE_BYTES);
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * DSTAGES + 2 * DSLOTS + 1);
+    uint8_t* sB = smem + STG * A_BYTES;
+    uint64_t* bars = (uint64_t*)(smem + STG * D::STAGE);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STG + 2 * SLOTS + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + DSTAGES);
-    const uint32_t tfull0 = smem_u32(bars + 2 * DSTAGES), tempty0 = smem_u32(bars + 2 * DSTAGES + DSLOTS);
-    const uint32_t drain = smem_u32(bars + 2 * DSTAGES + 2 * DSLOTS);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STG);
+    const uint32_t tfull0 = smem_u32(bars + 2 * STG), tempty0 = smem_u32(bars + 2 * STG + SLOTS);
+    const uint32_t drain = smem_u32(bars + 2 * STG + 2 * SLOTS);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mt = (M + BM - 1) / BM, nt = (N + DBN - 1) / DBN, kt = K / BK;
-    const int ntiles = mt * nt;
+    const int mt = (M + BM - 1) / BM, nt = (N + BNT - 1) / BNT, kt = K / BK;
+    const int ntiles = mt * nt, np = (kt + kd - 1) / kd;  // partials per tile
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < DSTAGES; ++s) {
+        for (int s = 0; s < STG; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
-        for (int a = 0; a < DSLOTS; ++a) {
+        for (int a = 0; a < SLOTS; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, 128);
+            mbar_init(tempty0 + 8 * a, DTHREADS - 64);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -356,27 +385,27 @@ __global__ void __launch_bounds__(THREADS, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
             int stage = 0;
             uint32_t phase = 0;
-            int issued[DSTAGES];
-            uint32_t issued_par[DSTAGES];
-            for (int s = 0; s < DSTAGES; ++s) issued[s] = 0;
+            int issued[STG];
+            uint32_t issued_par[STG];
+            for (int s = 0; s < STG; ++s) issued[s] = 0;
             bool ok = true;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 const int mb = t % mt, nb = t / mt;
                 for (int kb = 0; kb < kt; ++kb) {
                     if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
-                    mbar_expect_tx(full0 + 8 * stage, DSTAGE_BYTES);
+                    mbar_expect_tx(full0 + 8 * stage, D::STAGE);
                     tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
-                    tma_load_2d(smem_u32(sB + stage * DB_BYTES), &tmB, kb * BK, nb * DBN, full0 + 8 * stage);
+                    tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
                     issued[stage] = 1;
                     issued_par[stage] = phase;
-                    if (++stage == DSTAGES) { stage = 0; phase ^= 1; }
+                    if (++stage == STG) { stage = 0; phase ^= 1; }
                 }
             }
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                for (int s = 0; s < DSTAGES; ++s)
+                for (int s = 0; s < STG; ++s)
                     if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
             }
         }
@@ -387,17 +416,21 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 for (int kb = 0; kb < kt; ++kb) {
+                    const int g = kb % kd;  // position inside the current partial
                     if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
-                    if (!mbar_wait(tempty0 + 8 * slot, slot_phase ^ 1, abort_flag)) { ok = false; break; }
+                    if (g == 0 && !mbar_wait(tempty0 + 8 * slot, slot_phase ^ 1, abort_flag)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + stage * A_BYTES), b0 = smem_u32(sB + stage * DB_BYTES);
+                    const uint32_t a0 = smem_u32(sA + stage * A_BYTES), b0 = smem_u32(sB + stage * D::B_BYTES);
 #pragma unroll
                     for (int k = 0; k < BK / 16; ++k)
-                        umma_bf16_n128(tmem + slot * DBN, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), k != 0);
+                        umma_bf16_i(tmem + slot * BNT, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), D::IDESC,
+                                    (k != 0) || (g != 0));
                     umma_commit(empty0 + 8 * stage);
-                    umma_commit(tfull0 + 8 * slot);
-                    if (++stage == DSTAGES) { stage = 0; phase ^= 1; }
-                    if (++slot == DSLOTS) { slot = 0; slot_phase ^= 1; }
+                    if (g == kd - 1 || kb == kt - 1) {
+                        umma_commit(tfull0 + 8 * slot);
+                        if (++slot == SLOTS) { slot = 0; slot_phase ^= 1; }
+                    }
+                    if (++stage == STG) { stage = 0; phase ^= 1; }
                 }
             }
             if (!ok) {
@@ -408,17 +441,17 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
     } else {
-        const int q = warp & 3;
+        const int q = warp & 3, cb = ((warp - 2) >> 2) * CW;
         int slot = 0;
         uint32_t slot_phase = 0;
         const bool vec = (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
         for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
             const int mb = t % mt, nb = t / mt;
-            float acc[DBN];
+            float2 acc[CW / 2];
 #pragma unroll
-            for (int j = 0; j < DBN; ++j) acc[j] = 0.f;
-            for (int kb = 0; kb < kt; ++kb) {
+            for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
+            for (int p = 0; p < np; ++p) {
                 if (!mbar_wait(tfull0 + 8 * slot, slot_phase, abort_flag)) {
                     atomicExch(err, 1);
                     *abort_flag = 1;
@@ -427,28 +460,33 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 tc_fence_after();
 #pragma unroll
-                for (int c = 0; c < DBN; c += 32) {
-                    uint32_t r[32];
-                    tmem_ld32(tmem + slot * DBN + c + ((uint32_t)(q * 32) << 16), r);
+                for (int c = 0; c < CW; c += 64) {
+                    uint32_t r[64];
+                    tmem_ld64(tmem + slot * BNT + cb + c + ((uint32_t)(q * 32) << 16), r);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) acc[c + j] += __uint_as_float(r[j]);
+                    for (int j = 0; j < 32; ++j)
+                        acc[c / 2 + j] =
+                            __fadd2_rn(acc[c / 2 + j], make_float2(__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])));
                 }
                 tc_fence_before();
                 mbar_arrive(tempty0 + 8 * slot);
-                if (++slot == DSLOTS) { slot = 0; slot_phase ^= 1; }
+                if (++slot == SLOTS) { slot = 0; slot_phase ^= 1; }
             }
             if (!ok) break;
             const int row = mb * BM + q * 32 + lane;
-            const int col0 = nb * DBN;
+            const int col0 = nb * BNT + cb;
             if (row < M) {
                 float* dst = C + (long long)row * ldc + col0;
-                if (vec && col0 + DBN <= N) {
+                if (vec && col0 + CW <= N) {
 #pragma unroll
-                    for (int j = 0; j < DBN; j += 4) *(float4*)(dst + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+                    for (int j = 0; j < CW / 2; j += 2)
+                        *(float4*)(dst + 2 * j) = make_float4(acc[j].x, acc[j].y, acc[j + 1].x, acc[j + 1].y);
                 } else {
 #pragma unroll
-                    for (int j = 0; j < DBN; ++j)
-                        if (col0 + j < N) dst[j] = acc[j];
+                    for (int j = 0; j < CW / 2; ++j) {
+                        if (col0 + 2 * j < N) dst[2 * j] = acc[j].x;
+                        if (col0 + 2 * j + 1 < N) dst[2 * j + 1] = acc[j].y;
+                    }
                 }
             }
         }
@@ -517,32 +555,40 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     return AFQ_OK;
 }
 
-static bool g_drain_attr = false;
+template <int BNT>
+static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                        long long ldc, int kd, int* err, cudaStream_t s) {
+    using namespace tc;
+    static bool attr = false;
+    CUtensorMap ma, mb;
+    AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
+    AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT));
+    if (!attr) {
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Drain<BNT>::SMEM));
+        attr = true;
+    }
+    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
+    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+    k_gemm_tn_drain<BNT><<<grid, DTHREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, M, N, K, ldc, kd, err);
+    AFQ_LAUNCHED("k_gemm_tn_drain");
+    return AFQ_OK;
+}
 
 int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
-                            long long ldc, int* err, cudaStream_t s) {
+                            long long ldc, int* err, cudaStream_t s, int kd) {
     using namespace tc;
     if (M <= 0 || N <= 0) return AFQ_OK;
     if (K <= 0 || K % BK) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: K=%d must be a positive multiple of %d", K, BK);
     AFQ_TRY(get_encode());
-    CUtensorMap ma, mb;
-    AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
-    AFQ_TRY(make_map(&mb, B, N, K, ldb, DBN));
     if (!g_num_sms) {
         int dev = 0;
         AFQ_CUDA(cudaGetDevice(&dev));
         AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
         AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     }
-    if (!g_drain_attr) {
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain, cudaFuncAttributeMaxDynamicSharedMemorySize, DSMEM_BYTES));
-        g_drain_attr = true;
-    }
-    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + DBN - 1) / DBN);
-    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    k_gemm_tn_drain<<<grid, THREADS, DSMEM_BYTES, s>>>(ma, mb, C, M, N, K, ldc, err);
-    AFQ_LAUNCHED("k_gemm_tn_drain");
-    return AFQ_OK;
+    if (kd < 1) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: k blocks per partial %d < 1", kd);
+    return launch_drain<128>(M, N, K, A, lda, B, ldb, C, ldc, kd, err, s);
 }
 
 }  // namespace afq

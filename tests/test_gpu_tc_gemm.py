@@ -27,7 +27,7 @@ def gemm(A, B, M, N, K, ldc=None, accumulate=1):
     return C
 
 
-@pytest.mark.parametrize("accumulate", [0, 1])
+@pytest.mark.parametrize("accumulate", [0, 1, 3])
 @pytest.mark.parametrize("M,N,K,padk,ldc_pad", [(128, 256, 64, 0, 0), (300, 1000, 192, 8, 0), (129, 257, 128, 0, 3),
                                                  (1, 16, 64, 0, 0), (2048, 4096, 1024, 0, 0)])
 def test_tc_gemm_matches_fp32(cuda, M, N, K, padk, ldc_pad, accumulate):
