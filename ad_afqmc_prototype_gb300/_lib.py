@@ -21,6 +21,7 @@ AFQ_E_DEVICE_CHECK = -5
 
 AFQ_PREC_FP64 = 0
 AFQ_PREC_MIXED = 1
+AFQ_PREC_MIXED_FAST = 2
 
 
 class afq_dims(Structure):

@@ -39,7 +39,7 @@ static int check_dims(const afq_dims* d, bool need_chol = true) {
     if (d->nocc > 64) return fail(AFQ_E_UNSUPPORTED, "nocc=%d > 64", d->nocc);
     if (d->norb > 512) return fail(AFQ_E_UNSUPPORTED, "norb=%d > 512", d->norb);
     if (need_chol && d->nchol < 1) return fail(AFQ_E_INVALID_ARGUMENT, "nchol=%d < 1", d->nchol);
-    if (d->precision != AFQ_PREC_FP64 && d->precision != AFQ_PREC_MIXED)
+    if (d->precision != AFQ_PREC_FP64 && !is_mixed(d->precision))
         return fail(AFQ_E_INVALID_ARGUMENT, "unknown precision %d", d->precision);
     return AFQ_OK;
 }
@@ -63,18 +63,20 @@ struct LowpDims {
     int S_V, Kt_V;   // V-build:    x~ (2W x G)       . L   (n^2 x G)
     int S_F, Kt_F;   // force bias: G_half (2W x o n) . L~  (G x o n)
     int S_E, Kt_E;   // energy:     L~ (G o x n)      . G_half rows (2 o W x n)
+    int sec;         // sections per split row (6 or 3)
     long long ldv;   // row stride of V (fp32)
 };
 
 static LowpDims lowp_dims(const afq_dims* d) {
     LowpDims L;
     const int n = d->norb, o = d->nocc, G = d->nchol;
+    L.sec = split_sections(d->precision);
     L.S_V = G;
-    L.Kt_V = (int)round_up((long long)kSplit * G, 64);
+    L.Kt_V = (int)round_up((long long)L.sec * G, 64);
     L.S_F = o * n;
-    L.Kt_F = (int)round_up((long long)kSplit * o * n, 64);
+    L.Kt_F = (int)round_up((long long)L.sec * o * n, 64);
     L.S_E = n;
-    L.Kt_E = (int)round_up((long long)kSplit * n, 64);
+    L.Kt_E = (int)round_up((long long)L.sec * n, 64);
     L.ldv = round_up((long long)n * n, 4);
     return L;
 }
@@ -121,7 +123,7 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
     s.shift_term = a.take<double2>(W);
     s.fb_term = a.take<double2>(W);
     s.ovl_new = a.take<double2>(W);
-    if (d->precision == AFQ_PREC_MIXED) {
+    if (is_mixed(d->precision)) {
         const LowpDims L = lowp_dims(d);
         s.Ag = a.take<__nv_bfloat16>(2 * W * L.Kt_F);
         s.fbm = a.take<float>(2 * W * G);
@@ -165,9 +167,9 @@ static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
     BlockWS b = {};
     b.step = layout_step(a, d, n_chunks);
     const size_t W = d->n_walkers;
-    b.green = d->precision == AFQ_PREC_MIXED ? a.take<double2>(W * d->nocc * d->norb) : b.step.green;
+    b.green = is_mixed(d->precision) ? a.take<double2>(W * d->nocc * d->norb) : b.step.green;
     b.energy = a.take<double2>(W);
-    if (d->precision == AFQ_PREC_MIXED) {
+    if (is_mixed(d->precision)) {
         const LowpDims L = lowp_dims(d);
         const size_t we = energy_chunk(d);
         b.partial = (double*)a.take<double2>(W * exchange_chunks(d->nchol) * 2);
@@ -221,7 +223,7 @@ static int check_problem(const afq_problem* pb) {
     AFQ_NOTNULL(pb->rot_h1);
     AFQ_NOTNULL(pb->rot_chol);
     if (!(pb->dt > 0.0)) return fail(AFQ_E_INVALID_ARGUMENT, "dt=%g must be > 0", pb->dt);
-    if (pb->dims.precision == AFQ_PREC_MIXED) {
+    if (is_mixed(pb->dims.precision)) {
         if (!pb->lowp) return fail(AFQ_E_INVALID_ARGUMENT, "precision MIXED needs afq_prepare_lowp() output in lowp");
         if (!pb->dims.trial_is_real)
             return fail(AFQ_E_UNSUPPORTED, "precision MIXED supports real trial orbitals only");
@@ -240,6 +242,7 @@ static SplitOut fb_split(const afq_dims* d, const StepWS& ws) {
     so.W = d->n_walkers;
     so.ld = L.Kt_F;
     so.S = L.S_F;
+    so.sec = L.sec;
     return so;
 }
 
@@ -265,7 +268,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     const int Wc = chunk_size(W, p->n_chunks);
     { AFQ_PHASE("field_shift", s);
       AFQ_TRY(launch_field_shift_mixed(W, G, Wc, pb->sqrt_dt, fields, ws.fbm, G, (const double2*)pb->mf_shifts, ws.Av,
-                                       L.S_V, L.Kt_V, ws.shift_term, ws.fb_term, s)); }
+                                       L.S_V, L.Kt_V, L.sec, ws.shift_term, ws.fb_term, s)); }
     AFQ_TRY(launch_e_minus_i(n, pb->exp_h1_half, ws.emi, s));
     for (int w0 = 0; w0 < W; w0 += Wc) {
         const int wc = W - w0 < Wc ? W - w0 : Wc;
@@ -293,7 +296,7 @@ static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS
       AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
                            nullptr, ws.green, s)); }
     AFQ_PHASE("energy", s);
-    if (d->precision != AFQ_PREC_MIXED)
+    if (!is_mixed(d->precision))
         return launch_energy(W, n, o, G, pb->h0, ws.green, pb->rot_chol, d->trial_is_real,
                              (const double2*)pb->rot_h1, ws.partial, ws.energy, s);
     const LowpDims L = lowp_dims(d);
@@ -303,12 +306,15 @@ static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS
     double2* partial = (double2*)ws.partial;
     for (int w0 = 0; w0 < W; w0 += We) {
         const int wc = W - w0 < We ? W - w0 : We;
-        AFQ_TRY(launch_green_rows(wc, n, o, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, s));
-        // F[(w, part, k), (g, i)]: the sections of Bg ([hi lo hi]) and Le
-        // ([hi hi lo]) still pair up as hi.hi + lo.hi + hi.lo
-        AFQ_TRY(launch_tc_gemm_tn_drain(2 * o * wc, G * o, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.F, (long long)G * o,
-                                  ws.step.status, s));
-        AFQ_TRY(launch_exchange_reduce(wc, G, o, ws.F, (long long)G * o, partial + (size_t)w0 * nch * 2, s));
+        { AFQ_PHASE("e_green_rows", s);
+          AFQ_TRY(launch_green_rows(wc, n, o, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, L.sec, s)); }
+        // F[(w, part, k), (g, i)]: the six sections of Bg (left) and Le
+        // (right) pair up as hh + hm + mh + hl + lh + mm
+        { AFQ_PHASE("e_gemm", s);
+          AFQ_TRY(launch_tc_gemm_tn_drain(2 * o * wc, G * o, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.F,
+                                          (long long)G * o, ws.step.status, s)); }
+        { AFQ_PHASE("e_exchange", s);
+          AFQ_TRY(launch_exchange_reduce(wc, G, o, ws.F, (long long)G * o, partial + (size_t)w0 * nch * 2, s)); }
     }
     return launch_energy_finish(W, n, o, nch, pb->h0, ws.green, (const double2*)pb->rot_h1, partial, ws.energy, s);
 }
@@ -342,7 +348,7 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
         AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
         fields = ws.fields;
     }
-    if (d->precision == AFQ_PREC_MIXED) return step_mixed(pb, p, st, fields, ws, green_ready, s);
+    if (is_mixed(d->precision)) return step_mixed(pb, p, st, fields, ws, green_ready, s);
     // force bias (prop/afqmc.py:90-95)
     { AFQ_PHASE("green", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s)); }
     { AFQ_PHASE("fb_gemm", s); AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s)); }
@@ -370,7 +376,7 @@ static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cu
     double2* walk = (double2*)st->walkers;
     { AFQ_PHASE("qr", s); AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s)); }
     AFQ_PHASE("overlap", s);
-    if (ws && d->precision == AFQ_PREC_MIXED)
+    if (ws && is_mixed(d->precision))
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
                                     (double2*)st->overlaps, fb_split(d, *ws), s);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
@@ -496,11 +502,11 @@ int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_ch
     const long long n = d->norb, o = d->nocc, G = d->nchol;
     cudaStream_t s = as_stream(stream);
     // chol^T: row j = (i, k) of L_g[i, k] over g   (right operand of the V-build)
-    AFQ_TRY(launch_split_rows(n * n, (int)G, L.S_V, L.Kt_V, chol, 1, n * n, b.Bv, 0, s));
+    AFQ_TRY(launch_split_rows(n * n, (int)G, L.S_V, L.Kt_V, chol, 1, n * n, b.Bv, 0, L.sec, s));
     // rot_chol_flat: row g over (p, j)              (right operand of the force bias)
-    AFQ_TRY(launch_split_rows(G, (int)(o * n), L.S_F, L.Kt_F, rot_chol, o * n, 1, b.Bf, 0, s));
+    AFQ_TRY(launch_split_rows(G, (int)(o * n), L.S_F, L.Kt_F, rot_chol, o * n, 1, b.Bf, 0, L.sec, s));
     // rot_chol rows (g, p) over j                   (left operand of the energy)
-    AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, s));
+    AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, L.sec, s));
     return AFQ_OK;
 }
 

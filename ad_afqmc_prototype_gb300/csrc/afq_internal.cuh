@@ -86,13 +86,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 // -------------------------------------------- bf16 hi/lo split operands --
 // x = h + m + l with h = bf16(x), m = bf16(x - h), l = bf16(x - h - m):
 // three bf16 pieces carry 24 significant bits (an fp32 value exactly).  A row
-// of a split operand holds kSplit K sections starting at 0, S, 2S, ... (S >= K)
-// and is zero from kSplit*S up to its length Kt (a multiple of 64): a left (A)
-// operand stores [h h m h l m], a right (B) operand [h m h l h m], so that
-// A . B^T sums hh + hm + mh + hl + lh + mm -- every product above 2^-24
-// relative.  (bf16 has 8 significant bits, so a two-piece split would keep
-// only ~16 bits.)
-constexpr int kSplit = 6;
+// of a split operand holds `sec` K sections starting at 0, S, 2S, ... (S >= K)
+// and is zero from sec*S up to its length Kt (a multiple of 64).  Six
+// sections (AFQ_PREC_MIXED): a left (A) operand stores [h h m h l m], a
+// right (B) operand [h m h l h m], so that A . B^T sums hh + hm + mh + hl +
+// lh + mm -- every product above 2^-24 relative.  Three sections
+// (AFQ_PREC_MIXED_FAST): [h h m] and [h m h], hh + hm + mh, ~2^-17 relative
+// (bf16 has 8 significant bits).
+inline int split_sections(int precision) { return precision == AFQ_PREC_MIXED_FAST ? 3 : 6; }
+inline bool is_mixed(int precision) { return precision == AFQ_PREC_MIXED || precision == AFQ_PREC_MIXED_FAST; }
 
 template <class T>
 __device__ __forceinline__ void split_pieces(T x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l);
@@ -113,22 +115,24 @@ __device__ __forceinline__ void split_pieces<float>(float x, __nv_bfloat16& h, _
 }
 
 template <class T>
-__device__ __forceinline__ void split_store_t(__nv_bfloat16* row, int S, int k, T x, bool left) {
+__device__ __forceinline__ void split_store_t(__nv_bfloat16* row, int S, int k, T x, bool left, int sec) {
     __nv_bfloat16 h, m, l;
     split_pieces<T>(x, h, m, l);
     row[k] = h;
     row[S + k] = left ? h : m;
     row[2 * S + k] = left ? m : h;
-    row[3 * S + k] = left ? h : l;
-    row[4 * S + k] = left ? l : h;
-    row[5 * S + k] = m;
+    if (sec > 3) {
+        row[3 * S + k] = left ? h : l;
+        row[4 * S + k] = left ? l : h;
+        row[5 * S + k] = m;
+    }
 }
-__device__ __forceinline__ void split_store(__nv_bfloat16* row, int S, int k, double x, bool left) {
-    split_store_t<double>(row, S, k, x, left);
+__device__ __forceinline__ void split_store(__nv_bfloat16* row, int S, int k, double x, bool left, int sec) {
+    split_store_t<double>(row, S, k, x, left, sec);
 }
 // Same split of an fp32 value, on the fp32 pipe.
-__device__ __forceinline__ void split_storef(__nv_bfloat16* row, int S, int k, float x, bool left) {
-    split_store_t<float>(row, S, k, x, left);
+__device__ __forceinline__ void split_storef(__nv_bfloat16* row, int S, int k, float x, bool left, int sec) {
+    split_store_t<float>(row, S, k, x, left, sec);
 }
 
 // Destination of a split left operand written by a per-walker kernel: walker
@@ -138,6 +142,7 @@ struct SplitOut {
     int W = 0;
     long long ld = 0;  // row length Kt
     int S = 0;         // section stride
+    int sec = 6;       // sections per row
 };
 
 // ------------------------------------------------------------- workspace --
@@ -223,10 +228,10 @@ int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const doubl
 
 // k_mixed.cu
 int launch_split_rows(long long rows, int K, int S, int Kt, const double* src, long long rs, long long ks,
-                      __nv_bfloat16* dst, int left, cudaStream_t s);
+                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s);
 int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s);
 int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
-                             const double2* mf, __nv_bfloat16* av, int S, int Kt, double2* shift_term,
+                             const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
                              double2* fb_term, cudaStream_t s);
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
                          long long ldv, const double2* win, double2* wout, cudaStream_t s);
@@ -234,7 +239,8 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
                          SplitOut split, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
-int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, cudaStream_t s);
+int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
+                      cudaStream_t s);
 
 inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 

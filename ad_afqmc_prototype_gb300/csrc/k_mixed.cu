@@ -16,7 +16,7 @@ namespace afq {
 // entries [3S, Kt) and [K, S) of each section are zero.
 // src(r, k) = src[r * rs + k * ks].
 __global__ void k_split_rows(long long rows, int K, int S, int Kt, const double* __restrict__ src, long long rs,
-                             long long ks, __nv_bfloat16* __restrict__ dst, int left) {
+                             long long ks, __nv_bfloat16* __restrict__ dst, int left, int sec) {
     const long long total = rows * (long long)Kt;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
@@ -25,19 +25,19 @@ __global__ void k_split_rows(long long rows, int K, int S, int Kt, const double*
         __nv_bfloat16* row = dst + r * Kt;
         if (kk < S) {
             const double x = kk < K ? src[r * rs + (long long)kk * ks] : 0.0;
-            split_store(row, S, kk, x, left != 0);
-        } else if (kk >= kSplit * S) {
+            split_store(row, S, kk, x, left != 0, sec);
+        } else if (kk >= sec * S) {
             row[kk] = __double2bfloat16(0.0);
         }
     }
 }
 
 int launch_split_rows(long long rows, int K, int S, int Kt, const double* src, long long rs, long long ks,
-                      __nv_bfloat16* dst, int left, cudaStream_t s) {
+                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s) {
     const long long total = rows * (long long)Kt;
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_split_rows<<<(unsigned)blocks, 256, 0, s>>>(rows, K, S, Kt, src, rs, ks, dst, left);
+    k_split_rows<<<(unsigned)blocks, 256, 0, s>>>(rows, K, S, Kt, src, rs, ks, dst, left, sec);
     AFQ_LAUNCHED("k_split_rows");
     return AFQ_OK;
 }
@@ -61,8 +61,8 @@ int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s) {
 // per walker chunk [w0, w0 + wc) the Re rows come first, then the Im rows.
 __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* __restrict__ x,
                                     const float* __restrict__ fbm, long long ldf, const double2* __restrict__ mf,
-                                    __nv_bfloat16* __restrict__ av, int S, int Kt, double2* __restrict__ shift_term,
-                                    double2* __restrict__ fb_term) {
+                                    __nv_bfloat16* __restrict__ av, int S, int Kt, int sec,
+                                    double2* __restrict__ shift_term, double2* __restrict__ fb_term) {
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= W) return;
@@ -79,18 +79,18 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
             const double xv = x[(size_t)w * G + g];
             const double2 fs = make_double2(-sqrt_dt * (-f.y - m.x), -sqrt_dt * (f.x - m.y));
             const double2 xt = make_double2(xv - fs.x, -fs.y);
-            split_store(re_row, S, g, xt.x, true);
-            split_store(im_row, S, g, xt.y, true);
+            split_store(re_row, S, g, xt.x, true, sec);
+            split_store(im_row, S, g, xt.y, true, sec);
             sr += xt.x * m.x - xt.y * m.y;
             si += xt.x * m.y + xt.y * m.x;
             br += xv * fs.x - 0.5 * (fs.x * fs.x - fs.y * fs.y);
             bi += xv * fs.y - 0.5 * (2.0 * fs.x * fs.y);
         } else {
-            split_store(re_row, S, g, 0.0, true);
-            split_store(im_row, S, g, 0.0, true);
+            split_store(re_row, S, g, 0.0, true, sec);
+            split_store(im_row, S, g, 0.0, true, sec);
         }
     }
-    for (int k = kSplit * S + lane; k < Kt; k += 32) {
+    for (int k = sec * S + lane; k < Kt; k += 32) {
         re_row[k] = __double2bfloat16(0.0);
         im_row[k] = __double2bfloat16(0.0);
     }
@@ -102,9 +102,9 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
 }
 
 int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
-                             const double2* mf, __nv_bfloat16* av, int S, int Kt, double2* shift_term,
+                             const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
                              double2* fb_term, cudaStream_t s) {
-    k_field_shift_mixed<<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, shift_term,
+    k_field_shift_mixed<<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec, shift_term,
                                                     fb_term);
     AFQ_LAUNCHED("k_field_shift_mixed");
     return AFQ_OK;
@@ -556,16 +556,16 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
         for (int j = 0; j < BG; ++j) {
             const int b = bg * BG + j;
             if (b < o) {
-                split_storef(re_row, split.S, b * n + i, acc[j].x, true);
-                split_storef(im_row, split.S, b * n + i, acc[j].y, true);
+                split_storef(re_row, split.S, b * n + i, acc[j].x, true, split.sec);
+                split_storef(im_row, split.S, b * n + i, acc[j].y, true, split.sec);
             }
         }
     }
     for (int e = n * o + tid; e < split.S; e += blockDim.x) {
-        split_storef(re_row, split.S, e, 0.f, true);
-        split_storef(im_row, split.S, e, 0.f, true);
+        split_storef(re_row, split.S, e, 0.f, true, split.sec);
+        split_storef(im_row, split.S, e, 0.f, true, split.sec);
     }
-    for (long long e = (long long)kSplit * split.S + tid; e < split.ld; e += blockDim.x) {
+    for (long long e = (long long)split.sec * split.S + tid; e < split.ld; e += blockDim.x) {
         re_row[e] = __float2bfloat16(0.f);
         im_row[e] = __float2bfloat16(0.f);
     }
@@ -604,34 +604,67 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
 // GEMM produced F[(w, part, k), (g, i)] = sum_j G_part[w, k, j] L~[g, i, j]
 // (part 0 = Re, 1 = Im of G_half), so each walker's f_g blocks lie along
 // contiguous runs of a row; this kernel forms, per walker and chunk of
-// Cholesky vectors, sum_g c_g^2 and sum_g sum_ik f_g[i,k] f_g[k,i] in fp64.
+// Cholesky vectors, sum_g c_g^2 and sum_g sum_ik f_g[i,k] f_g[k,i].
+// The chunk's rows are copied into shared memory as they lie in F (plane
+// part, row k, column g o + i = f_g[i,k]) by cp.async, all copies in flight
+// at once.  The fp32 products of one f_g are summed per thread in fp32 (a
+// few terms) and those sums accumulate in fp64.
 constexpr int EX_G = 8;  // Cholesky vectors per CTA
 __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const float* __restrict__ F, long long ldf,
-                                                         double2* __restrict__ partial, int nchunk) {
-    extern __shared__ float2 fs[];  // EX_G x o x o complex, fs[(g o + i) o + k] = f_g[i, k]
+                                                         double2* __restrict__ partial, int nchunk, int v16) {
+    extern __shared__ float fsm[];  // [part][k][RS]: RS = EX_G o + 4 (16-byte rows, shifted banks)
     const int w = blockIdx.y, g0 = blockIdx.x * EX_G;
     const int ng = min(EX_G, G - g0);
-    const int oo = o * o;
-    for (int e = threadIdx.x; e < ng * oo; e += blockDim.x) {
-        const int i = e % o, k = (e / o) % o, g = e / oo;  // i fastest: contiguous columns (g, i)
-        const long long col = (long long)(g0 + g) * o + i;
-        const float re = F[(long long)((2 * w) * o + k) * ldf + col];
-        const float im = F[(long long)((2 * w + 1) * o + k) * ldf + col];
-        fs[(g * o + i) * o + k] = make_float2(re, im);
+    const int oo = o * o, nc = ng * o, RS = EX_G * o + 4;
+    float* Pr = fsm;
+    float* Pi = fsm + o * RS;
+    const float* Fr = F + (long long)(2 * w) * o * ldf + (long long)g0 * o;
+    const float* Fi = F + (long long)(2 * w + 1) * o * ldf + (long long)g0 * o;
+    if (v16 && (nc & 3) == 0) {
+        const int q = nc / 4;  // 16-byte chunks per row
+        for (int e = threadIdx.x; e < 2 * o * q; e += blockDim.x) {
+            const int c = e % q, r = e / q, part = r / o, k = r % o;
+            cp_async16((part ? Pi : Pr) + k * RS + 4 * c, (part ? Fi : Fr) + (long long)k * ldf + 4 * c);
+        }
+    } else {
+        for (int e = threadIdx.x; e < 2 * o * nc; e += blockDim.x) {
+            const int c = e % nc, r = e / nc, part = r / o, k = r % o;
+            cp_async4((part ? Pi : Pr) + k * RS + c, (part ? Fi : Fr) + (long long)k * ldf + c);
+        }
     }
+    cp_async_commit();
+    // this thread's (i, k) entries, the same for every g: offsets of f[i,k] and f[k,i]
+    constexpr int EX_R = 64 * 64 / 256;  // nocc <= 64
+    int oa[EX_R], ob[EX_R];
+#pragma unroll
+    for (int j = 0; j < EX_R; ++j) {
+        const int r = threadIdx.x + 256 * j, i = r / o, k = r % o;
+        oa[j] = r < oo ? k * RS + i : -1;  // f[i,k] at row k, column i
+        ob[j] = i * RS + k;                // f[k,i] at row i, column k
+    }
+    cp_async_wait_all();
     __syncthreads();
     double xr = 0.0, xi = 0.0, cr = 0.0, ci = 0.0;
-    for (int e = threadIdx.x; e < ng * oo; e += blockDim.x) {
-        const int g = e / oo, r = e % oo, i = r / o, k = r % o;
-        const float2 a = fs[e], b = fs[g * oo + k * o + i];
-        xr += (double)a.x * b.x - (double)a.y * b.y;
-        xi += (double)a.x * b.y + (double)a.y * b.x;
+    for (int g = 0; g < ng; ++g) {
+        const float* fr = Pr + g * o;
+        const float* fi = Pi + g * o;
+        float sr = 0.f, si = 0.f;
+#pragma unroll
+        for (int j = 0; j < EX_R; ++j) {
+            if (oa[j] >= 0) {
+                const float ar = fr[oa[j]], ai = fi[oa[j]], br = fr[ob[j]], bi = fi[ob[j]];
+                sr = fmaf(ar, br, fmaf(-ai, bi, sr));
+                si = fmaf(ar, bi, fmaf(ai, br, si));
+            }
+        }
+        xr += (double)sr;
+        xi += (double)si;
     }
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
         double tr = 0.0, ti = 0.0;
         for (int i = 0; i < o; ++i) {
-            tr += fs[g * oo + i * o + i].x;
-            ti += fs[g * oo + i * o + i].y;
+            tr += Pr[i * RS + g * o + i];
+            ti += Pi[i * RS + g * o + i];
         }
         cr += tr * tr - ti * ti;
         ci += 2.0 * tr * ti;
@@ -654,10 +687,11 @@ int exchange_chunks(int G) { return (G + EX_G - 1) / EX_G; }
 
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s) {
     if (wc <= 0) return AFQ_OK;
-    const size_t smem = (size_t)EX_G * o * o * sizeof(float2);
+    const size_t smem = (size_t)2 * o * (EX_G * o + 4) * sizeof(float);
     AFQ_TRY(smem_attr(k_exchange_reduce, smem));
+    const int v16 = (ldf % 4) == 0 && (((uintptr_t)F) & 15) == 0;
     dim3 grid(exchange_chunks(G), wc);
-    k_exchange_reduce<<<grid, 256, smem, s>>>(G, o, F, ldf, partial, exchange_chunks(G));
+    k_exchange_reduce<<<grid, 256, smem, s>>>(G, o, F, ldf, partial, exchange_chunks(G), v16);
     AFQ_LAUNCHED("k_exchange_reduce");
     return AFQ_OK;
 }
@@ -665,7 +699,7 @@ int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, 
 // Green's function rows for the energy GEMM: row (w*2 + part)*o + k holds
 // split(G_part[w, k, :]) with K = n in sections of S.
 __global__ void k_green_rows(int wc, int n, int o, const double2* __restrict__ green, __nv_bfloat16* __restrict__ dst,
-                             int S, int Kt) {
+                             int S, int Kt, int sec) {
     const long long rows = (long long)wc * o * 2;
     const long long total = rows * (long long)Kt;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -680,18 +714,19 @@ __global__ void k_green_rows(int wc, int n, int o, const double2* __restrict__ g
                 const double2 v = green[((size_t)w * o + k) * n + kk];
                 x = part ? v.y : v.x;
             }
-            split_store(row, S, kk, x, false);
-        } else if (kk >= kSplit * S) {
+            split_store(row, S, kk, x, false, sec);
+        } else if (kk >= sec * S) {
             row[kk] = __double2bfloat16(0.0);
         }
     }
 }
 
-int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, cudaStream_t s) {
+int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
+                      cudaStream_t s) {
     const long long total = (long long)wc * o * 2 * Kt;
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_green_rows<<<(unsigned)blocks, 256, 0, s>>>(wc, n, o, green, dst, S, Kt);
+    k_green_rows<<<(unsigned)blocks, 256, 0, s>>>(wc, n, o, green, dst, S, Kt, sec);
     AFQ_LAUNCHED("k_green_rows");
     return AFQ_OK;
 }

@@ -69,6 +69,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 // Bounded wait for the phase with `parity`; false on timeout or abort.
+__device__ __forceinline__ bool mbar_wait_inl(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (abort_flag && *abort_flag) return false;
+        if (now_ns() - t0 > WAIT_NS) return false;
+    }
+}
 __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = now_ns();
@@ -291,11 +300,18 @@ __global__ void __launch_bounds__(THREADS, 1)
 // round-to-nearest adds (two lanes per instruction) while the MMA thread
 // fills the next slot.  Warp w may only read TMEM lanes 32*(w%4)..+31, so
 // warps 2-5 and 6-9 each cover all 128 rows, one column half each.
-constexpr int DTHREADS = 320;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-9: epilogue
 constexpr int DTMEM_COLS = 512;
 
+// BNT = 128: 320 threads (warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9
+// epilogue), each epilogue thread sums 64 columns of one row.
+// BNT = 256: 384 threads; warpgroup 0 (warps 0-3: TMA, MMA, two idle) gives
+// registers back (setmaxnreg 40) to warpgroups 1-2 (warps 4-11, epilogue,
+// setmaxnreg 232), whose threads sum 128 columns of one row.  Launched at
+// 168 registers a thread: 128 x 40 + 256 x 232 = 384 x 168.
 template <int BNT>
 struct Drain {
+    static constexpr int THREADS = BNT == 128 ? 320 : 384;
+    static constexpr int EW0 = BNT == 128 ? 2 : 4;  // first epilogue warp
     static constexpr int SLOTS = DTMEM_COLS / BNT;
     static constexpr int STG = BNT == 128 ? 6 : 4;
     static constexpr int B_BYTES = BNT * BK * 2;
@@ -305,6 +321,8 @@ struct Drain {
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BNT >> 3) << 17) |
                                       ((uint32_t)(BM >> 4) << 24);
 };
+constexpr int DREG_LAUNCH = 168, DREG_PRODUCER = 40, DREG_EPILOGUE = 232;
+static_assert(128 * DREG_PRODUCER + 256 * DREG_EPILOGUE <= 384 * DREG_LAUNCH, "register split exceeds the launch");
 
 __device__ __forceinline__ void umma_bf16_i(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                             uint32_t accumulate) {
@@ -335,7 +353,7 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
 #undef AFQ_R8
 
 template <int BNT>
-__global__ void __launch_bounds__(DTHREADS, 1)
+__global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, int M, int N, int K, long long ldc, int kd, int* __restrict__ err) {
     using D = Drain<BNT>;
@@ -362,7 +380,7 @@ __global__ void __launch_bounds__(DTHREADS, 1)
         }
         for (int a = 0; a < SLOTS; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, DTHREADS - 64);
+            mbar_init(tempty0 + 8 * a, 256);  // eight epilogue warps
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -440,8 +458,8 @@ __global__ void __launch_bounds__(DTHREADS, 1)
                 mbar_wait(drain, 0, nullptr);
             }
         }
-    } else {
-        const int q = warp & 3, cb = ((warp - 2) >> 2) * CW;
+    } else if (warp >= D::EW0) {
+        const int q = warp & 3, cb = ((warp - D::EW0) >> 2) * CW;
         int slot = 0;
         uint32_t slot_phase = 0;
         const bool vec = (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
@@ -452,21 +470,37 @@ __global__ void __launch_bounds__(DTHREADS, 1)
 #pragma unroll
             for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
             for (int p = 0; p < np; ++p) {
-                if (!mbar_wait(tfull0 + 8 * slot, slot_phase, abort_flag)) {
+                if (!mbar_wait_inl(tfull0 + 8 * slot, slot_phase, abort_flag)) {
                     atomicExch(err, 1);
                     *abort_flag = 1;
                     ok = false;
                     break;
                 }
                 tc_fence_after();
+                // chunks of LC columns; the sums of a chunk are complete before the
+                // next load, so at most LC staged values are live
+                constexpr int LC = BNT == 128 ? 64 : 32;
 #pragma unroll
-                for (int c = 0; c < CW; c += 64) {
-                    uint32_t r[64];
-                    tmem_ld64(tmem + slot * BNT + cb + c + ((uint32_t)(q * 32) << 16), r);
+                for (int c = 0; c < CW; c += LC) {
+                    uint32_t r[LC];
+                    const uint32_t ta = tmem + slot * BNT + cb + c + ((uint32_t)(q * 32) << 16);
+                    if constexpr (LC == 64) tmem_ld64(ta, r);
+                    else tmem_ld32(ta, r);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        acc[c / 2 + j] =
-                            __fadd2_rn(acc[c / 2 + j], make_float2(__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])));
+                    for (int j = 0; j < LC / 2; ++j) {
+                        if constexpr (BNT == 128) {
+                            acc[c / 2 + j] = __fadd2_rn(acc[c / 2 + j], make_float2(__uint_as_float(r[2 * j]),
+                                                                                    __uint_as_float(r[2 * j + 1])));
+                        } else {  // scalar adds: fewer registers than paired ones at 128 sums a thread
+                            acc[c / 2 + j].x += __uint_as_float(r[2 * j]);
+                            acc[c / 2 + j].y += __uint_as_float(r[2 * j + 1]);
+                        }
+                    }
+                    if constexpr (BNT == 128) {
+#pragma unroll
+                        for (int j = 0; j < LC / 2; ++j)
+                            asm volatile("" : "+f"(acc[c / 2 + j].x), "+f"(acc[c / 2 + j].y));
+                    }
                 }
                 tc_fence_before();
                 mbar_arrive(tempty0 + 8 * slot);
@@ -570,7 +604,7 @@ static int launch_drain(int M, int N, int K, const void* A, long long lda, const
     }
     const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
     const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    k_gemm_tn_drain<BNT><<<grid, DTHREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, M, N, K, ldc, kd, err);
+    k_gemm_tn_drain<BNT><<<grid, Drain<BNT>::THREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, M, N, K, ldc, kd, err);
     AFQ_LAUNCHED("k_gemm_tn_drain");
     return AFQ_OK;
 }

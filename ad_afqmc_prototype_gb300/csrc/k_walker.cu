@@ -173,18 +173,18 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
             for (int j = 0; j < BG; ++j) {
                 const int b = bg * BG + j;
                 if (b < o) {
-                    split_store(re_row, split.S, b * n + i, (double)acc[j].x, true);
-                    split_store(im_row, split.S, b * n + i, (double)acc[j].y, true);
+                    split_store(re_row, split.S, b * n + i, (double)acc[j].x, true, split.sec);
+                    split_store(im_row, split.S, b * n + i, (double)acc[j].y, true, split.sec);
                 }
             }
         }
     }
     {  // zero the section gaps and the tail of the row
         for (int e = n * o + tid; e < split.S; e += blockDim.x) {
-            split_store(re_row, split.S, e, 0.0, true);
-            split_store(im_row, split.S, e, 0.0, true);
+            split_store(re_row, split.S, e, 0.0, true, split.sec);
+            split_store(im_row, split.S, e, 0.0, true, split.sec);
         }
-        for (long long e = (long long)kSplit * split.S + tid; e < split.ld; e += blockDim.x) {
+        for (long long e = (long long)split.sec * split.S + tid; e < split.ld; e += blockDim.x) {
             re_row[e] = __double2bfloat16(0.0);
             im_row[e] = __double2bfloat16(0.0);
         }

@@ -298,12 +298,15 @@ class Problem:
 
 
 def prepare_lowp(n_walkers: int, norb: int, nocc: int, nchol: int, chol: torch.Tensor,
-                 rot_chol: torch.Tensor) -> torch.Tensor:
-    """bf16 hi/lo split copies of chol and rot_chol in tensor-core operand
-    order, for the mixed-precision step (real trial orbitals only)."""
+                 rot_chol: torch.Tensor, precision: int = _lib.AFQ_PREC_MIXED) -> torch.Tensor:
+    """bf16 split copies of chol and rot_chol in tensor-core operand order,
+    for a mixed-precision step (real trial orbitals only); the layout depends
+    on the precision (six or three sections)."""
     if rot_chol.is_complex():
         raise ValueError("the mixed-precision form supports real trial orbitals only")
-    d = make_dims(n_walkers, norb, nocc, nchol, True, _lib.AFQ_PREC_MIXED)
+    if precision not in (_lib.AFQ_PREC_MIXED, _lib.AFQ_PREC_MIXED_FAST):
+        raise ValueError(f"precision {precision} has no low-precision operands")
+    d = make_dims(n_walkers, norb, nocc, nchol, True, precision)
     lib = _lib.load()
     nb = int(lib.afq_lowp_bytes(ctypes.byref(d)))
     buf = torch.empty((nb,), dtype=torch.uint8, device=chol.device)

@@ -23,7 +23,7 @@ from ..trial.rhf import overlap_r, rhf_trial
 from .chol_afqmc_ops import chol_afqmc_ctx, chol_afqmc_ops
 from .types import PRNGKey, afqmc_params, prop_state, split
 
-_PREC = {"fp64": _lib.AFQ_PREC_FP64, "mixed": _lib.AFQ_PREC_MIXED}
+_PREC = {"fp64": _lib.AFQ_PREC_FP64, "mixed": _lib.AFQ_PREC_MIXED, "mixed_fast": _lib.AFQ_PREC_MIXED_FAST}
 
 
 def init_prop_state(*, sys: system, n_walkers: int, seed: int, ham_data: ham_chol, trial_ops_,
@@ -64,15 +64,15 @@ def engine_problem(*, params, ham_data, trial_data, meas_ops, prop_ops, prop_ctx
         return None
     prec = _PREC.get(str(getattr(params, "precision", "fp64")).lower())
     if prec is None:
-        raise ValueError(f"unknown precision {params.precision!r}; expected 'fp64' or 'mixed'")
+        raise ValueError(f"unknown precision {params.precision!r}; expected 'fp64', 'mixed' or 'mixed_fast'")
     lowp = None
-    if prec == _lib.AFQ_PREC_MIXED:
-        # cached on the measurement context: it depends on chol and rot_chol only
+    if prec != _lib.AFQ_PREC_FP64:
+        # cached on the measurement context: it depends on chol, rot_chol and the precision only
         cached = getattr(meas_ctx, "_lowp", None)
-        if cached is None or cached[0] is not ham_data.chol or cached[1] < n_walkers:
+        if cached is None or cached[0] is not ham_data.chol or cached[1] < n_walkers or cached[3] != prec:
             buf = engine.prepare_lowp(n_walkers, trial_data.norb, trial_data.nocc, int(ham_data.chol.shape[0]),
-                                      ham_data.chol, meas_ctx.rot_chol)
-            cached = (ham_data.chol, n_walkers, buf)
+                                      ham_data.chol, meas_ctx.rot_chol, prec)
+            cached = (ham_data.chol, n_walkers, buf, prec)
             object.__setattr__(meas_ctx, "_lowp", cached)
         lowp = cached[2]
     return engine.Problem(

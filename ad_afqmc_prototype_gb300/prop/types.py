@@ -37,7 +37,7 @@ def split(key: torch.Tensor):
 class afqmc_params:
     """Defaults as prop/types.py:19-32.  Extra fields: ``qr_every`` (an
     orthonormalisation after every qr_every-th step inside a block, 0 = only
-    at block end) and ``precision`` ("fp64" or "mixed")."""
+    at block end) and ``precision`` ("fp64", "mixed" or "mixed_fast")."""
 
     dt: float = 0.005
     n_chunks: int = 1

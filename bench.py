@@ -30,7 +30,8 @@ METRIC = "walker-steps/s at |ΔE|≤0.1 mHa vs FP64 oracle: chosen form vs plain
 UNIT = "walker-steps/s"
 STEPS_PER_BLOCK = 10
 QR_EVERY = 5
-SPLIT_SECTIONS = 6  # bf16 sections of a split tensor-core operand (kSplit in the CUDA sources)
+# bf16 sections of a split tensor-core operand row, per precision (split_sections in the CUDA sources)
+SPLIT_SECTIONS = {"mixed": 6, "mixed_fast": 3}
 
 
 def parse():
@@ -39,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed_fast", choices=["fp64", "mixed", "mixed_fast"])
     ap.add_argument("--workload", default="c4_n200_o30_g1000_w4096")
     ap.add_argument("--walkers", type=int, default=0, help="override the workload's walker count")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
@@ -113,10 +114,11 @@ def _r64(x):
 
 
 def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
-    """(FLOPs per launch, pipe) of each timed phase.  FP64 form: algorithmic
-    real flops.  Mixed form: the tensor-core phases count the flops the
-    tensor cores execute on the bf16 hi/lo split operands (2 M N K with K the
-    three-section row length), the others algorithmic flops on their pipe."""
+    """(work per launch, pipe) of each timed phase.  FP64 form: algorithmic
+    real flops.  Mixed forms: the tensor-core phases count the flops the
+    tensor cores execute on the bf16 split operands (2 M N K with K the split
+    row length), the exchange reduction the bytes of F it must read, the
+    others algorithmic flops on their pipe."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
     work = {
         "vbuild_gemm": (4.0 * G * n * n * W, "fp64"),
@@ -127,24 +129,46 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
         "energy": ((cm * G * o * o * n + 8.0 * G * o * o) * W, "fp64"),
         "qr": ((32.0 * n * o * o - 10.7 * o ** 3) * W, "fp64"),
     }
-    if precision == "mixed":
-        ks = SPLIT_SECTIONS
+    if precision in SPLIT_SECTIONS:
+        ks = SPLIT_SECTIONS[precision]
         work["vbuild_gemm"] = (2.0 * (2 * W) * n * n * _r64(ks * G), "tensor")
         work["fb_gemm"] = (2.0 * (2 * W) * G * _r64(ks * o * n), "tensor")
-        work["energy"] = (2.0 * (G * o) * (2 * o * W) * _r64(ks * n), "tensor")
+        del work["energy"]  # composite phase: e_green_rows + e_gemm + e_exchange
+        work["e_gemm"] = (2.0 * (G * o) * (2 * o * W) * _r64(ks * n), "tensor")
+        work["e_exchange"] = (4.0 * (2 * o * W) * (G * o), "hbm")
         work["trotter"] = ((48.0 + 8.0) * n * n * o * W, "fp32")
     return work
 
 
-def roofline_for(phases, work, lib, steps):
-    """Roofline object of the phase with the largest device time."""
-    dname, (dcalls, dms) = max(phases.items(), key=lambda kv: kv[1][1])
-    if dname not in work:
+def roofline_for(phases, work, lib, steps, name=None):
+    """Roofline object of phase `name`, or of the phase with the largest
+    device time (composite phases that enclose timed sub-phases are not
+    candidates).  work[] is per logical call over all walkers; phases that
+    launch once per walker chunk make several launches per call, so achieved
+    = work x calls per block / device time per block."""
+    leaf = {k: v for k, v in phases.items() if not (k == "energy" and "e_gemm" in phases)}
+    dname = name or max(leaf.items(), key=lambda kv: kv[1][1])[0]
+    if dname not in work or dname not in phases:
         return None
+    dcalls, dms = phases[dname]
     flops, pipe = work[dname]
-    avg_ms = dms / dcalls
-    achieved = flops / (avg_ms / 1000.0) / 1e12
+    chunked = {"vbuild_gemm": STEPS_PER_BLOCK, "trotter": STEPS_PER_BLOCK, "e_gemm": 1, "e_exchange": 1,
+               "e_green_rows": 1, "energy": 1}
+    flops *= chunked.get(dname, dcalls / steps)
+    ms_block = dms / steps
+    common = {"kernel": dname, "traffic": None, "avg_launch_ms": round(dms / dcalls, 4),
+              "launches_per_step": round(dcalls / steps, 2),
+              "share_of_step": round(dms / sum(v[1] for v in leaf.values()), 4)}
     peaks = load_peaks() or {}
+    if pipe == "hbm":
+        achieved = flops / (ms_block / 1000.0) / 1e9
+        peak = peaks.get("hbm_gbs")
+        src = "MEASURED_PEAKS.json hbm_gbs" if peak else None
+        if not peak:
+            peak, src = 6800.0, "fallback (no MEASURED_PEAKS.json)"
+        return {**common, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": src}
+    achieved = flops / (ms_block / 1000.0) / 1e12
     if pipe == "tensor":
         peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
         src = "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)" if peak else None
@@ -152,10 +176,8 @@ def roofline_for(phases, work, lib, steps):
             peak, src = 1700.0, "fallback (no MEASURED_PEAKS.json)"
     else:
         peak, src = fma_peak(lib, pipe == "fp64")
-    return {"kernel": dname, "bound": pipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
-            "frac": round(achieved / peak, 4) if peak else None, "traffic": None, "peak_source": src,
-            "avg_launch_ms": round(avg_ms, 4), "launches_per_step": round(dcalls / steps, 2),
-            "share_of_step": round(dms / sum(v[1] for v in phases.values()), 4)}
+    return {**common, "bound": pipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4) if peak else None, "peak_source": src}
 
 
 # ------------------------------------------------------------ our engine ---
@@ -246,11 +268,11 @@ def run_ours(args, rank, world):
     # dominant kernel and its roofline
     work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=args.precision)
     roof = roofline_for(phases, work, lib, args.steps)
-    tc = {k: roofline_for({k: v}, work, lib, args.steps) for k, v in phases.items()
-          if k in work and work[k][1] == "tensor"}
+    tc = {k: roofline_for(phases, work, lib, args.steps, name=k) for k in phases
+          if k in work and work[k][1] in ("tensor", "hbm")}
 
     compare = None
-    if args.precision == "mixed" and not args.no_fp64:
+    if args.precision in SPLIT_SECTIONS and not args.no_fp64:
         compare = compare_with_fp64(env, st, W)
 
     e2e = None
@@ -259,7 +281,8 @@ def run_ours(args, rank, world):
 
     out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3/f32+f64",
+           "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else
+           ("bf16x3" if args.precision == "mixed" else "bf16x2") + "/f32+f64",
            "data": "synthetic (seeded Cholesky Hamiltonian, see ad_afqmc_prototype_gb300/synth.py)",
            "config": {"workload": args.workload, "norb": n, "nocc": o, "nchol": G, "n_walkers_per_gpu": W,
                       "precision": args.precision, "parallelism": f"replicas{world}",

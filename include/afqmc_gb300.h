@@ -44,6 +44,7 @@ extern "C" {
 
 #define AFQ_PREC_FP64 0  /* every product in binary64 */
 #define AFQ_PREC_MIXED 1 /* tensor-core / FP32 products, FP64 overlaps, QR, weights */
+#define AFQ_PREC_MIXED_FAST 2 /* as MIXED with two-piece bf16 operands (~2^-17 products): half the GEMM work */
 
 /* Sizes of one batch.  trial_is_real selects the real-trial fast path:
  * mo_coeff is still passed as complex128 but its imaginary parts must be 0,

@@ -1,7 +1,8 @@
-"""The mixed-precision form against the binary64 form, through the same API,
-from identical states and fields.  Tolerances: one step moves walkers by
-<= 1e-4 relative (bf16 hi/lo split products, ~2^-16); block energies agree
-to 1e-4 Ha (0.1 mHa, the accuracy target of the mixed form) and the
+"""The mixed-precision forms against the binary64 form, through the same API,
+from identical states and fields, for both split widths ("mixed": six bf16
+sections, products to ~2^-24; "mixed_fast": three sections, ~2^-17).
+Tolerances: one step moves walkers by <= 1e-4 relative; block energies
+agree to 1e-4 Ha (0.1 mHa, the accuracy target of the mixed form) and the
 energy kernel alone (a block of zero steps) to 1e-4 Ha as well."""
 import numpy as np
 import pytest
@@ -42,11 +43,15 @@ def _dstate(st):
     return device_state(st, inplace=False)
 
 
+PRECISIONS = ["mixed", "mixed_fast"]
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
 @pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 64), ("c1_n12_o6_g48_w256", 100)])
-def test_mixed_step_close_to_fp64(cuda, wl, W):
+def test_mixed_step_close_to_fp64(cuda, wl, W, prec):
     from ad_afqmc_prototype_gb300 import engine
     pa, pra, st = _setup(wl, W, "fp64")
-    pb, prb, _ = _setup(wl, W, "mixed")
+    pb, prb, _ = _setup(wl, W, prec)
     a, b = _dstate(st), _dstate(st)
     G = pa.nchol
     for k in range(3):
@@ -62,12 +67,13 @@ def test_mixed_step_close_to_fp64(cuda, wl, W):
     assert relo < 1e-3, relo
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
 @pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 128), ("c4_n200_o30_g1000_w4096", 256)])
-def test_mixed_energy_kernel_close_to_fp64(cuda, wl, W):
+def test_mixed_energy_kernel_close_to_fp64(cuda, wl, W, prec):
     """A block of zero steps is QR + energy + comb: isolates the energy GEMM."""
     from ad_afqmc_prototype_gb300 import engine
     pa, pra, st = _setup(wl, W, "fp64", n_prop_steps=3)
-    pb, prb, _ = _setup(wl, W, "mixed", n_prop_steps=3)
+    pb, prb, _ = _setup(wl, W, prec, n_prop_steps=3)
     a = _dstate(st)
     engine.block(pa, pra, a, 5, 0)  # move the walkers off the trial
     z0a = pra.__class__(**{**pra.__dict__, "n_prop_steps": 0})
@@ -80,13 +86,14 @@ def test_mixed_energy_kernel_close_to_fp64(cuda, wl, W):
     assert abs(float(ea) - float(eb)) < 1e-4, (float(ea), float(eb))
 
 
-def test_mixed_block_energy_error_per_block(cuda):
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_mixed_block_energy_error_per_block(cuda, prec):
     """From identical block-start states and fields: |E_mixed - E_fp64| per
     10-step block (QR after step 5) within 0.1 mHa."""
     from ad_afqmc_prototype_gb300 import engine
     W = 512
     pa, pra, st = _setup("c4_n200_o30_g1000_w4096", W, "fp64", n_prop_steps=10, qr_every=5)
-    pb, prb, _ = _setup("c4_n200_o30_g1000_w4096", W, "mixed", n_prop_steps=10, qr_every=5)
+    pb, prb, _ = _setup("c4_n200_o30_g1000_w4096", W, prec, n_prop_steps=10, qr_every=5)
     ref = _dstate(st)
     errs = []
     for blk in range(3):
