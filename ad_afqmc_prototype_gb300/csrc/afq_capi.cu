@@ -112,6 +112,7 @@ struct StepWS {
     __nv_bfloat16* Av;  // 2W x Kt_V
     float* Vm;          // 2Wc x ldv
     float* emi;         // n*n
+    float2* tsum;       // Wc*n*o: fp32 sum of the Taylor terms of a chunk
 };
 
 static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
@@ -130,6 +131,7 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         s.Av = a.take<__nv_bfloat16>(2 * W * L.Kt_V);
         s.Vm = a.take<float>(2 * Wc * L.ldv);
         s.emi = a.take<float>(n * n);
+        s.tsum = a.take<float2>(Wc * n * o);
     } else {
         s.green = a.take<double2>(W * o * n);
         s.fb = a.take<double2>(W * G);
@@ -277,7 +279,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
                                     ws.Vm, L.ldv, ws.status, s)); }
         { AFQ_PHASE("trotter", s);
           AFQ_TRY(launch_trotter_mixed(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.emi, ws.Vm, L.ldv,
-                                       walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, s)); }
+                                       walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.tsum, s)); }
     }
     // overlaps, and the next step's force-bias operand from the same factorisation
     { AFQ_PHASE("overlap", s);
@@ -289,12 +291,16 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
 }
 
 // Local energies of all walkers into ws.energy (meas/rhf.py:36-50).
-static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS& ws, cudaStream_t s) {
+// green_ready: ws.green already holds the Green's function of the walkers.
+static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS& ws, cudaStream_t s,
+                       bool green_ready = false) {
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
-    { AFQ_PHASE("green", s);
-      AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
-                           nullptr, ws.green, s)); }
+    if (!green_ready) {
+        AFQ_PHASE("green", s);
+        AFQ_TRY(launch_green(W, n, o, (const double2*)pb->mo_coeff, d->trial_is_real, (const double2*)st->walkers,
+                             nullptr, ws.green, s));
+    }
     AFQ_PHASE("energy", s);
     if (!is_mixed(d->precision))
         return launch_energy(W, n, o, G, pb->h0, ws.green, pb->rot_chol, d->trial_is_real,
@@ -370,17 +376,24 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
 
 // QR and overlap refresh (prop/blocks.py:53-57); in the mixed form the same
 // kernel also writes the next step's force-bias operand into ws->Ag.
+// QR of the walkers, then their overlaps from the same pass that writes
+// either the next step's force-bias operand (mixed, ws given) or, with
+// green_out, the Green's function the block's energy needs.
 static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s,
-                                  const StepWS* ws = nullptr) {
+                                  const StepWS* ws = nullptr, double2* green_out = nullptr) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
-    { AFQ_PHASE("qr", s); AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s)); }
-    AFQ_PHASE("overlap", s);
+    {
+        AFQ_PHASE("qr", s);
+        if (is_mixed(d->precision)) AFQ_TRY(launch_cholqr2(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+        else AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+    }
+    AFQ_PHASE(green_out ? "green" : "overlap", s);
     if (ws && is_mixed(d->precision))
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
                                     (double2*)st->overlaps, fb_split(d, *ws), s);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
-                        (double2*)st->overlaps, nullptr, s);
+                        (double2*)st->overlaps, green_out, s);
 }
 
 }  // namespace afq
@@ -601,6 +614,9 @@ int afq_apply_trotter(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_
 int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_out, double* det_r, void* stream) {
     AFQ_TRY(check_dims(d, false));
     AFQ_NOTNULL(walkers); AFQ_NOTNULL(walkers_out);
+    if (is_mixed(d->precision))
+        return launch_cholqr2(d->n_walkers, d->norb, d->nocc, (const double2*)walkers, (double2*)walkers_out,
+                              (double2*)det_r, as_stream(stream));
     return launch_qr(d->n_walkers, d->norb, d->nocc, (const double2*)walkers, (double2*)walkers_out,
                      (double2*)det_r, as_stream(stream));
 }
@@ -741,10 +757,10 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
         if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps)
             AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));
     }
-    // prop/blocks.py:53-57
-    AFQ_TRY(orthonormalize_refresh(pb, st, s));
+    // prop/blocks.py:53-57, with the energy's Green's function from the same pass
+    AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green));
     // prop/blocks.py:59-79
-    AFQ_TRY(energy_impl(pb, st, ws, s));
+    AFQ_TRY(energy_impl(pb, st, ws, s, true));
     { AFQ_PHASE("block_measure", s);
     AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
                                  st->pop_control_ene_shift, block_energy, block_weight, s)); }

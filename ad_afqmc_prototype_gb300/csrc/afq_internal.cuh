@@ -234,9 +234,10 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
                              const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
                              double2* fb_term, cudaStream_t s);
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
-                         long long ldv, const double2* win, double2* wout, cudaStream_t s);
+                         long long ldv, const double2* win, double2* wout, float2* tsum, cudaStream_t s);
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
                          SplitOut split, cudaStream_t s);
+int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
 int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,

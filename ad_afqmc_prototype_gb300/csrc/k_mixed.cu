@@ -117,11 +117,12 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
 // stage, so the next columns are in flight while the current ones are
 // multiplied.  Thread (rg, cg) owns rows rg + RG q (q < NR) and the complex
 // columns 2cg, 2cg+1, 16+2cg, 16+2cg+1 (so a warp's T reads are contiguous
-// 128-byte rows).  The running sum lives in the binary64 output walker, which
-// each thread updates only at its own entries (walkers_out may alias
-// walkers_in):
-//   W1 = W + (E-I) W;  out = W1 + sum_k (i sqrt_dt V)^k / k! W1;
-//   W' = out + (E-I) out.
+// 128-byte rows).  Each thread touches only its own entries of the output
+// walker (walkers_out may alias walkers_in) and of the fp32 scratch Ts that
+// sums the series terms, so the binary64 pipe sees three additions per
+// entry, not one per term:
+//   W1 = W + (E-I) W;  Ts = sum_k (i sqrt_dt V)^k / k! W1 (fp32);
+//   out = W1 + Ts;  W' = out + (E-I) out.
 constexpr int TR_CG = 8, TR_OC = 32, TR_BJ = 8;
 // Row stride (floats) of a staged operand plane: 16-byte rows for cp.async,
 // and rows 0..3 of a warp start in different banks.
@@ -201,21 +202,18 @@ __device__ __forceinline__ void tr_matmul(int n, const float* __restrict__ re, c
                 const float4 ta = tb[(jj + h) * (TR_OC / 2) + cg], tc = tb[(jj + h) * (TR_OC / 2) + TR_CG + cg];
                 const float2 t[4] = {make_float2(ta.x, ta.y), make_float2(ta.z, ta.w), make_float2(tc.x, tc.y),
                                      make_float2(tc.z, tc.w)};
+                float2 tn[4];  // i t
 #pragma unroll
-                for (int q = 0; q < NR; ++q) {
+                for (int j = 0; j < 4; ++j) tn[j] = make_float2(-t[j].y, t[j].x);
+#pragma unroll
+                for (int q = 0; q < NR; ++q) {  // acc += a t + b (i t), two lanes per instruction
                     const float a = h ? mr[q].y : mr[q].x;
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        acc[q][j].x = fmaf(a, t[j].x, acc[q][j].x);
-                        acc[q][j].y = fmaf(a, t[j].y, acc[q][j].y);
-                    }
+                    for (int j = 0; j < 4; ++j) acc[q][j] = __ffma2_rn(make_float2(a, a), t[j], acc[q][j]);
                     if (CPLX) {
                         const float bq = h ? mi[q].y : mi[q].x;
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            acc[q][j].x = fmaf(-bq, t[j].y, acc[q][j].x);
-                            acc[q][j].y = fmaf(bq, t[j].x, acc[q][j].y);
-                        }
+                        for (int j = 0; j < 4; ++j) acc[q][j] = __ffma2_rn(make_float2(bq, bq), tn[j], acc[q][j]);
                     }
                 }
             }
@@ -230,7 +228,7 @@ template <int NR>
 __global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms, float sqrt_dt,
                                                           const float* __restrict__ emi, const float* __restrict__ vm,
                                                           long long ldv, int wc, const double2* win, double2* wout,
-                                                          int v16) {
+                                                          float2* __restrict__ tsum, int v16) {
     extern __shared__ float4 smf4[];
     const int RG = blockDim.x / TR_CG, rows = RG * NR;
     const int nT = (n + TR_BJ - 1) / TR_BJ * TR_BJ;
@@ -243,6 +241,7 @@ __global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms
     double2* Wo = wout + (size_t)w * n * o;
     const float* Vr = vm + (long long)w * ldv;
     const float* Vi = vm + (long long)(wc + w) * ldv;
+    float2* Ts = tsum + (size_t)w * n * o;
 
     for (int e = threadIdx.x; e < 4 * rows * TR_VS; e += blockDim.x) stg[e] = 0.f;
     for (int e = threadIdx.x; e < nT * TR_OC; e += blockDim.x) {
@@ -290,16 +289,19 @@ __global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms
                 const float2 t = make_float2(-sk * acc[q][j].y, sk * acc[q][j].x);
                 if (i < n) T[i * TR_OC + cl] = (c < o) ? t : make_float2(0.f, 0.f);
                 if (i < n && c < o) {
-                    double2 v = Wo[(size_t)i * o + c];
-                    v.x += (double)t.x;
-                    v.y += (double)t.y;
-                    Wo[(size_t)i * o + c] = v;
+                    float2* ts = Ts + (size_t)i * o + c;
+                    if (k == 1) {
+                        *ts = t;
+                    } else {
+                        const float2 u = *ts;
+                        *ts = make_float2(u.x + t.x, u.y + t.y);
+                    }
                 }
             }
         }
         __syncthreads();
     }
-    // W' = out + (E - I) out
+    // out = W1 + Ts;  W' = out + (E - I) out
     rgl = rg;
     asm volatile("" : "+r"(rgl));
 #pragma unroll
@@ -309,7 +311,13 @@ __global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms
         for (int j = 0; j < 4; ++j) {
             const int cl = tr_col(cg, j), c = c0 + cl;
             if (i < n && c < o) {
-                const double2 v = Wo[(size_t)i * o + c];
+                double2 v = Wo[(size_t)i * o + c];
+                if (n_terms > 0) {
+                    const float2 u = Ts[(size_t)i * o + c];
+                    v.x += (double)u.x;
+                    v.y += (double)u.y;
+                    Wo[(size_t)i * o + c] = v;
+                }
                 T[i * TR_OC + cl] = make_float2((float)v.x, (float)v.y);
             }
         }
@@ -343,7 +351,7 @@ static int smem_attr(K kernel, size_t bytes) {
 }
 
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
-                         long long ldv, const double2* win, double2* wout, cudaStream_t s) {
+                         long long ldv, const double2* win, double2* wout, float2* tsum, cudaStream_t s) {
     if (wc <= 0) return AFQ_OK;
     if (wc > 65535) return fail(AFQ_E_UNSUPPORTED, "mixed trotter: chunk of %d walkers > 65535", wc);
     // 256 threads (32 row groups) up to 7 rows each, else 512 threads
@@ -358,7 +366,7 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
     case NRV:                                                                                            \
         AFQ_TRY(smem_attr(k_trotter_mixed<NRV>, smem));                                                  \
         k_trotter_mixed<NRV><<<grid, threads, smem, s>>>(n, o, n_terms, (float)sqrt_dt, emi, vm, ldv, wc, win, \
-                                                         wout, v16);                                     \
+                                                         wout, tsum, v16);                               \
         break;
     switch (nr) {
         AFQ_TM(1) AFQ_TM(2) AFQ_TM(3) AFQ_TM(4) AFQ_TM(5) AFQ_TM(6) AFQ_TM(7) AFQ_TM(8)
@@ -599,6 +607,199 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
     return AFQ_OK;
 }
 
+// ---------------------------------------------------- orthonormalisation --
+// Mixed-form QR with the reference's output (walkers.py:169-211: the unique
+// Q with diag(R) real and > 0), by CholeskyQR2 in shared memory, one CTA per
+// walker:
+//   pass 1: G1 = W^H W with fp32 products, R1 = chol(G1) in binary64,
+//           X = W R1^-1 by binary64 forward substitution;
+//   pass 2: G2 = X^H X, R2 = chol(G2), Q = X R2^-1, all binary64.
+// X spans W's columns to binary64 accuracy whatever the error of R1 (R1 only
+// preconditions), and pass 2 restores orthonormality; Q = W (R2 R1)^-1 with
+// R2 R1 upper triangular with a positive real diagonal, the Householder
+// form's Q.  If a pivot of the fp32 Gram matrix falls below 1e-5 of its
+// column's squared norm (cond(W) beyond ~300, where fp32 rounding would
+// leave X far from orthonormal), pass 1 is redone with binary64 products.  A
+// numerically rank-deficient W (a non-positive binary64 pivot) gets the
+// pivot 1 and a zero row of R there, so the output stays finite; such a
+// walker has a vanishing overlap and no weight.
+// Upper-triangle entry e (row-major) -> (j, k), j <= k.
+__device__ __forceinline__ void cq_entry(int o, int e, int& j, int& k) {
+    j = 0;
+    while (e >= o - j) { e -= o - j; ++j; }
+    k = j + e;
+}
+
+constexpr int CQ_RB = 32;   // rows per fp32 conversion block
+constexpr int CQ_RS = CQ_RB + 1;  // odd stride (in float2): a warp's columns fall in distinct banks
+constexpr int CQ_EPT = 9;   // upper-triangle entries per thread (o <= 64: 2080 <= 256 x 9)
+
+// fp32 Gram matrix: rows of A are converted to fp32 once per block of CQ_RB
+// rows (buf: o columns of CQ_RS float2), so the binary64 pipe only converts.
+__device__ __forceinline__ void cq_gram_f32(int n, int o, int ld, const double2* A, double2* Gm, float2* buf) {
+    const int P = o * (o + 1) / 2;
+    float2 acc[CQ_EPT];
+    int jj[CQ_EPT], kk[CQ_EPT];
+#pragma unroll
+    for (int t = 0; t < CQ_EPT; ++t) {
+        acc[t] = make_float2(0.f, 0.f);
+        const int e = threadIdx.x + t * blockDim.x;
+        if (e < P) cq_entry(o, e, jj[t], kk[t]);
+        else jj[t] = kk[t] = -1;
+    }
+    for (int r0 = 0; r0 < n; r0 += CQ_RB) {
+        const int rn = min(CQ_RB, n - r0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < rn * o; e += blockDim.x) {
+            const int j = e / rn, r = e % rn;
+            const double2 v = A[(size_t)j * ld + r0 + r];
+            buf[j * CQ_RS + r] = make_float2((float)v.x, (float)v.y);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < CQ_EPT; ++t) {
+            if (jj[t] < 0) continue;
+            const float2* a = buf + jj[t] * CQ_RS;
+            const float2* b = buf + kk[t] * CQ_RS;
+            float sr = acc[t].x, si = acc[t].y;
+            for (int r = 0; r < rn; ++r) {
+                const float2 x = a[r], y = b[r];
+                sr = fmaf(x.x, y.x, fmaf(x.y, y.y, sr));
+                si = fmaf(x.x, y.y, fmaf(-x.y, y.x, si));
+            }
+            acc[t] = make_float2(sr, si);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < CQ_EPT; ++t)
+        if (jj[t] >= 0) Gm[jj[t] * o + kk[t]] = make_double2(acc[t].x, acc[t].y);
+}
+
+__device__ __forceinline__ void cq_gram(int n, int o, int ld, const double2* A, double2* Gm) {
+    const int P = o * (o + 1) / 2;
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        int j, k;
+        cq_entry(o, e, j, k);
+        const double2* a = A + (size_t)j * ld;
+        const double2* b = A + (size_t)k * ld;
+        {  // four independent chains
+            double sr0 = 0.0, si0 = 0.0, sr1 = 0.0, si1 = 0.0;
+            int i = 0;
+            for (; i + 1 < n; i += 2) {
+                const double2 x0 = a[i], y0 = b[i], x1 = a[i + 1], y1 = b[i + 1];
+                sr0 = fma(x0.x, y0.x, fma(x0.y, y0.y, sr0));
+                si0 = fma(x0.x, y0.y, fma(-x0.y, y0.x, si0));
+                sr1 = fma(x1.x, y1.x, fma(x1.y, y1.y, sr1));
+                si1 = fma(x1.x, y1.y, fma(-x1.y, y1.x, si1));
+            }
+            if (i < n) {
+                const double2 x0 = a[i], y0 = b[i];
+                sr0 = fma(x0.x, y0.x, fma(x0.y, y0.y, sr0));
+                si0 = fma(x0.x, y0.y, fma(-x0.y, y0.x, si0));
+            }
+            Gm[j * o + k] = make_double2(sr0 + sr1, si0 + si1);
+        }
+    }
+}
+
+// In-place upper Cholesky G = R^H R of the upper triangle of Gm (row-major,
+// R[k][j] at Gm[k o + j]); thread 0 multiplies the pivots into *det.
+// Returns (uniformly) whether a pivot was not above rel_tol times the
+// column's diagonal entry before elimination (d0, o entries of scratch); such
+// a pivot becomes 1 with a zero row.
+__device__ __forceinline__ bool cq_chol(int o, double2* Gm, double* det, double rel_tol, double* d0) {
+    for (int k = threadIdx.x; k < o; k += blockDim.x) d0[k] = Gm[k * o + k].x;
+    __syncthreads();
+    bool bad = false;
+    for (int k = 0; k < o; ++k) {
+        const double gkk = Gm[k * o + k].x;
+        const bool b = !(gkk > rel_tol * d0[k]) || !(gkk > 0.0);
+        bad |= b;
+        const double rkk = b ? 1.0 : sqrt(gkk), ir = 1.0 / rkk;
+        if (threadIdx.x == 0) *det *= rkk;
+        __syncthreads();
+        for (int j = k + threadIdx.x; j < o; j += blockDim.x) {
+            const double2 g = Gm[k * o + j];
+            Gm[k * o + j] = j == k ? make_double2(rkk, 0.0) : (b ? make_double2(0.0, 0.0) : cscale(g, ir));
+        }
+        __syncthreads();
+        const int m = o - k - 1;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            const int i = k + 1 + e / m, j = k + 1 + e % m;
+            if (i <= j) Gm[i * o + j] = csub(Gm[i * o + j], cmulc(Gm[k * o + i], Gm[k * o + j]));
+        }
+        __syncthreads();
+    }
+    return bad;
+}
+
+// A <- A R^-1 in place, one thread per row of A (column-major, leading dim ld).
+__device__ __forceinline__ void cq_solve(int n, int o, int ld, double2* A, const double2* R) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int k = 0; k < o; ++k) {  // two independent chains over j
+            double2 a0 = A[(size_t)k * ld + i], a1 = make_double2(0.0, 0.0);
+            int j = 0;
+            for (; j + 1 < k; j += 2) {  // a -= x r, four fused multiply-adds
+                const double2 x0 = A[(size_t)j * ld + i], r0 = R[j * o + k];
+                const double2 x1 = A[(size_t)(j + 1) * ld + i], r1 = R[(j + 1) * o + k];
+                a0.x = fma(-x0.x, r0.x, fma(x0.y, r0.y, a0.x));
+                a0.y = fma(-x0.x, r0.y, fma(-x0.y, r0.x, a0.y));
+                a1.x = fma(-x1.x, r1.x, fma(x1.y, r1.y, a1.x));
+                a1.y = fma(-x1.x, r1.y, fma(-x1.y, r1.x, a1.y));
+            }
+            if (j < k) {
+                const double2 x0 = A[(size_t)j * ld + i], r0 = R[j * o + k];
+                a0.x = fma(-x0.x, r0.x, fma(x0.y, r0.y, a0.x));
+                a0.y = fma(-x0.x, r0.y, fma(-x0.y, r0.x, a0.y));
+            }
+            A[(size_t)k * ld + i] = cscale(cadd(a0, a1), 1.0 / R[k * o + k].x);
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_cholqr2(int n, int o, const double2* __restrict__ win,
+                                                 double2* __restrict__ wout, double2* __restrict__ det_out) {
+    extern __shared__ double2 csm[];
+    __shared__ double s_det;  // prod diag(R1) prod diag(R2) = prod diag(R)
+    __shared__ double s_d0[64];
+    const int ld = n | 1;
+    double2* A = csm;                     // ld x o, A[j ld + i] = W[i, j]
+    double2* Gm = csm + (size_t)ld * o;  // o x o
+    float2* buf = (float2*)(Gm + o * o);  // CQ_RB x o
+    const int w = blockIdx.x;
+    const double2* Wp = win + (size_t)w * n * o;
+    for (int e = threadIdx.x; e < n * o; e += blockDim.x) A[(size_t)(e % o) * ld + e / o] = Wp[e];
+    if (threadIdx.x == 0) s_det = 1.0;
+    __syncthreads();
+    cq_gram_f32(n, o, ld, A, Gm, buf);
+    __syncthreads();
+    if (cq_chol(o, Gm, &s_det, 1e-5, s_d0)) {  // fp32 cannot resolve W's conditioning: binary64 products
+        if (threadIdx.x == 0) s_det = 1.0;
+        cq_gram(n, o, ld, A, Gm);
+        __syncthreads();
+        cq_chol(o, Gm, &s_det, 0.0, s_d0);
+    }
+    cq_solve(n, o, ld, A, Gm);
+    cq_gram(n, o, ld, A, Gm);
+    __syncthreads();
+    cq_chol(o, Gm, &s_det, 0.0, s_d0);
+    cq_solve(n, o, ld, A, Gm);
+    double2* Wo = wout + (size_t)w * n * o;
+    for (int e = threadIdx.x; e < n * o; e += blockDim.x) Wo[e] = A[(size_t)(e % o) * ld + e / o];
+    if (det_out && threadIdx.x == 0) det_out[w] = make_double2(s_det, 0.0);
+}
+
+int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    if (o > 64) return fail(AFQ_E_UNSUPPORTED, "qr: nocc=%d > 64", o);
+    const size_t smem = ((size_t)(n | 1) * o + (size_t)o * o) * sizeof(double2) + (size_t)CQ_RS * o * sizeof(float2);
+    AFQ_TRY(smem_attr(k_cholqr2, smem));
+    k_cholqr2<<<W, 256, smem, s>>>(n, o, win, wout, det_r);
+    AFQ_LAUNCHED("k_cholqr2");
+    return AFQ_OK;
+}
+
 // ------------------------------------------------------------------ energy
 // Mixed energy (meas/rhf.py:36-50) for a chunk of walkers: the tensor-core
 // GEMM produced F[(w, part, k), (g, i)] = sum_j G_part[w, k, j] L~[g, i, j]
@@ -607,8 +808,8 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
 // Cholesky vectors, sum_g c_g^2 and sum_g sum_ik f_g[i,k] f_g[k,i].
 // The chunk's rows are copied into shared memory as they lie in F (plane
 // part, row k, column g o + i = f_g[i,k]) by cp.async, all copies in flight
-// at once.  The fp32 products of one f_g are summed per thread in fp32 (a
-// few terms) and those sums accumulate in fp64.
+// at once.  The fp32 products are summed in fp32 per thread (EX_G o^2 / 256
+// terms, ~28) and per warp; the warp sums accumulate in fp64.
 constexpr int EX_G = 8;  // Cholesky vectors per CTA
 __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const float* __restrict__ F, long long ldf,
                                                          double2* __restrict__ partial, int nchunk, int v16) {
@@ -644,11 +845,11 @@ __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const flo
     }
     cp_async_wait_all();
     __syncthreads();
-    double xr = 0.0, xi = 0.0, cr = 0.0, ci = 0.0;
+    double cr = 0.0, ci = 0.0;
+    float sr = 0.f, si = 0.f;
     for (int g = 0; g < ng; ++g) {
         const float* fr = Pr + g * o;
         const float* fi = Pi + g * o;
-        float sr = 0.f, si = 0.f;
 #pragma unroll
         for (int j = 0; j < EX_R; ++j) {
             if (oa[j] >= 0) {
@@ -657,9 +858,13 @@ __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const flo
                 si = fmaf(ar, bi, fmaf(ai, br, si));
             }
         }
-        xr += (double)sr;
-        xi += (double)si;
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, off);
+        si += __shfl_xor_sync(0xffffffffu, si, off);
+    }
+    const double xr = (double)sr, xi = (double)si;
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
         double tr = 0.0, ti = 0.0;
         for (int i = 0; i < o; ++i) {
@@ -670,7 +875,7 @@ __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const flo
         ci += 2.0 * tr * ti;
     }
     __shared__ double red[4][8];
-    cr = warp_sum(cr); ci = warp_sum(ci); xr = warp_sum(xr); xi = warp_sum(xi);
+    if (threadIdx.x < 32) { cr = warp_sum(cr); ci = warp_sum(ci); }  // the c_g sums live in warp 0 (ng <= 32)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) { red[0][wid] = cr; red[1][wid] = ci; red[2][wid] = xr; red[3][wid] = xi; }
     __syncthreads();

@@ -195,8 +195,9 @@ def apply_trotter(walkers, shifted_fields, chol, exp_h1_half, sqrt_dt: float, n_
     return out
 
 
-def orthogonalize(walkers, out: Optional[torch.Tensor] = None):
-    """Returns (Q, det_r) with diag(R) >= 0 (walkers.py:169-203)."""
+def orthogonalize(walkers, out: Optional[torch.Tensor] = None, precision: int = _lib.AFQ_PREC_FP64):
+    """Returns (Q, det_r) with diag(R) >= 0 (walkers.py:169-203); Householder
+    for the FP64 precision, CholeskyQR2 for the mixed ones."""
     w = as_device(walkers, C128)
     if w.dim() != 3:
         raise ValueError("walkers must be (n_walkers, norb, nocc)")
@@ -204,7 +205,7 @@ def orthogonalize(walkers, out: Optional[torch.Tensor] = None):
     if out is None:
         out = torch.empty_like(w)
     det = torch.empty((W,), dtype=C128, device=w.device)
-    d = make_dims(W, n, o, 1, True)
+    d = make_dims(W, n, o, 1, True, precision)
     _lib.call("afq_orthogonalize", ctypes.byref(d), ptr(w), ptr(out), ptr(det), stream_ptr())
     return out, det
 

@@ -181,10 +181,12 @@ int afq_apply_trotter(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_
                       const double* shifted_fields, double* walkers_out, void* workspace,
                       size_t workspace_bytes, void* stream);
 
-/* orthogonalize / orthonormalize (restricted): Householder QR with diag(R)
- * real >= 0 (walkers.py:169-211).  det_r (optional) receives prod diag(R)
- * (W,) c128; the restricted normalisation is det_r^2.  walkers_out may equal
- * walkers. */
+/* orthogonalize / orthonormalize (restricted): QR with diag(R) real >= 0
+ * (walkers.py:169-211).  det_r (optional) receives prod diag(R) (W,) c128;
+ * the restricted normalisation is det_r^2.  walkers_out may equal walkers.
+ * d->precision FP64: Householder (as the reference's LAPACK QR); MIXED and
+ * MIXED_FAST: CholeskyQR2, fp32 first Gram matrix, otherwise binary64 (the
+ * same Q and R to ~cond(W) * 1e-16; the mixed block uses it). */
 int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_out,
                       double* det_r, void* stream);
 

@@ -103,6 +103,27 @@ def test_qr_matches_oracle(E, n, o, W):
     np.testing.assert_allclose(cpu(det), dr, rtol=1e-11)
 
 
+@pytest.mark.parametrize("n,o,W,cond", [(12, 6, 5, 0), (200, 30, 3, 0), (64, 64, 2, 0), (9, 1, 4, 0),
+                                        (120, 20, 3, 1e4)])
+def test_cholqr2_matches_oracle(E, n, o, W, cond):
+    """The mixed forms' CholeskyQR2 gives the Householder form's unique Q and
+    det(R); cond > 0 mixes the columns through singular values spanning
+    `cond`, past what the fp32 first Gram matrix resolves (the binary64
+    retry)."""
+    from ad_afqmc_prototype_gb300 import _lib
+    rng = np.random.default_rng(o + 7)
+    w = rng.normal(size=(W, n, o)) + 1j * rng.normal(size=(W, n, o))
+    if cond:
+        u, _ = np.linalg.qr(rng.normal(size=(o, o)))
+        v, _ = np.linalg.qr(rng.normal(size=(o, o)))
+        w = w @ (u * np.logspace(0, -np.log10(cond), o)[None, :] @ v)
+    for prec in (_lib.AFQ_PREC_MIXED, _lib.AFQ_PREC_MIXED_FAST):
+        q, det = E.orthogonalize(dev(w, E.C128), precision=prec)
+        qr, dr = O.qr_phase(w)
+        np.testing.assert_allclose(cpu(q), qr, rtol=0, atol=1e-10)
+        np.testing.assert_allclose(cpu(det), dr, rtol=1e-10)
+
+
 @pytest.mark.parametrize("W", [1, 2, 3, 31, 32, 33, 256, 1000, 4096, 5000])
 def test_comb_indices_bit_exact(E, W):
     rng = np.random.default_rng(W)
