@@ -113,6 +113,7 @@ struct StepWS {
     float* Vm;          // 2Wc x ldv
     float* emi;         // n*n
     float2* tsum;       // Wc*n*o: fp32 sum of the Taylor terms of a chunk
+    __nv_bfloat16* esplit;  // 2 n*n: E - I as bf16 hi, mid (tensor-core Taylor products)
 };
 
 static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
@@ -132,6 +133,7 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         s.Vm = a.take<float>(2 * Wc * L.ldv);
         s.emi = a.take<float>(n * n);
         s.tsum = a.take<float2>(Wc * n * o);
+        s.esplit = a.take<__nv_bfloat16>(2 * n * n);
     } else {
         s.green = a.take<double2>(W * o * n);
         s.fb = a.take<double2>(W * G);
@@ -271,6 +273,23 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     { AFQ_PHASE("field_shift", s);
       AFQ_TRY(launch_field_shift_mixed(W, G, Wc, pb->sqrt_dt, fields, ws.fbm, G, (const double2*)pb->mf_shifts, ws.Av,
                                        L.S_V, L.Kt_V, L.sec, ws.shift_term, ws.fb_term, s)); }
+    // three-section form: V-build writes V as bf16 hi/mid pieces and the
+    // Taylor products run on the tensor cores
+    const bool tc_taylor = d->precision == AFQ_PREC_MIXED_FAST && trotter_tc_supported(n, o) && L.ldv == (long long)n * n;
+    if (tc_taylor) {
+        AFQ_TRY(launch_e_minus_i_split(n, pb->exp_h1_half, ws.esplit, ws.esplit + (size_t)n * n, s));
+        for (int w0 = 0; w0 < W; w0 += Wc) {
+            const int wc = W - w0 < Wc ? W - w0 : Wc;
+            __nv_bfloat16* vh = (__nv_bfloat16*)ws.Vm;
+            __nv_bfloat16* vmid = vh + (size_t)2 * wc * L.ldv;
+            { AFQ_PHASE("vbuild_gemm", s);
+              AFQ_TRY(launch_tc_gemm_tn_drain_split(2 * wc, n * n, L.Kt_V, ws.Av + (size_t)2 * w0 * L.Kt_V, L.Kt_V,
+                                                    lb.Bv, L.Kt_V, vh, vmid, L.ldv, ws.status, s)); }
+            { AFQ_PHASE("trotter", s);
+              AFQ_TRY(launch_trotter_tc(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.esplit, ws.esplit + (size_t)n * n, vh,
+                                        vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.status, s)); }
+        }
+    } else {
     AFQ_TRY(launch_e_minus_i(n, pb->exp_h1_half, ws.emi, s));
     for (int w0 = 0; w0 < W; w0 += Wc) {
         const int wc = W - w0 < Wc ? W - w0 : Wc;
@@ -280,6 +299,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
         { AFQ_PHASE("trotter", s);
           AFQ_TRY(launch_trotter_mixed(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.emi, ws.Vm, L.ldv,
                                        walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.tsum, s)); }
+    }
     }
     // overlaps, and the next step's force-bias operand from the same factorisation
     { AFQ_PHASE("overlap", s);

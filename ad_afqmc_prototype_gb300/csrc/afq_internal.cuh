@@ -218,6 +218,10 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
 // (round-to-nearest) instead of in the tensor cores' truncating accumulator.
 int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                             long long ldc, int* err, cudaStream_t s, int kd = 1);
+// Same product, written as the two-piece bf16 split (hi, mid) of each sum.
+int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb,
+                                  __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int* err, cudaStream_t s,
+                                  int kd = 1);
 
 // k_walker.cu : Green's function with an optional split (bf16) output
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
@@ -238,6 +242,12 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
                          SplitOut split, cudaStream_t s);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
+// k_trotter_tc.cu
+bool trotter_tc_supported(int n, int o);
+int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
+                      const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
+                      double2* wout, int* err, cudaStream_t s);
+int launch_e_minus_i_split(int n, const double* E, __nv_bfloat16* eh, __nv_bfloat16* em, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
 int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,

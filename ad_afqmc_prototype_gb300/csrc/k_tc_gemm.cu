@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 
 #include "afq_internal.cuh"
+#include "tc_common.cuh"
 
 namespace afq {
 namespace tc {
@@ -32,7 +33,6 @@ constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int ACC_COLS = BN;
 constexpr int TMEM_COLS = 2 * ACC_COLS;
 constexpr int THREADS = 192;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-5: epilogue
-constexpr unsigned long long WAIT_NS = 1000000000ull;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 
 // instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16 (7-9 = 1),
@@ -40,104 +40,9 @@ constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long now_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the phase with `parity`; false on timeout or abort.
-__device__ __forceinline__ bool mbar_wait_inl(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (;;) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (abort_flag && *abort_flag) return false;
-        if (now_ns() - t0 > WAIT_NS) return false;
-    }
-}
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (;;) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (abort_flag && *abort_flag) return false;
-        if (now_ns() - t0 > WAIT_NS) return false;
-    }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            dst),
-        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// K-major operand tile with 128-byte swizzle: 128-byte rows, 8-row atoms
-// 1024 bytes apart (stride byte offset), descriptor version 1 (bit 46),
-// swizzle mode 2 (bits 61-63).  The leading byte offset is unused for this
-// layout.  Advancing K by 16 bf16 (32 bytes) inside the 128-byte row moves the
-// start address; the tile base is 1024-byte aligned so the swizzle phase is 0.
-__device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
-    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(1024 >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-
 __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
-        : "memory");
+    umma_bf16_i(d_tmem, adesc, bdesc, IDESC, accumulate);
 }
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 __global__ void __launch_bounds__(THREADS, 1)
     k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, float* __restrict__ C,
               int M, int N, int K, long long ldc, int* __restrict__ err) {
@@ -302,18 +207,14 @@ __global__ void __launch_bounds__(THREADS, 1)
 // warps 2-5 and 6-9 each cover all 128 rows, one column half each.
 constexpr int DTMEM_COLS = 512;
 
-// BNT = 128: 320 threads (warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9
-// epilogue), each epilogue thread sums 64 columns of one row.
-// BNT = 256: 384 threads; warpgroup 0 (warps 0-3: TMA, MMA, two idle) gives
-// registers back (setmaxnreg 40) to warpgroups 1-2 (warps 4-11, epilogue,
-// setmaxnreg 232), whose threads sum 128 columns of one row.  Launched at
-// 168 registers a thread: 128 x 40 + 256 x 232 = 384 x 168.
+// 320 threads (warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9 epilogue);
+// each epilogue thread sums BNT/2 = 64 columns of one row.
 template <int BNT>
 struct Drain {
-    static constexpr int THREADS = BNT == 128 ? 320 : 384;
-    static constexpr int EW0 = BNT == 128 ? 2 : 4;  // first epilogue warp
+    static constexpr int THREADS = 320;
+    static constexpr int EW0 = 2;  // first epilogue warp
     static constexpr int SLOTS = DTMEM_COLS / BNT;
-    static constexpr int STG = BNT == 128 ? 6 : 4;
+    static constexpr int STG = 6;
     static constexpr int B_BYTES = BNT * BK * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
     static constexpr int SMEM = STG * STAGE + 1024 + 256;
@@ -321,41 +222,15 @@ struct Drain {
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BNT >> 3) << 17) |
                                       ((uint32_t)(BM >> 4) << 24);
 };
-constexpr int DREG_LAUNCH = 168, DREG_PRODUCER = 40, DREG_EPILOGUE = 232;
-static_assert(128 * DREG_PRODUCER + 256 * DREG_EPILOGUE <= 384 * DREG_LAUNCH, "register split exceeds the launch");
+static_assert(Drain<128>::STG * Drain<128>::STAGE + 1024 + 256 <= 227 * 1024, "drained GEMM shared memory");
 
-__device__ __forceinline__ void umma_bf16_i(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                            uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-#define AFQ_R8(i)                                                                                              \
-    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
-        "=r"(r[i + 7])
-// 64 consecutive fp32 columns of this warp's 32 lanes; returns after the load completed.
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, "
-        "%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, "
-        "%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
-        : AFQ_R8(0), AFQ_R8(8), AFQ_R8(16), AFQ_R8(24), AFQ_R8(32), AFQ_R8(40), AFQ_R8(48), AFQ_R8(56)
-        : "r"(taddr)
-        : "memory");
-}
-#undef AFQ_R8
-
-template <int BNT>
+// SPLIT: instead of fp32 C, write the two-piece bf16 split of each sum to
+// Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.
+template <int BNT, bool SPLIT>
 __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    float* __restrict__ C, int M, int N, int K, long long ldc, int kd, int* __restrict__ err) {
+                    float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
+                    int N, int K, long long ldc, int kd, int* __restrict__ err) {
     using D = Drain<BNT>;
     constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
     extern __shared__ uint8_t smem_raw[];
@@ -462,7 +337,8 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
         const int q = warp & 3, cb = ((warp - D::EW0) >> 2) * CW;
         int slot = 0;
         uint32_t slot_phase = 0;
-        const bool vec = (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
+        const bool vec = SPLIT ? (ldc % 8) == 0 && ((((uintptr_t)Ch) | ((uintptr_t)Cm)) & 15) == 0
+                               : (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
         for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
             const int mb = t % mt, nb = t / mt;
@@ -509,7 +385,36 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
             if (!ok) break;
             const int row = mb * BM + q * 32 + lane;
             const int col0 = nb * BNT + cb;
-            if (row < M) {
+            if (row < M && SPLIT) {
+                __nv_bfloat16* dh = Ch + (long long)row * ldc + col0;
+                __nv_bfloat16* dm = Cm + (long long)row * ldc + col0;
+                if (vec && col0 + CW <= N) {
+#pragma unroll
+                    for (int j = 0; j < CW / 2; j += 4) {
+                        uint32_t ph[4], pm[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const __nv_bfloat162 h = __floats2bfloat162_rn(acc[j + u].x, acc[j + u].y);
+                            const float2 hf = __bfloat1622float2(h);
+                            const __nv_bfloat162 m = __floats2bfloat162_rn(acc[j + u].x - hf.x, acc[j + u].y - hf.y);
+                            ph[u] = *(const uint32_t*)&h;
+                            pm[u] = *(const uint32_t*)&m;
+                        }
+                        *(uint4*)(dh + 2 * j) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+                        *(uint4*)(dm + 2 * j) = make_uint4(pm[0], pm[1], pm[2], pm[3]);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < CW; ++j) {
+                        if (col0 + j < N) {
+                            const float v = (j & 1) ? acc[j / 2].y : acc[j / 2].x;
+                            const __nv_bfloat16 h = __float2bfloat16(v);
+                            dh[j] = h;
+                            dm[j] = __float2bfloat16(v - __bfloat162float(h));
+                        }
+                    }
+                }
+            } else if (row < M) {
                 float* dst = C + (long long)row * ldc + col0;
                 if (vec && col0 + CW <= N) {
 #pragma unroll
@@ -532,35 +437,6 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DTMEM_COLS) : "memory");
     }
-}
-
-// ------------------------------------------------------------------- host --
-static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-
-static int get_encode() {
-    if (g_encode) return AFQ_OK;
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-        return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    return AFQ_OK;
-}
-
-// rows x cols bf16 matrix, row stride ld elements, box = box_rows x BK
-static int make_map(CUtensorMap* m, const void* base, long long rows, long long cols, long long ld, int box_rows) {
-    if (((uintptr_t)base) & 15) return fail(AFQ_E_INVALID_ARGUMENT, "tensor base not 16-byte aligned");
-    if ((ld * 2) % 16) return fail(AFQ_E_INVALID_ARGUMENT, "tensor row stride not a multiple of 16 bytes");
-    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    return AFQ_OK;
 }
 
 }  // namespace tc
@@ -589,31 +465,31 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     return AFQ_OK;
 }
 
-template <int BNT>
+template <int BNT, bool SPLIT>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
-                        long long ldc, int kd, int* err, cudaStream_t s) {
+                        __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s) {
     using namespace tc;
     static bool attr = false;
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
     AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT));
     if (!attr) {
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       Drain<BNT>::SMEM));
         attr = true;
     }
     const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
     const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    k_gemm_tn_drain<BNT><<<grid, Drain<BNT>::THREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, M, N, K, ldc, kd, err);
+    k_gemm_tn_drain<BNT, SPLIT><<<grid, Drain<BNT>::THREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc,
+                                                                                  kd, err);
     AFQ_LAUNCHED("k_gemm_tn_drain");
     return AFQ_OK;
 }
 
-int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
-                            long long ldc, int* err, cudaStream_t s, int kd) {
+static int drain_prologue(int K, int kd) {
     using namespace tc;
-    if (M <= 0 || N <= 0) return AFQ_OK;
     if (K <= 0 || K % BK) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: K=%d must be a positive multiple of %d", K, BK);
+    if (kd < 1) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: k blocks per partial %d < 1", kd);
     AFQ_TRY(get_encode());
     if (!g_num_sms) {
         int dev = 0;
@@ -621,8 +497,22 @@ int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, c
         AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
         AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     }
-    if (kd < 1) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: k blocks per partial %d < 1", kd);
-    return launch_drain<128>(M, N, K, A, lda, B, ldb, C, ldc, kd, err, s);
+    return AFQ_OK;
+}
+
+int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                            long long ldc, int* err, cudaStream_t s, int kd) {
+    if (M <= 0 || N <= 0) return AFQ_OK;
+    AFQ_TRY(drain_prologue(K, kd));
+    return launch_drain<128, false>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
+}
+
+int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb,
+                                  __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int* err, cudaStream_t s,
+                                  int kd) {
+    if (M <= 0 || N <= 0) return AFQ_OK;
+    AFQ_TRY(drain_prologue(K, kd));
+    return launch_drain<128, true>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
 }
 
 }  // namespace afq

@@ -1,0 +1,369 @@
+// Taylor propagation of the three-section mixed form (AFQ_PREC_MIXED_FAST)
+// on the tensor cores (prop/chol_afqmc_ops.py:173-183, prop/utils.py:20-31):
+//   W1 = W + (E - I) W;   out = W1 + sum_{k=1..K} (i sqrt_dt V)^k / k! W1;
+//   W' = out + (E - I) out
+// with E = exp(-dt h1 / 2) and V = sum_g x_g L_g of the walker.
+//
+// Each complex product is one real GEMM per 128-row tile of the walker:
+//   [Yr | Yi] = [Vr | Vi] . B,   B = [[Tr, Ti], [-Ti, Tr]]   (K = 2n)
+// on tcgen05.mma kind::f16 (M = 128, K = 16).  Operands are two-piece bf16
+// splits, x = hi + mid, and each K step issues A_hi . [B_hi; B_mid] (N = 128,
+// the hi.hi and hi.mid products land in separate accumulator columns and A is
+// read once) and A_mid . B_hi (N = 64): hi.hi + hi.mid + mid.hi, ~2^-17
+// relative, the precision of the three-section GEMMs.  Keeping hi.hi in an
+// accumulator of its own bounds the tensor cores' truncating fp32
+// accumulation to one add per K step of the dominant sum.  The E - I products
+// use A = [(E - I) | 0], i.e. only the top half of B's K range.
+//
+// A (V of the walker, or E - I: hi and mid tiles of 128 rows x 64 K) streams
+// by TMA through a three-stage ring.  B, the current Taylor term, lives in
+// shared memory in the 128-byte-swizzled K-major layout the MMA reads, and is
+// rewritten by the epilogue warps after each product: rows c < o hold
+// [Tr; -Ti] of column c, rows 32 + c hold [Ti; Tr] (so output column c is Yr
+// and 32 + c is Yi), rows 64.. the same for the mid piece.  The top half of
+// B's K range holds rows 0..n-1 at K = i, the bottom half at K = 16 S + i
+// (S = ceil(n / 16) K steps per half), so no K step straddles the two halves.
+// Per 128-row tile the tensor memory holds 192 fp32 columns: hi.hi, hi.mid,
+// mid.hi, summed by the epilogue with round-to-nearest adds.
+//
+// The binary64 walker is read and written only by the epilogue thread that
+// owns the row, and the fp32 sum of the series terms stays in that thread's
+// registers, so the binary64 pipe sees three additions per entry.
+//
+// Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-9 epilogue
+// (warp w reads lanes 32 (w % 4).. of the accumulator of tile (w - 2) / 4,
+// as tcgen05.ld allows).  Persistent over the chunk's walkers, one walker at
+// a time per CTA.  Every mbarrier wait is bounded; on a timeout the CTA
+// raises *err and unwinds (the producer waits for its copies in flight, the
+// MMA thread for its MMAs, and the tensor memory is freed).
+#include "afq_internal.cuh"
+#include "tc_common.cuh"
+
+namespace afq {
+namespace tc {
+
+constexpr int TT_THREADS = 320;
+constexpr int TT_N = 64;                 // output columns: 32 Yr, 32 Yi (nocc <= 32)
+constexpr int TT_STG = 3;                // A stages
+constexpr int TT_TILE = 128 * 64 * 2;    // one 128 x 64 bf16 tile, 16 KB
+constexpr int TT_STAGE = 2 * TT_TILE;    // hi + mid
+constexpr int TT_BBLK = 2 * TT_N * 128;  // one 64-wide K block of B (hi rows 0-63, mid rows 64-127), 16 KB
+constexpr int TT_MAXKBB = 8;             // B K blocks for norb <= 256
+constexpr int TT_TCOLS = 3 * TT_N;       // tensor-memory columns per tile: hi.hi | hi.mid | mid.hi
+constexpr int TT_SMEM = TT_MAXKBB * TT_BBLK + TT_STG * TT_STAGE + 1024 + 256;
+constexpr uint32_t TT_IDESC128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                                 ((uint32_t)(128 >> 4) << 24);
+constexpr uint32_t TT_IDESC64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                                ((uint32_t)(128 >> 4) << 24);
+static_assert(TT_SMEM <= 227 * 1024, "tensor-core Trotter shared memory");
+
+// Byte offset of element (row r, K index k) of B (K-major, 128-byte swizzle:
+// 16-byte chunk index XOR row % 8 within each 8-row, 1024-byte atom).
+__device__ __forceinline__ uint32_t tt_boff(int r, int k) {
+    return (uint32_t)((k >> 6) * TT_BBLK + (r >> 3) * 1024 + (r & 7) * 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) +
+                      ((k & 7) << 1));
+}
+
+__device__ __forceinline__ void tt_put(uint8_t* b, int r, int k, float v) {
+    const __nv_bfloat16 h = __float2bfloat16(v);
+    const __nv_bfloat16 m = __float2bfloat16(v - __bfloat162float(h));
+    *(__nv_bfloat16*)(b + tt_boff(r, k)) = h;
+    *(__nv_bfloat16*)(b + tt_boff(TT_N + r, k)) = m;
+}
+
+// B <- the embedding of T(i, c) = t, c < o, for this thread's row i.
+__device__ __forceinline__ void tt_write_b(uint8_t* b, int i, int kb0, int c, float2 t) {
+    tt_put(b, c, i, t.x);
+    tt_put(b, c, kb0 + i, -t.y);
+    tt_put(b, 32 + c, i, t.y);
+    tt_put(b, 32 + c, kb0 + i, t.x);
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__global__ void __launch_bounds__(TT_THREADS, 1)
+    k_trotter_tc(const __grid_constant__ CUtensorMap mVh, const __grid_constant__ CUtensorMap mVm,
+                 const __grid_constant__ CUtensorMap mEh, const __grid_constant__ CUtensorMap mEm, int wc, int n,
+                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, int* __restrict__ err) {
+    extern __shared__ uint8_t tt_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)tt_raw + 1023) & ~(uintptr_t)1023);
+    const int S = (n + 15) >> 4;             // K steps per half
+    const int KBB = (2 * S + 3) >> 2;        // B K blocks
+    const int kbh = (n + 63) >> 6;           // A K blocks per half
+    const int MT = (n + 127) >> 7;           // 128-row tiles
+    const int R = n_terms + 2;               // products per walker
+    uint8_t* sB = smem;
+    uint8_t* sA = smem + TT_MAXKBB * TT_BBLK;
+    uint64_t* bars = (uint64_t*)(sA + TT_STG * TT_STAGE);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TT_STG + 3);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TT_STG);
+    const uint32_t dfull = smem_u32(bars + 2 * TT_STG), bready = smem_u32(bars + 2 * TT_STG + 1);
+    const uint32_t drain = smem_u32(bars + 2 * TT_STG + 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TT_STG; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(dfull, 1);
+        mbar_init(bready, TT_THREADS - 64);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mVh) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mVm) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mEh) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mEm) : "memory");
+            int stage = 0;
+            uint32_t phase = 0;
+            int issued[TT_STG];
+            uint32_t issued_par[TT_STG];
+            for (int s = 0; s < TT_STG; ++s) issued[s] = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
+                for (int r = 0; ok && r < R; ++r) {
+                    const bool e = (r == 0 || r == R - 1);
+                    for (int mt = 0; ok && mt < MT; ++mt)
+                        for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
+                            for (int kb = 0; kb < kbh; ++kb) {
+                                if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
+                                issued[stage] = 0;
+                                const uint32_t full = full0 + 8 * stage;
+                                const uint32_t dh = smem_u32(sA + stage * TT_STAGE), dm = dh + TT_TILE;
+                                mbar_expect_tx(full, TT_STAGE);
+                                if (e) {
+                                    tma_load_2d(dh, &mEh, kb * 64, mt * 128, full);
+                                    tma_load_2d(dm, &mEm, kb * 64, mt * 128, full);
+                                } else {
+                                    const int y = (hf * wc + w) * n + mt * 128;
+                                    tma_load_2d(dh, &mVh, kb * 64, y, full);
+                                    tma_load_2d(dm, &mVm, kb * 64, y, full);
+                                }
+                                issued[stage] = 1;
+                                issued_par[stage] = phase;
+                                if (++stage == TT_STG) { stage = 0; phase ^= 1; }
+                            }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                for (int s = 0; s < TT_STG; ++s)
+                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, rr = 0;
+            bool ok = true;
+            const uint32_t b0 = smem_u32(sB);
+            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
+                for (int r = 0; ok && r < R; ++r, ++rr) {
+                    const bool e = (r == 0 || r == R - 1);
+                    if (!mbar_wait(bready, rr & 1, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    for (int mt = 0; ok && mt < MT; ++mt) {
+                        uint32_t acc = 0;
+                        const uint32_t d = tmem + mt * TT_TCOLS;
+                        for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
+                            for (int kb = 0; kb < kbh; ++kb) {
+                                if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                                tc_fence_after();
+                                const uint32_t ah = smem_u32(sA + stage * TT_STAGE), am = ah + TT_TILE;
+                                for (int s = 0; s < 4; ++s) {
+                                    const int t = kb * 4 + s;
+                                    if (t >= S) break;
+                                    const int g = hf * S + t;  // K step within B
+                                    const uint64_t db = desc_k128(b0 + (uint32_t)((g >> 2) * TT_BBLK + (g & 3) * 32));
+                                    // hi . [hi; mid] -> columns 0-127, mid . hi -> columns 128-191
+                                    umma_bf16_i(d, desc_k128(ah + 32 * s), db, TT_IDESC128, acc);
+                                    umma_bf16_i(d + 2 * TT_N, desc_k128(am + 32 * s), db, TT_IDESC64, acc);
+                                    acc = 1;
+                                }
+                                umma_commit(empty0 + 8 * stage);
+                                if (++stage == TT_STG) { stage = 0; phase ^= 1; }
+                            }
+                    }
+                    if (ok) umma_commit(dfull);
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                umma_commit(drain);
+                mbar_wait(drain, 0, nullptr);
+            }
+        }
+    } else {
+        const int q = warp & 3, mt = (warp - 2) >> 2;
+        const int i = mt * 128 + q * 32 + lane;
+        const bool row = i < n;
+        const int kb0 = 16 * S;  // K index of the bottom half
+        // B starts (and its padding stays) zero
+        for (int e = threadIdx.x - 64; e < KBB * TT_BBLK / 16; e += TT_THREADS - 64)
+            ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
+        asm volatile("bar.sync 1, %0;" ::"r"(TT_THREADS - 64) : "memory");
+        uint32_t rr = 0;
+        bool ok = true;
+        for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
+            double2* Wr = wout + ((size_t)w * n + i) * o;   // this thread's row
+            const double2* Wi = win + ((size_t)w * n + i) * o;
+            if (row) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (c < o) {
+                        const double2 v = Wi[c];
+                        tt_write_b(sB, i, kb0, c, make_float2((float)v.x, (float)v.y));
+                    }
+            }
+            fence_proxy_async();
+            mbar_arrive(bready);
+            float2 S2[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) S2[c] = make_float2(0.f, 0.f);
+            for (int r = 0; r < R; ++r, ++rr) {
+                if (!mbar_wait_inl(dfull, rr & 1, abort_flag)) {
+                    atomicExch(err, 1);
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t dv[64];  // Y = hi.hi + hi.mid + mid.hi, columns 0-31 Yr, 32-63 Yi
+                {
+                    const uint32_t ta = tmem + mt * TT_TCOLS + ((uint32_t)(q * 32) << 16);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        uint32_t a[32], b[32];
+                        tmem_ld32(ta + 32 * h, a);
+                        tmem_ld32(ta + TT_N + 32 * h, b);
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) a[c] = __float_as_uint(__uint_as_float(a[c]) + __uint_as_float(b[c]));
+                        tmem_ld32(ta + 2 * TT_N + 32 * h, b);
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) dv[32 * h + c] = __float_as_uint(__uint_as_float(a[c]) + __uint_as_float(b[c]));
+                    }
+                }
+                if (row) {
+                    if (r == 0) {  // W1 = W + (E - I) W
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (c < o) {
+                                const double2 v = Wi[c];
+                                const double2 w1 = make_double2(v.x + (double)__uint_as_float(dv[c]),
+                                                                v.y + (double)__uint_as_float(dv[32 + c]));
+                                Wr[c] = w1;
+                                tt_write_b(sB, i, kb0, c, make_float2((float)w1.x, (float)w1.y));
+                            }
+                    } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
+                        const float sk = sqrt_dt / (float)r;
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (c < o) {
+                                const float2 t = make_float2(-sk * __uint_as_float(dv[32 + c]), sk * __uint_as_float(dv[c]));
+                                S2[c] = make_float2(S2[c].x + t.x, S2[c].y + t.y);
+                                if (r < n_terms) {
+                                    tt_write_b(sB, i, kb0, c, t);
+                                } else {  // out = W1 + sum
+                                    const double2 v = Wr[c];
+                                    const double2 u = make_double2(v.x + (double)S2[c].x, v.y + (double)S2[c].y);
+                                    Wr[c] = u;
+                                    tt_write_b(sB, i, kb0, c, make_float2((float)u.x, (float)u.y));
+                                }
+                            }
+                    } else {  // W' = out + (E - I) out
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (c < o) {
+                                const double2 v = Wr[c];
+                                Wr[c] = make_double2(v.x + (double)__uint_as_float(dv[c]),
+                                                     v.y + (double)__uint_as_float(dv[32 + c]));
+                            }
+                    }
+                }
+                tc_fence_before();
+                if (r < R - 1) {
+                    fence_proxy_async();
+                    mbar_arrive(bready);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+    }
+}
+
+}  // namespace tc
+
+bool trotter_tc_supported(int n, int o) { return n % 8 == 0 && n <= 256 && o <= 32; }
+
+int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
+                      const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
+                      double2* wout, int* err, cudaStream_t s) {
+    using namespace tc;
+    if (wc <= 0) return AFQ_OK;
+    if (!trotter_tc_supported(n, o))
+        return fail(AFQ_E_UNSUPPORTED, "tensor-core Trotter: norb=%d nocc=%d (needs norb %% 8 == 0, <= 256, nocc <= 32)",
+                    n, o);
+    static bool attr = false;
+    static int nsm = 0;
+    AFQ_TRY(get_encode());
+    if (!attr) {
+        int dev = 0;
+        AFQ_CUDA(cudaGetDevice(&dev));
+        AFQ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        AFQ_CUDA(cudaFuncSetAttribute(k_trotter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_SMEM));
+        attr = true;
+    }
+    CUtensorMap mvh, mvm, meh, mem;
+    AFQ_TRY(make_map(&mvh, vh, 2LL * wc * n, n, n, 128));
+    AFQ_TRY(make_map(&mvm, vm, 2LL * wc * n, n, n, 128));
+    AFQ_TRY(make_map(&meh, eh, n, n, n, 128));
+    AFQ_TRY(make_map(&mem, em, n, n, n, 128));
+    const int grid = wc < nsm ? wc : nsm;
+    k_trotter_tc<<<grid, TT_THREADS, TT_SMEM, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, win, wout,
+                                                 err);
+    AFQ_LAUNCHED("k_trotter_tc");
+    return AFQ_OK;
+}
+
+// (E - I) as bf16 hi and mid pieces (n x n), the A operand of the E products.
+__global__ void k_e_minus_i_split(int n, const double* __restrict__ E, __nv_bfloat16* __restrict__ eh,
+                                  __nv_bfloat16* __restrict__ em) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+        const float v = (float)(E[e] - ((e / n) == (e % n) ? 1.0 : 0.0));
+        const __nv_bfloat16 h = __float2bfloat16(v);
+        eh[e] = h;
+        em[e] = __float2bfloat16(v - __bfloat162float(h));
+    }
+}
+
+int launch_e_minus_i_split(int n, const double* E, __nv_bfloat16* eh, __nv_bfloat16* em, cudaStream_t s) {
+    k_e_minus_i_split<<<(n * n + 255) / 256, 256, 0, s>>>(n, E, eh, em);
+    AFQ_LAUNCHED("k_e_minus_i_split");
+    return AFQ_OK;
+}
+
+}  // namespace afq

@@ -47,8 +47,11 @@ PRECISIONS = ["mixed", "mixed_fast"]
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
-@pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 64), ("c1_n12_o6_g48_w256", 100)])
+@pytest.mark.parametrize("wl,W", [("c3_n60_o10_g300_w1024", 64), ("c1_n12_o6_g48_w256", 100),
+                                  ("c4_n200_o30_g1000_w4096", 40)])
 def test_mixed_step_close_to_fp64(cuda, wl, W, prec):
+    """c4 (norb 200 = 8 k, nocc 30 <= 32) takes the tensor-core Taylor kernel
+    in the three-section form; c1 and c3 the fp32 SIMT one."""
     from ad_afqmc_prototype_gb300 import engine
     pa, pra, st = _setup(wl, W, "fp64")
     pb, prb, _ = _setup(wl, W, prec)
