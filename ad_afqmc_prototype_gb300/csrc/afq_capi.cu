@@ -287,7 +287,8 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
                                                     lb.Bv, L.Kt_V, vh, vmid, L.ldv, ws.status, s)); }
             { AFQ_PHASE("trotter", s);
               AFQ_TRY(launch_trotter_tc(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.esplit, ws.esplit + (size_t)n * n, vh,
-                                        vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.status, s)); }
+                                        vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.tsum, ws.status,
+                                        s)); }
         }
     } else {
     AFQ_TRY(launch_e_minus_i(n, pb->exp_h1_half, ws.emi, s));
@@ -412,6 +413,10 @@ static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cu
     if (ws && is_mixed(d->precision))
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
                                     (double2*)st->overlaps, fb_split(d, *ws), s);
+    // the three-section energy resolves less than fp32: its Green's function in fp32
+    if (green_out && d->precision == AFQ_PREC_MIXED_FAST)
+        return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
+                                    (double2*)st->overlaps, SplitOut{}, s, green_out);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
                         (double2*)st->overlaps, green_out, s);
 }

@@ -240,13 +240,13 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
                          long long ldv, const double2* win, double2* wout, float2* tsum, cudaStream_t s);
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
-                         SplitOut split, cudaStream_t s);
+                         SplitOut split, cudaStream_t s, double2* green_out = nullptr);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
 // k_trotter_tc.cu
 bool trotter_tc_supported(int n, int o);
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
                       const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
-                      double2* wout, int* err, cudaStream_t s);
+                      double2* wout, float2* scratch, int* err, cudaStream_t s);
 int launch_e_minus_i_split(int n, const double* E, __nv_bfloat16* eh, __nv_bfloat16* em, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);

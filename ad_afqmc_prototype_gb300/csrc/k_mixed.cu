@@ -382,14 +382,17 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 //   m = C^H W in binary64; LU with partial pivoting in binary64 gives
 //   det(m) and the overlap det(m)^2 -- the only binary64 work;
 //   m^-1 by fp32 Gauss-Jordan on a float copy of m, and
-//   G_half^T = W m^-1 in fp32, written as the bf16 hi/lo split operand
-//   (which resolves ~2^-17, so fp32 here costs no accuracy downstream).
+//   G_half^T = W m^-1 in fp32, written as the bf16 split operand (which
+//   resolves at most ~2^-24, so fp32 here costs no accuracy downstream)
+//   and/or, widened, as the Green's function G_half (o x n) the mixed
+//   energy reads (its bf16 split resolves less than fp32 as well).
 // Pivot reciprocals are computed once per pivot and shared through shared
 // memory.  Real trial orbitals (the mixed form requires them).
 template <int MA, bool STAGE_W>
 __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
-                                                       double2* __restrict__ ovlp_out, SplitOut split) {
+                                                       double2* __restrict__ ovlp_out, SplitOut split,
+                                                       double2* __restrict__ green_out) {
     extern __shared__ double2 smd[];
     double2* m = smd;                              // o x o binary64 (LU in place)
     float2* mf = (float2*)(m + o * o);             // o x o fp32 copy -> Gauss-Jordan
@@ -532,9 +535,10 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
         __syncthreads();
     }
 
-    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand
-    __nv_bfloat16* re_row = split.ptr + (size_t)w * split.ld;
-    __nv_bfloat16* im_row = split.ptr + (size_t)(split.W + w) * split.ld;
+    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
+    __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
+    __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
+    double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
     constexpr int BG = 8;
     const int nbg = (o + BG - 1) / BG;
     for (int t = tid; t < n * nbg; t += blockDim.x) {
@@ -564,11 +568,15 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
         for (int j = 0; j < BG; ++j) {
             const int b = bg * BG + j;
             if (b < o) {
-                split_storef(re_row, split.S, b * n + i, acc[j].x, true, split.sec);
-                split_storef(im_row, split.S, b * n + i, acc[j].y, true, split.sec);
+                if (re_row) {
+                    split_storef(re_row, split.S, b * n + i, acc[j].x, true, split.sec);
+                    split_storef(im_row, split.S, b * n + i, acc[j].y, true, split.sec);
+                }
+                if (Gp) Gp[(size_t)b * n + i] = make_double2(acc[j].x, acc[j].y);
             }
         }
     }
+    if (!re_row) return;
     for (int e = n * o + tid; e < split.S; e += blockDim.x) {
         split_storef(re_row, split.S, e, 0.f, true, split.sec);
         split_storef(im_row, split.S, e, 0.f, true, split.sec);
@@ -580,7 +588,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
 }
 
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
-                         SplitOut split, cudaStream_t s) {
+                         SplitOut split, cudaStream_t s, double2* green_out) {
     if (W <= 0) return AFQ_OK;
     const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
     const size_t wbytes = (size_t)n * o * sizeof(float2);
@@ -591,10 +599,10 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
     do {                                                                                          \
         if (stage) {                                                                              \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, true>, smem));                                 \
-            k_overlap_split<MAV, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split);  \
+            k_overlap_split<MAV, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out); \
         } else {                                                                                  \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, false>, smem));                                \
-            k_overlap_split<MAV, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split); \
+            k_overlap_split<MAV, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out); \
         }                                                                                         \
     } while (0)
     if (ma <= 1) AFQ_OS(1);

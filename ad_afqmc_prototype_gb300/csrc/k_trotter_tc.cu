@@ -26,9 +26,11 @@
 // Per 128-row tile the tensor memory holds 192 fp32 columns: hi.hi, hi.mid,
 // mid.hi, summed by the epilogue with round-to-nearest adds.
 //
-// The binary64 walker is read and written only by the epilogue thread that
-// owns the row, and the fp32 sum of the series terms stays in that thread's
-// registers, so the binary64 pipe sees three additions per entry.
+// The walker update W' - W = (E - I) W + sum_k T_k + (E - I) out is summed in
+// fp32 in the registers of the epilogue thread that owns the row (with an
+// fp32 copy of the row in a scratch buffer for the operand sums), and added to
+// the binary64 walker once: per entry the binary64 pipe converts W once and
+// the update once and adds once.
 //
 // Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-9 epilogue
 // (warp w reads lanes 32 (w % 4).. of the accumulator of tile (w - 2) / 4,
@@ -80,11 +82,52 @@ __device__ __forceinline__ void tt_write_b(uint8_t* b, int i, int kb0, int c, fl
 }
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+#define TT_R8(i)                                                                                               \
+    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
+        "=r"(r[i + 7])
+// Six 8-column loads of this warp's 32 lanes, one wait.
+__device__ __forceinline__ void tmem_ld8x6(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4,
+                                           uint32_t a5, uint32_t (&r)[48]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%48];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%49];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%50];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%51];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%32, %33, %34, %35, %36, %37, %38, %39}, [%52];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40, %41, %42, %43, %44, %45, %46, %47}, [%53];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : TT_R8(0), TT_R8(8), TT_R8(16), TT_R8(24), TT_R8(32), TT_R8(40)
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(a4), "r"(a5)
+        : "memory");
+}
+// Two 8-column loads (one wait) and stores (then wait for the stores).
+__device__ __forceinline__ void tmem_ld8x2(uint32_t a0, uint32_t a1, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%16];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%17];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : TT_R8(0), TT_R8(8)
+        : "r"(a0), "r"(a1)
+        : "memory");
+}
+#undef TT_R8
+__device__ __forceinline__ void tmem_st8x2(uint32_t a0, uint32_t a1, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%2, %3, %4, %5, %6, %7, %8, %9};\n\t"
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%1], {%10, %11, %12, %13, %14, %15, %16, %17};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(a0),
+        "r"(a1), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
 
 __global__ void __launch_bounds__(TT_THREADS, 1)
     k_trotter_tc(const __grid_constant__ CUtensorMap mVh, const __grid_constant__ CUtensorMap mVm,
                  const __grid_constant__ CUtensorMap mEh, const __grid_constant__ CUtensorMap mEm, int wc, int n,
-                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, int* __restrict__ err) {
+                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, float2* __restrict__ wf,
+                 int* __restrict__ err) {
     extern __shared__ uint8_t tt_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)tt_raw + 1023) & ~(uintptr_t)1023);
     const int S = (n + 15) >> 4;             // K steps per half
@@ -223,22 +266,31 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         uint32_t rr = 0;
         bool ok = true;
         for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
-            double2* Wr = wout + ((size_t)w * n + i) * o;   // this thread's row
+            double2* Wr = wout + ((size_t)w * n + i) * o;  // this thread's row
             const double2* Wi = win + ((size_t)w * n + i) * o;
+            float2* Fr = wf + ((size_t)w * n + i) * o;      // fp32 copy of the row
             if (row) {
 #pragma unroll
                 for (int c = 0; c < 32; ++c)
                     if (c < o) {
                         const double2 v = Wi[c];
-                        tt_write_b(sB, i, kb0, c, make_float2((float)v.x, (float)v.y));
+                        const float2 f = make_float2((float)v.x, (float)v.y);
+                        Fr[c] = f;
+                        tt_write_b(sB, i, kb0, c, f);
                     }
             }
             fence_proxy_async();
             mbar_arrive(bready);
-            float2 S2[32];
-#pragma unroll
-            for (int c = 0; c < 32; ++c) S2[c] = make_float2(0.f, 0.f);
+            // S = (E - I) W + sum of the series terms (the walker update before the last E
+            // product) lives in tensor memory next to the accumulators: Re in 32 columns, Im in 32
+            const uint32_t ts = tmem + 2 * TT_TCOLS + mt * TT_N + ((uint32_t)(q * 32) << 16);
             for (int r = 0; r < R; ++r, ++rr) {
+                if (row && r == R - 1) {  // rows read after the last product: this walker's, the next one's
+                    for (int b = 0; b < o * 16; b += 128) prefetch_l2((const char*)Wi + b);
+                    if (w + (int)gridDim.x < wc)
+                        for (int b = 0; b < o * 16; b += 128)
+                            prefetch_l2((const char*)(Wi + (size_t)gridDim.x * n * o) + b);
+                }
                 if (!mbar_wait_inl(dfull, rr & 1, abort_flag)) {
                     atomicExch(err, 1);
                     *abort_flag = 1;
@@ -246,57 +298,49 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                uint32_t dv[64];  // Y = hi.hi + hi.mid + mid.hi, columns 0-31 Yr, 32-63 Yi
-                {
-                    const uint32_t ta = tmem + mt * TT_TCOLS + ((uint32_t)(q * 32) << 16);
+                const uint32_t ta = tmem + mt * TT_TCOLS + ((uint32_t)(q * 32) << 16);
+                const float sk = sqrt_dt / (float)(r > 0 ? r : 1);
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        uint32_t a[32], b[32];
-                        tmem_ld32(ta + 32 * h, a);
-                        tmem_ld32(ta + TT_N + 32 * h, b);
+                for (int cb = 0; cb < 32; cb += 8) {
+                    // Y columns cb..cb+7: hi.hi + hi.mid + mid.hi of Yr and of Yi
+                    uint32_t y[48], sv[16];  // sv: S of columns cb..cb+7, Re then Im
+                    tmem_ld8x6(ta + cb, ta + TT_N + cb, ta + 2 * TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb,
+                               ta + 2 * TT_N + 32 + cb, y);
+                    if (r > 0) tmem_ld8x2(ts + cb, ts + 32 + cb, sv);
+                    if (row) {
 #pragma unroll
-                        for (int c = 0; c < 32; ++c) a[c] = __float_as_uint(__uint_as_float(a[c]) + __uint_as_float(b[c]));
-                        tmem_ld32(ta + 2 * TT_N + 32 * h, b);
-#pragma unroll
-                        for (int c = 0; c < 32; ++c) dv[32 * h + c] = __float_as_uint(__uint_as_float(a[c]) + __uint_as_float(b[c]));
-                    }
-                }
-                if (row) {
-                    if (r == 0) {  // W1 = W + (E - I) W
-#pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (c < o) {
-                                const double2 v = Wi[c];
-                                const double2 w1 = make_double2(v.x + (double)__uint_as_float(dv[c]),
-                                                                v.y + (double)__uint_as_float(dv[32 + c]));
-                                Wr[c] = w1;
-                                tt_write_b(sB, i, kb0, c, make_float2((float)w1.x, (float)w1.y));
-                            }
-                    } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
-                        const float sk = sqrt_dt / (float)r;
-#pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (c < o) {
-                                const float2 t = make_float2(-sk * __uint_as_float(dv[32 + c]), sk * __uint_as_float(dv[c]));
-                                S2[c] = make_float2(S2[c].x + t.x, S2[c].y + t.y);
+                        for (int u = 0; u < 8; ++u) {
+                            const int c = cb + u;
+                            if (c >= o) continue;
+                            const float yr =
+                                (__uint_as_float(y[u]) + __uint_as_float(y[8 + u])) + __uint_as_float(y[16 + u]);
+                            const float yi = (__uint_as_float(y[24 + u]) + __uint_as_float(y[32 + u])) +
+                                             __uint_as_float(y[40 + u]);
+                            float sr = __uint_as_float(sv[u]), si = __uint_as_float(sv[8 + u]);
+                            if (r == 0) {  // W1 = W + (E - I) W
+                                sr = yr;
+                                si = yi;
+                                const float2 f = Fr[c];
+                                tt_write_b(sB, i, kb0, c, make_float2(f.x + yr, f.y + yi));
+                            } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
+                                const float2 t = make_float2(-sk * yi, sk * yr);
+                                sr += t.x;
+                                si += t.y;
                                 if (r < n_terms) {
                                     tt_write_b(sB, i, kb0, c, t);
-                                } else {  // out = W1 + sum
-                                    const double2 v = Wr[c];
-                                    const double2 u = make_double2(v.x + (double)S2[c].x, v.y + (double)S2[c].y);
-                                    Wr[c] = u;
-                                    tt_write_b(sB, i, kb0, c, make_float2((float)u.x, (float)u.y));
+                                } else {  // out = W1 + sum_k T_k
+                                    const float2 f = Fr[c];
+                                    tt_write_b(sB, i, kb0, c, make_float2(f.x + sr, f.y + si));
                                 }
+                            } else {  // W' = W + (S + (E - I) out): the one binary64 update
+                                const double2 v = Wi[c];
+                                Wr[c] = make_double2(v.x + (double)(sr + yr), v.y + (double)(si + yi));
                             }
-                    } else {  // W' = out + (E - I) out
-#pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (c < o) {
-                                const double2 v = Wr[c];
-                                Wr[c] = make_double2(v.x + (double)__uint_as_float(dv[c]),
-                                                     v.y + (double)__uint_as_float(dv[32 + c]));
-                            }
+                            sv[u] = __float_as_uint(sr);
+                            sv[8 + u] = __float_as_uint(si);
+                        }
                     }
+                    if (r < R - 1) tmem_st8x2(ts + cb, ts + 32 + cb, sv);
                 }
                 tc_fence_before();
                 if (r < R - 1) {
@@ -321,7 +365,7 @@ bool trotter_tc_supported(int n, int o) { return n % 8 == 0 && n <= 256 && o <= 
 
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
                       const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
-                      double2* wout, int* err, cudaStream_t s) {
+                      double2* wout, float2* scratch, int* err, cudaStream_t s) {
     using namespace tc;
     if (wc <= 0) return AFQ_OK;
     if (!trotter_tc_supported(n, o))
@@ -344,7 +388,7 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
     AFQ_TRY(make_map(&mem, em, n, n, n, 128));
     const int grid = wc < nsm ? wc : nsm;
     k_trotter_tc<<<grid, TT_THREADS, TT_SMEM, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, win, wout,
-                                                 err);
+                                                 scratch, err);
     AFQ_LAUNCHED("k_trotter_tc");
     return AFQ_OK;
 }
