@@ -114,6 +114,7 @@ struct StepWS {
     float* emi;         // n*n
     float2* tsum;       // Wc*n*o: fp32 sum of the Taylor terms of a chunk
     __nv_bfloat16* esplit;  // 2 n*n: E - I as bf16 hi, mid (tensor-core Taylor products)
+    float2* csplit;     // n*o: trial orbitals as (hi, lo) fp32 pairs (double-float overlap)
 };
 
 static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
@@ -134,6 +135,7 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         s.emi = a.take<float>(n * n);
         s.tsum = a.take<float2>(Wc * n * o);
         s.esplit = a.take<__nv_bfloat16>(2 * n * n);
+        s.csplit = a.take<float2>(n * o);
     } else {
         s.green = a.take<double2>(W * o * n);
         s.fb = a.take<double2>(W * G);
@@ -262,10 +264,11 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     const LowpBufs lb = layout_lowp(la, d);
     const double2* mo = (const double2*)pb->mo_coeff;
     double2* walk = (double2*)st->walkers;
+    AFQ_TRY(launch_split_c(n * o, mo, ws.csplit, s));
     // force bias: G_half split straight from the Green's function kernel
     if (!green_ready) {
         AFQ_PHASE("green", s);
-        AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, nullptr, fb_split(d, ws), s));
+        AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, nullptr, fb_split(d, ws), s, nullptr, ws.csplit));
     }
     { AFQ_PHASE("fb_gemm", s);
       AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s)); }
@@ -304,7 +307,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     }
     // overlaps, and the next step's force-bias operand from the same factorisation
     { AFQ_PHASE("overlap", s);
-      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s)); }
+      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s, nullptr, ws.csplit)); }
     AFQ_PHASE("weight_update", s);
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
@@ -401,7 +404,8 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
 // either the next step's force-bias operand (mixed, ws given) or, with
 // green_out, the Green's function the block's energy needs.
 static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s,
-                                  const StepWS* ws = nullptr, double2* green_out = nullptr) {
+                                  const StepWS* ws = nullptr, double2* green_out = nullptr,
+                                  const float2* cs = nullptr) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
     {
@@ -412,11 +416,11 @@ static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cu
     AFQ_PHASE(green_out ? "green" : "overlap", s);
     if (ws && is_mixed(d->precision))
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
-                                    (double2*)st->overlaps, fb_split(d, *ws), s);
+                                    (double2*)st->overlaps, fb_split(d, *ws), s, nullptr, ws->csplit);
     // the three-section energy resolves less than fp32: its Green's function in fp32
     if (green_out && d->precision == AFQ_PREC_MIXED_FAST)
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
-                                    (double2*)st->overlaps, SplitOut{}, s, green_out);
+                                    (double2*)st->overlaps, SplitOut{}, s, green_out, cs);
     return launch_green(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, d->trial_is_real, walk,
                         (double2*)st->overlaps, green_out, s);
 }
@@ -783,7 +787,9 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
             AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));
     }
     // prop/blocks.py:53-57, with the energy's Green's function from the same pass
-    AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green));
+    if (is_mixed(d->precision))
+        AFQ_TRY(launch_split_c(n * o, (const double2*)pb->mo_coeff, ws.step.csplit, s));
+    AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green, is_mixed(d->precision) ? ws.step.csplit : nullptr));
     // prop/blocks.py:59-79
     AFQ_TRY(energy_impl(pb, st, ws, s, true));
     { AFQ_PHASE("block_measure", s);

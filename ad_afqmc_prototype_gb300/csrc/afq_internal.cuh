@@ -239,8 +239,10 @@ int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double*
                              double2* fb_term, cudaStream_t s);
 int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, const float* emi, const float* vm,
                          long long ldv, const double2* win, double2* wout, float2* tsum, cudaStream_t s);
+// cs (optional): (hi, lo) fp32 pairs of the trial orbitals -> double-float m
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
-                         SplitOut split, cudaStream_t s, double2* green_out = nullptr);
+                         SplitOut split, cudaStream_t s, double2* green_out = nullptr, const float2* cs = nullptr);
+int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
 // k_trotter_tc.cu
 bool trotter_tc_supported(int n, int o);

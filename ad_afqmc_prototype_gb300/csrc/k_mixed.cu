@@ -388,16 +388,38 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 //   energy reads (its bf16 split resolves less than fp32 as well).
 // Pivot reciprocals are computed once per pivot and shared through shared
 // memory.  Real trial orbitals (the mixed form requires them).
-template <int MA, bool STAGE_W>
+//
+// DF: m by double-float arithmetic on the fp32 pipe instead of binary64
+// FMAs (the binary64 pipe runs ~1/64 of the fp32 rate on this GPU).  C and W
+// are split as x = x_hi + x_lo (fp32 pair, 48 significant bits); each term's
+// c_hi w_hi is formed exactly (TwoProd: product and fma residual) and summed
+// by TwoSum into (s, e), while the residual, c_hi w_lo and c_lo w_hi go to
+// the fp32 error sum e: m = s + e to ~2^-44 relative, binary64 for the
+// determinant's purposes, from fp32 instructions only.
+constexpr int OS_CH = 64;  // rows of W per double-float staging chunk
+
+__device__ __forceinline__ void df_acc(float& s, float& e, float ch, float cl, float wh, float wl) {
+    const float p = __fmul_rn(ch, wh);
+    const float pe = __fmaf_rn(ch, wh, -p);  // exact: ch wh = p + pe
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v));  // exact: s + p = t + r
+    s = t;
+    e = __fadd_rn(e, __fadd_rn(__fadd_rn(r, pe), __fmaf_rn(ch, wl, __fmul_rn(cl, wh))));
+}
+
+template <int MA, bool STAGE_W, bool DF>
 __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
                                                        double2* __restrict__ ovlp_out, SplitOut split,
-                                                       double2* __restrict__ green_out) {
+                                                       double2* __restrict__ green_out,
+                                                       const float2* __restrict__ cs) {
     extern __shared__ double2 smd[];
     double2* m = smd;                              // o x o binary64 (LU in place)
     float2* mf = (float2*)(m + o * o);             // o x o fp32 copy -> Gauss-Jordan
     float2* invf = mf + o * o;                     // o x o fp32 inverse
-    float2* wf = invf + o * o;                     // n x o fp32 copy of W
+    float2* wf = invf + o * o;                     // n x o fp32 copy of W (its hi part)
+    float2* wl = wf + (size_t)OS_CH * o;           // DF: lo part of a chunk of OS_CH rows
     __shared__ int s_piv;
     __shared__ double2 s_rp;
     __shared__ float2 s_rpf;
@@ -405,7 +427,56 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
-    {  // m (binary64) and the fp32 copy of W
+    if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
+        const int AG = blockDim.x / o;
+        const int b = tid % o, ag = tid / o;
+        float sr[MA], er[MA], si[MA], ei[MA];
+#pragma unroll
+        for (int k = 0; k < MA; ++k) sr[k] = er[k] = si[k] = ei[k] = 0.f;
+        for (int i0 = 0; i0 < n; i0 += OS_CH) {
+            const int rows = min(OS_CH, n - i0);
+            __syncthreads();
+            for (int e = tid; e < rows * o; e += blockDim.x) {
+                const double2 x = Wp[(size_t)i0 * o + e];
+                const float2 h = make_float2((float)x.x, (float)x.y);
+                wf[e] = h;
+                wl[e] = make_float2((float)(x.x - (double)h.x), (float)(x.y - (double)h.y));
+            }
+            __syncthreads();
+            if (ag < AG) {
+                for (int i = 0; i < rows; ++i) {
+                    const float2 xh = wf[i * o + b], xl = wl[i * o + b];
+#pragma unroll
+                    for (int k = 0; k < MA; ++k) {
+                        const int a = ag + AG * k;
+                        if (a < o) {
+                            const float2 c = cs[(i0 + i) * o + a];  // (hi, lo) of C[i, a]
+                            df_acc(sr[k], er[k], c.x, c.y, xh.x, xl.x);
+                            df_acc(si[k], ei[k], c.x, c.y, xh.y, xl.y);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < n * o; e += blockDim.x) {  // the fp32 copy of W for G_half
+            const double2 x = Wp[e];
+            wf[e] = make_float2((float)x.x, (float)x.y);
+        }
+        if (ag < AG) {
+#pragma unroll
+            for (int k = 0; k < MA; ++k) {
+                const int a = ag + AG * k;
+                if (a < o) {
+                    const double2 v = make_double2((double)sr[k] + (double)er[k], (double)si[k] + (double)ei[k]);
+                    m[a * o + b] = v;
+                    mf[a * o + b] = make_float2((float)v.x, (float)v.y);
+                }
+            }
+        }
+        for (int e = tid; e < o * o; e += blockDim.x)
+            invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
+    } else {  // m (binary64) and the fp32 copy of W
         const int AG = blockDim.x / o;
         const int b = tid % o, ag = tid / o;
         double2 acc[MA];
@@ -588,22 +659,29 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
 }
 
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
-                         SplitOut split, cudaStream_t s, double2* green_out) {
+                         SplitOut split, cudaStream_t s, double2* green_out, const float2* cs) {
     if (W <= 0) return AFQ_OK;
     const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
     const size_t wbytes = (size_t)n * o * sizeof(float2);
-    const bool stage = base + wbytes <= 160 * 1024;  // else read W from global in the last loop
-    const size_t smem = base + (stage ? wbytes : 0);
+    const size_t dfbytes = 2 * (size_t)OS_CH * o * sizeof(float2);
+    const bool df = cs && base + (wbytes > dfbytes ? wbytes : dfbytes) <= 160 * 1024;  // double-float m
+    const bool stage = df || base + wbytes <= 160 * 1024;  // else read W from global in the last loop
+    const size_t smem = base + (df ? (wbytes > dfbytes ? wbytes : dfbytes) : stage ? wbytes : 0);
     const int ag = 256 / o, ma = (o + ag - 1) / ag;
-#define AFQ_OS(MAV)                                                                               \
-    do {                                                                                          \
-        if (stage) {                                                                              \
-            AFQ_TRY(smem_attr(k_overlap_split<MAV, true>, smem));                                 \
-            k_overlap_split<MAV, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out); \
-        } else {                                                                                  \
-            AFQ_TRY(smem_attr(k_overlap_split<MAV, false>, smem));                                \
-            k_overlap_split<MAV, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out); \
-        }                                                                                         \
+#define AFQ_OS(MAV)                                                                                              \
+    do {                                                                                                         \
+        if (df) {                                                                                                \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, true, true>, smem));                                          \
+            k_overlap_split<MAV, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, cs); \
+        } else if (stage) {                                                                                      \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, true, false>, smem));                                         \
+            k_overlap_split<MAV, true, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out,  \
+                                                                  nullptr);                                      \
+        } else {                                                                                                 \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, false, false>, smem));                                        \
+            k_overlap_split<MAV, false, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, \
+                                                                   nullptr);                                     \
+        }                                                                                                        \
     } while (0)
     if (ma <= 1) AFQ_OS(1);
     else if (ma <= 2) AFQ_OS(2);
@@ -906,6 +984,22 @@ int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, 
     dim3 grid(exchange_chunks(G), wc);
     k_exchange_reduce<<<grid, 256, smem, s>>>(G, o, F, ldf, partial, exchange_chunks(G), v16);
     AFQ_LAUNCHED("k_exchange_reduce");
+    return AFQ_OK;
+}
+
+// (hi, lo) fp32 pair of each real trial orbital coefficient, for the
+// double-float overlap.
+__global__ void k_split_c(int count, const double2* __restrict__ mo, float2* __restrict__ cs) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+        const double c = mo[e].x;
+        const float h = (float)c;
+        cs[e] = make_float2(h, (float)(c - (double)h));
+    }
+}
+
+int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s) {
+    k_split_c<<<(count + 255) / 256, 256, 0, s>>>(count, mo, cs);
+    AFQ_LAUNCHED("k_split_c");
     return AFQ_OK;
 }
 

@@ -109,3 +109,24 @@ def test_mixed_block_energy_error_per_block(cuda, prec):
     assert engine.workspace_status() == 0
     print("per-block |dE| (Ha):", errs)
     assert max(errs) < 1e-4, errs
+
+
+def test_mixed_overlap_matches_binary64(cuda):
+    """The mixed forms form m = C^H W in double-float arithmetic (fp32 pairs,
+    ~2^-44): after a block of zero steps (QR, overlap, energy, comb) the
+    overlaps agree with the binary64 form's to 1e-10 relative."""
+    from ad_afqmc_prototype_gb300 import engine
+    W = 64
+    pa, pra, st = _setup("c4_n200_o30_g1000_w4096", W, "fp64", n_prop_steps=3)
+    pb, prb, _ = _setup("c4_n200_o30_g1000_w4096", W, "mixed_fast", n_prop_steps=3)
+    a = _dstate(st)
+    engine.block(pa, pra, a, 5, 0)  # move the walkers off the trial
+    z0a = pra.__class__(**{**pra.__dict__, "n_prop_steps": 0})
+    z0b = prb.__class__(**{**prb.__dict__, "n_prop_steps": 0})
+    x = engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)])
+    y = engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)])
+    engine.block(pa, z0a, x, 5, 100, zeta=0.5)
+    engine.block(pb, z0b, y, 5, 100, zeta=0.5)
+    assert engine.workspace_status() == 0
+    rel = float(((x.overlaps - y.overlaps).abs() / x.overlaps.abs()).max().item())
+    assert rel < 1e-10, rel
