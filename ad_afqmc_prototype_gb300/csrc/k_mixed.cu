@@ -696,19 +696,23 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
 // ---------------------------------------------------- orthonormalisation --
 // Mixed-form QR with the reference's output (walkers.py:169-211: the unique
 // Q with diag(R) real and > 0), by CholeskyQR2 in shared memory, one CTA per
-// walker:
-//   pass 1: G1 = W^H W with fp32 products, R1 = chol(G1) in binary64,
-//           X = W R1^-1 by binary64 forward substitution;
-//   pass 2: G2 = X^H X, R2 = chol(G2), Q = X R2^-1, all binary64.
-// X spans W's columns to binary64 accuracy whatever the error of R1 (R1 only
+// walker, with the walker held as fp32 pairs x = x_hi + x_lo (48 significant
+// bits) and its products formed in double-float arithmetic on the fp32 pipe
+// (df_acc: TwoProd + TwoSum), which runs ~64x the binary64 rate here:
+//   pass 1: G1 = W_hi^H W_hi in fp32, R1 = chol(G1) in binary64,
+//           X = W R1^-1 by double-float forward substitution;
+//   pass 2: G2 = X^H X in double-float, R2 = chol(G2) in binary64,
+//           Q = X R2^-1 in double-float, widened to binary64.
+// X spans W's columns to ~2^-44 whatever the error of R1 (R1 only
 // preconditions), and pass 2 restores orthonormality; Q = W (R2 R1)^-1 with
 // R2 R1 upper triangular with a positive real diagonal, the Householder
 // form's Q.  If a pivot of the fp32 Gram matrix falls below 1e-5 of its
 // column's squared norm (cond(W) beyond ~300, where fp32 rounding would
-// leave X far from orthonormal), pass 1 is redone with binary64 products.  A
-// numerically rank-deficient W (a non-positive binary64 pivot) gets the
-// pivot 1 and a zero row of R there, so the output stays finite; such a
-// walker has a vanishing overlap and no weight.
+// leave X far from orthonormal), G1 is recomputed in double-float.  A
+// numerically rank-deficient W (a non-positive pivot) gets the pivot 1 and a
+// zero row of R there, so the output stays finite; such a walker has a
+// vanishing overlap and no weight.
+
 // Upper-triangle entry e (row-major) -> (j, k), j <= k.
 __device__ __forceinline__ void cq_entry(int o, int e, int& j, int& k) {
     j = 0;
@@ -716,74 +720,36 @@ __device__ __forceinline__ void cq_entry(int o, int e, int& j, int& k) {
     k = j + e;
 }
 
-constexpr int CQ_RB = 32;   // rows per fp32 conversion block
-constexpr int CQ_RS = CQ_RB + 1;  // odd stride (in float2): a warp's columns fall in distinct banks
-constexpr int CQ_EPT = 9;   // upper-triangle entries per thread (o <= 64: 2080 <= 256 x 9)
-
-// fp32 Gram matrix: rows of A are converted to fp32 once per block of CQ_RB
-// rows (buf: o columns of CQ_RS float2), so the binary64 pipe only converts.
-__device__ __forceinline__ void cq_gram_f32(int n, int o, int ld, const double2* A, double2* Gm, float2* buf) {
-    const int P = o * (o + 1) / 2;
-    float2 acc[CQ_EPT];
-    int jj[CQ_EPT], kk[CQ_EPT];
-#pragma unroll
-    for (int t = 0; t < CQ_EPT; ++t) {
-        acc[t] = make_float2(0.f, 0.f);
-        const int e = threadIdx.x + t * blockDim.x;
-        if (e < P) cq_entry(o, e, jj[t], kk[t]);
-        else jj[t] = kk[t] = -1;
-    }
-    for (int r0 = 0; r0 < n; r0 += CQ_RB) {
-        const int rn = min(CQ_RB, n - r0);
-        __syncthreads();
-        for (int e = threadIdx.x; e < rn * o; e += blockDim.x) {
-            const int j = e / rn, r = e % rn;
-            const double2 v = A[(size_t)j * ld + r0 + r];
-            buf[j * CQ_RS + r] = make_float2((float)v.x, (float)v.y);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int t = 0; t < CQ_EPT; ++t) {
-            if (jj[t] < 0) continue;
-            const float2* a = buf + jj[t] * CQ_RS;
-            const float2* b = buf + kk[t] * CQ_RS;
-            float sr = acc[t].x, si = acc[t].y;
-            for (int r = 0; r < rn; ++r) {
-                const float2 x = a[r], y = b[r];
-                sr = fmaf(x.x, y.x, fmaf(x.y, y.y, sr));
-                si = fmaf(x.x, y.y, fmaf(-x.y, y.x, si));
-            }
-            acc[t] = make_float2(sr, si);
-        }
-    }
-#pragma unroll
-    for (int t = 0; t < CQ_EPT; ++t)
-        if (jj[t] >= 0) Gm[jj[t] * o + kk[t]] = make_double2(acc[t].x, acc[t].y);
-}
-
-__device__ __forceinline__ void cq_gram(int n, int o, int ld, const double2* A, double2* Gm) {
+// Gram matrix of the columns of A = Ah + Al (column-major, leading dim ld)
+// into Gm (upper triangle, binary64): from Ah alone in fp32 (DF false) or in
+// double-float (DF true).
+template <bool DF>
+__device__ __forceinline__ void cq_gram(int n, int o, int ld, const float2* Ah, const float2* Al, double2* Gm) {
     const int P = o * (o + 1) / 2;
     for (int e = threadIdx.x; e < P; e += blockDim.x) {
         int j, k;
         cq_entry(o, e, j, k);
-        const double2* a = A + (size_t)j * ld;
-        const double2* b = A + (size_t)k * ld;
-        {  // four independent chains
-            double sr0 = 0.0, si0 = 0.0, sr1 = 0.0, si1 = 0.0;
-            int i = 0;
-            for (; i + 1 < n; i += 2) {
-                const double2 x0 = a[i], y0 = b[i], x1 = a[i + 1], y1 = b[i + 1];
-                sr0 = fma(x0.x, y0.x, fma(x0.y, y0.y, sr0));
-                si0 = fma(x0.x, y0.y, fma(-x0.y, y0.x, si0));
-                sr1 = fma(x1.x, y1.x, fma(x1.y, y1.y, sr1));
-                si1 = fma(x1.x, y1.y, fma(-x1.y, y1.x, si1));
+        const float2* ah = Ah + (size_t)j * ld;
+        const float2* bh = Ah + (size_t)k * ld;
+        float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+        if (DF) {
+            const float2* al = Al + (size_t)j * ld;
+            const float2* bl = Al + (size_t)k * ld;
+            for (int i = 0; i < n; ++i) {  // conj(a) b
+                const float2 xh = ah[i], xl = al[i], yh = bh[i], yl = bl[i];
+                df_acc(sr, er, xh.x, xl.x, yh.x, yl.x);
+                df_acc(sr, er, xh.y, xl.y, yh.y, yl.y);
+                df_acc(si, ei, xh.x, xl.x, yh.y, yl.y);
+                df_acc(si, ei, -xh.y, -xl.y, yh.x, yl.x);
             }
-            if (i < n) {
-                const double2 x0 = a[i], y0 = b[i];
-                sr0 = fma(x0.x, y0.x, fma(x0.y, y0.y, sr0));
-                si0 = fma(x0.x, y0.y, fma(-x0.y, y0.x, si0));
+            Gm[j * o + k] = make_double2((double)sr + (double)er, (double)si + (double)ei);
+        } else {
+            for (int i = 0; i < n; ++i) {
+                const float2 x = ah[i], y = bh[i];
+                sr = fmaf(x.x, y.x, fmaf(x.y, y.y, sr));
+                si = fmaf(x.x, y.y, fmaf(-x.y, y.x, si));
             }
-            Gm[j * o + k] = make_double2(sr0 + sr1, si0 + si1);
+            Gm[j * o + k] = make_double2(sr, si);
         }
     }
 }
@@ -819,26 +785,53 @@ __device__ __forceinline__ bool cq_chol(int o, double2* Gm, double* det, double 
     return bad;
 }
 
-// A <- A R^-1 in place, one thread per row of A (column-major, leading dim ld).
-__device__ __forceinline__ void cq_solve(int n, int o, int ld, double2* A, const double2* R) {
+// R (upper triangle of Gm, binary64) as double-float pairs for the solve:
+// Rd[j o + k] = (re hi, re lo, im hi, im lo); rinv[k] = (hi, lo) of 1 / R_kk.
+__device__ __forceinline__ void cq_rsplit(int o, const double2* Gm, float4* Rd, float2* rinv) {
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const double2 r = Gm[e];
+        const float rh = (float)r.x, ih = (float)r.y;
+        Rd[e] = make_float4(rh, (float)(r.x - (double)rh), ih, (float)(r.y - (double)ih));
+    }
+    for (int k = threadIdx.x; k < o; k += blockDim.x) {
+        const double v = 1.0 / Gm[k * o + k].x;
+        const float h = (float)v;
+        rinv[k] = make_float2(h, (float)(v - (double)h));
+    }
+    __syncthreads();
+}
+
+// A <- A R^-1 in place in double-float, one thread per row of A.
+__device__ __forceinline__ void cq_solve(int n, int o, int ld, float2* Ah, float2* Al, const float4* Rd,
+                                         const float2* rinv) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        for (int k = 0; k < o; ++k) {  // two independent chains over j
-            double2 a0 = A[(size_t)k * ld + i], a1 = make_double2(0.0, 0.0);
-            int j = 0;
-            for (; j + 1 < k; j += 2) {  // a -= x r, four fused multiply-adds
-                const double2 x0 = A[(size_t)j * ld + i], r0 = R[j * o + k];
-                const double2 x1 = A[(size_t)(j + 1) * ld + i], r1 = R[(j + 1) * o + k];
-                a0.x = fma(-x0.x, r0.x, fma(x0.y, r0.y, a0.x));
-                a0.y = fma(-x0.x, r0.y, fma(-x0.y, r0.x, a0.y));
-                a1.x = fma(-x1.x, r1.x, fma(x1.y, r1.y, a1.x));
-                a1.y = fma(-x1.x, r1.y, fma(-x1.y, r1.x, a1.y));
+        for (int k = 0; k < o; ++k) {
+            const float2 ah = Ah[(size_t)k * ld + i], al = Al[(size_t)k * ld + i];
+            float sr = ah.x, er = al.x, si = ah.y, ei = al.y;
+            for (int j = 0; j < k; ++j) {  // a -= x r
+                const float2 xh = Ah[(size_t)j * ld + i], xl = Al[(size_t)j * ld + i];
+                const float4 r = Rd[j * o + k];
+                df_acc(sr, er, -xh.x, -xl.x, r.x, r.y);
+                df_acc(sr, er, xh.y, xl.y, r.z, r.w);
+                df_acc(si, ei, -xh.x, -xl.x, r.z, r.w);
+                df_acc(si, ei, -xh.y, -xl.y, r.x, r.y);
             }
-            if (j < k) {
-                const double2 x0 = A[(size_t)j * ld + i], r0 = R[j * o + k];
-                a0.x = fma(-x0.x, r0.x, fma(x0.y, r0.y, a0.x));
-                a0.y = fma(-x0.x, r0.y, fma(-x0.y, r0.x, a0.y));
+            const float2 q = rinv[k];  // x = (s + e) q, renormalised to a pair
+            float2 h, l;
+            {
+                const float p = __fmul_rn(sr, q.x);
+                const float t = __fadd_rn(__fmaf_rn(sr, q.x, -p), __fmaf_rn(sr, q.y, __fmul_rn(er, q.x)));
+                h.x = __fadd_rn(p, t);
+                l.x = __fsub_rn(t, __fsub_rn(h.x, p));
             }
-            A[(size_t)k * ld + i] = cscale(cadd(a0, a1), 1.0 / R[k * o + k].x);
+            {
+                const float p = __fmul_rn(si, q.x);
+                const float t = __fadd_rn(__fmaf_rn(si, q.x, -p), __fmaf_rn(si, q.y, __fmul_rn(ei, q.x)));
+                h.y = __fadd_rn(p, t);
+                l.y = __fsub_rn(t, __fsub_rn(h.y, p));
+            }
+            Ah[(size_t)k * ld + i] = h;
+            Al[(size_t)k * ld + i] = l;
         }
     }
     __syncthreads();
@@ -850,36 +843,51 @@ __global__ void __launch_bounds__(256) k_cholqr2(int n, int o, const double2* __
     __shared__ double s_det;  // prod diag(R1) prod diag(R2) = prod diag(R)
     __shared__ double s_d0[64];
     const int ld = n | 1;
-    double2* A = csm;                     // ld x o, A[j ld + i] = W[i, j]
-    double2* Gm = csm + (size_t)ld * o;  // o x o
-    float2* buf = (float2*)(Gm + o * o);  // CQ_RB x o
+    double2* Gm = csm;                                // o x o binary64
+    float4* Rd = (float4*)(Gm + o * o);               // o x o double-float R
+    float2* rinv = (float2*)(Rd + o * o);             // o
+    float2* Ah = rinv + ((o + 1) & ~1);               // ld x o: A[j ld + i] = W[i, j], hi
+    float2* Al = Ah + (size_t)ld * o;                 // lo
     const int w = blockIdx.x;
     const double2* Wp = win + (size_t)w * n * o;
-    for (int e = threadIdx.x; e < n * o; e += blockDim.x) A[(size_t)(e % o) * ld + e / o] = Wp[e];
+    for (int e = threadIdx.x; e < n * o; e += blockDim.x) {
+        const double2 x = Wp[e];
+        const float2 h = make_float2((float)x.x, (float)x.y);
+        const size_t d = (size_t)(e % o) * ld + e / o;
+        Ah[d] = h;
+        Al[d] = make_float2((float)(x.x - (double)h.x), (float)(x.y - (double)h.y));
+    }
     if (threadIdx.x == 0) s_det = 1.0;
     __syncthreads();
-    cq_gram_f32(n, o, ld, A, Gm, buf);
+    cq_gram<false>(n, o, ld, Ah, Al, Gm);
     __syncthreads();
-    if (cq_chol(o, Gm, &s_det, 1e-5, s_d0)) {  // fp32 cannot resolve W's conditioning: binary64 products
+    if (cq_chol(o, Gm, &s_det, 1e-5, s_d0)) {  // fp32 cannot resolve W's conditioning: double-float G1
         if (threadIdx.x == 0) s_det = 1.0;
-        cq_gram(n, o, ld, A, Gm);
+        cq_gram<true>(n, o, ld, Ah, Al, Gm);
         __syncthreads();
         cq_chol(o, Gm, &s_det, 0.0, s_d0);
     }
-    cq_solve(n, o, ld, A, Gm);
-    cq_gram(n, o, ld, A, Gm);
+    cq_rsplit(o, Gm, Rd, rinv);
+    cq_solve(n, o, ld, Ah, Al, Rd, rinv);
+    cq_gram<true>(n, o, ld, Ah, Al, Gm);
     __syncthreads();
     cq_chol(o, Gm, &s_det, 0.0, s_d0);
-    cq_solve(n, o, ld, A, Gm);
+    cq_rsplit(o, Gm, Rd, rinv);
+    cq_solve(n, o, ld, Ah, Al, Rd, rinv);
     double2* Wo = wout + (size_t)w * n * o;
-    for (int e = threadIdx.x; e < n * o; e += blockDim.x) Wo[e] = A[(size_t)(e % o) * ld + e / o];
+    for (int e = threadIdx.x; e < n * o; e += blockDim.x) {
+        const size_t d = (size_t)(e % o) * ld + e / o;
+        const float2 h = Ah[d], l = Al[d];
+        Wo[e] = make_double2((double)h.x + (double)l.x, (double)h.y + (double)l.y);
+    }
     if (det_out && threadIdx.x == 0) det_out[w] = make_double2(s_det, 0.0);
 }
 
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     if (o > 64) return fail(AFQ_E_UNSUPPORTED, "qr: nocc=%d > 64", o);
-    const size_t smem = ((size_t)(n | 1) * o + (size_t)o * o) * sizeof(double2) + (size_t)CQ_RS * o * sizeof(float2);
+    const size_t smem = (size_t)o * o * (sizeof(double2) + sizeof(float4)) + (size_t)((o + 1) & ~1) * sizeof(float2) +
+                        2 * (size_t)(n | 1) * o * sizeof(float2);
     AFQ_TRY(smem_attr(k_cholqr2, smem));
     k_cholqr2<<<W, 256, smem, s>>>(n, o, win, wout, det_r);
     AFQ_LAUNCHED("k_cholqr2");
