@@ -1,12 +1,14 @@
-// Kernels of the mixed-precision step (AFQ_PREC_MIXED).
+// Kernels of the mixed-precision steps (AFQ_PREC_MIXED, AFQ_PREC_MIXED_FAST).
 //
 // Precision plan: the V-build, force-bias and energy contractions run on
-// tensor cores (k_tc_gemm.cu) with bf16 hi/lo split operands and fp32
-// accumulation (~2^-17 relative); the Taylor series multiplies in fp32 but
-// adds every term into binary64 walkers, and applies E_half as
+// tensor cores (k_tc_gemm.cu) with bf16 split operands (six sections, every
+// product above 2^-24, or three sections, ~2^-17) and drained fp32
+// accumulation; the Taylor series multiplies in fp32 (here, or on the tensor
+// cores in k_trotter_tc.cu) and updates binary64 walkers, applying E_half as
 // W + (E_half - I) W with the small correction in fp32, so the walkers carry
-// binary64 and do not drift; overlaps (det), QR, weights, the phaseless
-// cut and every energy accumulator stay binary64.
+// binary64 and do not drift.  The overlap matrix and the QR run in
+// double-float (fp32 pairs) on the fp32 pipe; the determinant's LU, the
+// phaseless cut, the weights and every energy accumulator stay binary64.
 #include "afq_internal.cuh"
 
 namespace afq {

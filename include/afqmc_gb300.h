@@ -122,8 +122,9 @@ int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* 
                        const double* chol, const double* mo_coeff, int32_t trial_is_real,
                        double* rot_h1, double* rot_chol, void* stream);
 
-/* Low-precision copies of chol / rot_chol for AFQ_PREC_MIXED (bf16 hi+lo
- * splits in tensor-core tile order).  `out` must hold afq_lowp_bytes(). */
+/* Low-precision copies of chol / rot_chol for AFQ_PREC_MIXED / MIXED_FAST
+ * (bf16 splits in six or three K sections, tensor-core operand order; the
+ * layout depends on d->precision).  `out` must hold afq_lowp_bytes(). */
 size_t afq_lowp_bytes(const afq_dims* d);
 int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_chol,
                      void* out, size_t out_bytes, void* stream);
@@ -136,8 +137,9 @@ int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_ch
  * expired (the kernel then stops early instead of hanging).
  * accumulate: 0 = fp32 accumulation inside the tensor cores (truncating:
  * a sum of K positive terms drifts low by ~K/16 * 2^-25 relative);
- * 1 = each 64-wide K block is a fresh tensor-core partial, summed in fp32
- * registers with round-to-nearest adds (what the mixed step uses). */
+ * d >= 1 = every d 64-wide K blocks form a fresh tensor-core partial,
+ * summed in fp32 registers with round-to-nearest adds (the mixed step
+ * uses d = 1). */
 int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B,
                      int64_t ldb, float* C, int64_t ldc, int32_t* err, int32_t accumulate,
                      void* stream);
