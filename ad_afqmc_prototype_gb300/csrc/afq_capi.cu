@@ -290,8 +290,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
                                                     lb.Bv, L.Kt_V, vh, vmid, L.ldv, ws.status, s)); }
             { AFQ_PHASE("trotter", s);
               AFQ_TRY(launch_trotter_tc(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.esplit, ws.esplit + (size_t)n * n, vh,
-                                        vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.tsum, ws.status,
-                                        s)); }
+                                        vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.status, s)); }
         }
     } else {
     AFQ_TRY(launch_e_minus_i(n, pb->exp_h1_half, ws.emi, s));

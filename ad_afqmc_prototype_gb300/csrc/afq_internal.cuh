@@ -248,7 +248,7 @@ int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, doubl
 bool trotter_tc_supported(int n, int o);
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
                       const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
-                      double2* wout, float2* scratch, int* err, cudaStream_t s);
+                      double2* wout, int* err, cudaStream_t s);
 int launch_e_minus_i_split(int n, const double* E, __nv_bfloat16* eh, __nv_bfloat16* em, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);

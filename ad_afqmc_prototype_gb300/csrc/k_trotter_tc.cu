@@ -9,10 +9,11 @@
 // on tcgen05.mma kind::f16 (M = 128, K = 16).  Operands are two-piece bf16
 // splits, x = hi + mid, and each K step issues A_hi . [B_hi; B_mid] (N = 128,
 // the hi.hi and hi.mid products land in separate accumulator columns and A is
-// read once) and A_mid . B_hi (N = 64): hi.hi + hi.mid + mid.hi, ~2^-17
-// relative, the precision of the three-section GEMMs.  Keeping hi.hi in an
-// accumulator of its own bounds the tensor cores' truncating fp32
-// accumulation to one add per K step of the dominant sum.  The E - I products
+// read once) and A_mid . B_hi (N = 64, into the hi.mid columns): hi.hi +
+// hi.mid + mid.hi, ~2^-17 relative, the precision of the three-section
+// GEMMs.  Keeping hi.hi in an accumulator of its own bounds the tensor
+// cores' truncating fp32 accumulation to one add per K step of the dominant
+// sum.  The E - I products
 // use A = [(E - I) | 0], i.e. only the top half of B's K range.
 //
 // A (V of the walker, or E - I: hi and mid tiles of 128 rows x 64 K) streams
@@ -23,14 +24,16 @@
 // and 32 + c is Yi), rows 64.. the same for the mid piece.  The top half of
 // B's K range holds rows 0..n-1 at K = i, the bottom half at K = 16 S + i
 // (S = ceil(n / 16) K steps per half), so no K step straddles the two halves.
-// Per 128-row tile the tensor memory holds 192 fp32 columns: hi.hi, hi.mid,
-// mid.hi, summed by the epilogue with round-to-nearest adds.
+// Tensor memory (512 columns): per 128-row tile 128 accumulator columns
+// (hi.hi | hi.mid + mid.hi, summed by the epilogue with a round-to-nearest
+// add), then per tile 64 columns of the running walker update and 64 of the
+// fp32 copy of the walker's rows.
 //
 // The walker update W' - W = (E - I) W + sum_k T_k + (E - I) out is summed in
-// fp32 in the registers of the epilogue thread that owns the row (with an
-// fp32 copy of the row in a scratch buffer for the operand sums), and added to
-// the binary64 walker once: per entry the binary64 pipe converts W once and
-// the update once and adds once.
+// fp32 by the epilogue thread that owns the row (in tensor memory, next to
+// an fp32 copy of the row for the operand sums), and added to the binary64
+// walker once: per entry the binary64 pipe converts W once and the update
+// once and adds once.
 //
 // Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-9 epilogue
 // (warp w reads lanes 32 (w % 4).. of the accumulator of tile (w - 2) / 4,
@@ -51,7 +54,9 @@ constexpr int TT_TILE = 128 * 64 * 2;    // one 128 x 64 bf16 tile, 16 KB
 constexpr int TT_STAGE = 2 * TT_TILE;    // hi + mid
 constexpr int TT_BBLK = 2 * TT_N * 128;  // one 64-wide K block of B (hi rows 0-63, mid rows 64-127), 16 KB
 constexpr int TT_MAXKBB = 8;             // B K blocks for norb <= 256
-constexpr int TT_TCOLS = 3 * TT_N;       // tensor-memory columns per tile: hi.hi | hi.mid | mid.hi
+constexpr int TT_TCOLS = 2 * TT_N;       // accumulator columns per tile: hi.hi | hi.mid + mid.hi
+constexpr int TT_SCOL = 2 * TT_TCOLS;    // running update: tile t at TT_SCOL + t TT_N (Re 32, Im 32)
+constexpr int TT_FCOL = TT_SCOL + 2 * TT_N;  // fp32 copy of the rows, same layout
 constexpr int TT_SMEM = TT_MAXKBB * TT_BBLK + TT_STG * TT_STAGE + 1024 + 256;
 constexpr uint32_t TT_IDESC128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
                                  ((uint32_t)(128 >> 4) << 24);
@@ -113,6 +118,22 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t a0, uint32_t a1, uint32_t (&
         : "memory");
 }
 #undef TT_R8
+// Four 8-column loads, one wait.
+#define TT_R8(i)                                                                                               \
+    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
+        "=r"(r[i + 7])
+__device__ __forceinline__ void tmem_ld8x4(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%33];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%34];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%35];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : TT_R8(0), TT_R8(8), TT_R8(16), TT_R8(24)
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3)
+        : "memory");
+}
+#undef TT_R8
 __device__ __forceinline__ void tmem_st8x2(uint32_t a0, uint32_t a1, const uint32_t (&v)[16]) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%2, %3, %4, %5, %6, %7, %8, %9};\n\t"
@@ -126,8 +147,7 @@ __device__ __forceinline__ void tmem_st8x2(uint32_t a0, uint32_t a1, const uint3
 __global__ void __launch_bounds__(TT_THREADS, 1)
     k_trotter_tc(const __grid_constant__ CUtensorMap mVh, const __grid_constant__ CUtensorMap mVm,
                  const __grid_constant__ CUtensorMap mEh, const __grid_constant__ CUtensorMap mEm, int wc, int n,
-                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, float2* __restrict__ wf,
-                 int* __restrict__ err) {
+                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, int* __restrict__ err) {
     extern __shared__ uint8_t tt_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)tt_raw + 1023) & ~(uintptr_t)1023);
     const int S = (n + 15) >> 4;             // K steps per half
@@ -235,9 +255,9 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                     if (t >= S) break;
                                     const int g = hf * S + t;  // K step within B
                                     const uint64_t db = desc_k128(b0 + (uint32_t)((g >> 2) * TT_BBLK + (g & 3) * 32));
-                                    // hi . [hi; mid] -> columns 0-127, mid . hi -> columns 128-191
+                                    // hi . [hi; mid] -> columns 0-127, mid . hi added to columns 64-127
                                     umma_bf16_i(d, desc_k128(ah + 32 * s), db, TT_IDESC128, acc);
-                                    umma_bf16_i(d + 2 * TT_N, desc_k128(am + 32 * s), db, TT_IDESC64, acc);
+                                    umma_bf16_i(d + TT_N, desc_k128(am + 32 * s), db, TT_IDESC64, 1);
                                     acc = 1;
                                 }
                                 umma_commit(empty0 + 8 * stage);
@@ -268,22 +288,30 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
             double2* Wr = wout + ((size_t)w * n + i) * o;  // this thread's row
             const double2* Wi = win + ((size_t)w * n + i) * o;
-            float2* Fr = wf + ((size_t)w * n + i) * o;      // fp32 copy of the row
-            if (row) {
+            const uint32_t lq = (uint32_t)(q * 32) << 16;
+            const uint32_t ta = tmem + mt * TT_TCOLS + lq;            // accumulator
+            const uint32_t ts = tmem + TT_SCOL + mt * TT_N + lq;      // running update
+            const uint32_t tf = tmem + TT_FCOL + mt * TT_N + lq;      // fp32 copy of the row
 #pragma unroll
-                for (int c = 0; c < 32; ++c)
-                    if (c < o) {
+            for (int cb = 0; cb < 32; cb += 8) {
+                uint32_t fv[16];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int c = cb + u;
+                    float2 f = make_float2(0.f, 0.f);
+                    if (row && c < o) {
                         const double2 v = Wi[c];
-                        const float2 f = make_float2((float)v.x, (float)v.y);
-                        Fr[c] = f;
+                        f = make_float2((float)v.x, (float)v.y);
                         tt_write_b(sB, i, kb0, c, f);
                     }
+                    fv[u] = __float_as_uint(f.x);
+                    fv[8 + u] = __float_as_uint(f.y);
+                }
+                tmem_st8x2(tf + cb, tf + 32 + cb, fv);
             }
+            tc_fence_before();
             fence_proxy_async();
             mbar_arrive(bready);
-            // S = (E - I) W + sum of the series terms (the walker update before the last E
-            // product) lives in tensor memory next to the accumulators: Re in 32 columns, Im in 32
-            const uint32_t ts = tmem + 2 * TT_TCOLS + mt * TT_N + ((uint32_t)(q * 32) << 16);
             for (int r = 0; r < R; ++r, ++rr) {
                 if (row && r == R - 1) {  // rows read after the last product: this walker's, the next one's
                     for (int b = 0; b < o * 16; b += 128) prefetch_l2((const char*)Wi + b);
@@ -298,43 +326,37 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t ta = tmem + mt * TT_TCOLS + ((uint32_t)(q * 32) << 16);
                 const float sk = sqrt_dt / (float)(r > 0 ? r : 1);
 #pragma unroll
                 for (int cb = 0; cb < 32; cb += 8) {
-                    // Y columns cb..cb+7: hi.hi + hi.mid + mid.hi of Yr and of Yi
-                    uint32_t y[48], sv[16];  // sv: S of columns cb..cb+7, Re then Im
-                    tmem_ld8x6(ta + cb, ta + TT_N + cb, ta + 2 * TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb,
-                               ta + 2 * TT_N + 32 + cb, y);
-                    if (r > 0) tmem_ld8x2(ts + cb, ts + 32 + cb, sv);
+                    // Y columns cb..cb+7 of Yr and Yi (hi.hi + corrections); S and the row copy
+                    uint32_t y[32], sf[32];
+                    tmem_ld8x4(ta + cb, ta + TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb, y);
+                    tmem_ld8x4(ts + cb, ts + 32 + cb, tf + cb, tf + 32 + cb, sf);
+                    uint32_t sv[16];
                     if (row) {
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
                             const int c = cb + u;
-                            if (c >= o) continue;
-                            const float yr =
-                                (__uint_as_float(y[u]) + __uint_as_float(y[8 + u])) + __uint_as_float(y[16 + u]);
-                            const float yi = (__uint_as_float(y[24 + u]) + __uint_as_float(y[32 + u])) +
-                                             __uint_as_float(y[40 + u]);
-                            float sr = __uint_as_float(sv[u]), si = __uint_as_float(sv[8 + u]);
-                            if (r == 0) {  // W1 = W + (E - I) W
-                                sr = yr;
-                                si = yi;
-                                const float2 f = Fr[c];
-                                tt_write_b(sB, i, kb0, c, make_float2(f.x + yr, f.y + yi));
-                            } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
-                                const float2 t = make_float2(-sk * yi, sk * yr);
-                                sr += t.x;
-                                si += t.y;
-                                if (r < n_terms) {
-                                    tt_write_b(sB, i, kb0, c, t);
-                                } else {  // out = W1 + sum_k T_k
-                                    const float2 f = Fr[c];
-                                    tt_write_b(sB, i, kb0, c, make_float2(f.x + sr, f.y + si));
+                            const float yr = __uint_as_float(y[u]) + __uint_as_float(y[8 + u]);
+                            const float yi = __uint_as_float(y[16 + u]) + __uint_as_float(y[24 + u]);
+                            float sr = __uint_as_float(sf[u]), si = __uint_as_float(sf[8 + u]);
+                            const float fr = __uint_as_float(sf[16 + u]), fi = __uint_as_float(sf[24 + u]);
+                            if (c < o) {
+                                if (r == 0) {  // W1 = W + (E - I) W
+                                    sr = yr;
+                                    si = yi;
+                                    tt_write_b(sB, i, kb0, c, make_float2(fr + yr, fi + yi));
+                                } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
+                                    const float2 t = make_float2(-sk * yi, sk * yr);
+                                    sr += t.x;
+                                    si += t.y;
+                                    if (r < n_terms) tt_write_b(sB, i, kb0, c, t);
+                                    else tt_write_b(sB, i, kb0, c, make_float2(fr + sr, fi + si));  // out = W1 + sum T_k
+                                } else {  // W' = W + (S + (E - I) out): the one binary64 update
+                                    const double2 v = Wi[c];
+                                    Wr[c] = make_double2(v.x + (double)(sr + yr), v.y + (double)(si + yi));
                                 }
-                            } else {  // W' = W + (S + (E - I) out): the one binary64 update
-                                const double2 v = Wi[c];
-                                Wr[c] = make_double2(v.x + (double)(sr + yr), v.y + (double)(si + yi));
                             }
                             sv[u] = __float_as_uint(sr);
                             sv[8 + u] = __float_as_uint(si);
@@ -365,7 +387,7 @@ bool trotter_tc_supported(int n, int o) { return n % 8 == 0 && n <= 256 && o <= 
 
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
                       const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
-                      double2* wout, float2* scratch, int* err, cudaStream_t s) {
+                      double2* wout, int* err, cudaStream_t s) {
     using namespace tc;
     if (wc <= 0) return AFQ_OK;
     if (!trotter_tc_supported(n, o))
@@ -388,7 +410,7 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
     AFQ_TRY(make_map(&mem, em, n, n, n, 128));
     const int grid = wc < nsm ? wc : nsm;
     k_trotter_tc<<<grid, TT_THREADS, TT_SMEM, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, win, wout,
-                                                 scratch, err);
+                                                 err);
     AFQ_LAUNCHED("k_trotter_tc");
     return AFQ_OK;
 }
