@@ -398,7 +398,7 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 // by TwoSum into (s, e), while the residual, c_hi w_lo and c_lo w_hi go to
 // the fp32 error sum e: m = s + e to ~2^-44 relative, binary64 for the
 // determinant's purposes, from fp32 instructions only.
-constexpr int OS_CH = 64;  // rows of W per double-float staging chunk
+constexpr int OS_CH = 32;  // rows of W per staging chunk (double-float m, then G_half)
 
 __device__ __forceinline__ void df_acc(float& s, float& e, float ch, float cl, float wh, float wl) {
     const float p = __fmul_rn(ch, wh);
@@ -459,11 +459,6 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
                     }
                 }
             }
-        }
-        __syncthreads();
-        for (int e = tid; e < n * o; e += blockDim.x) {  // the fp32 copy of W for G_half
-            const double2 x = Wp[e];
-            wf[e] = make_float2((float)x.x, (float)x.y);
         }
         if (ag < AG) {
 #pragma unroll
@@ -614,15 +609,26 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
     double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
     constexpr int BG = 8;
     const int nbg = (o + BG - 1) / BG;
-    for (int t = tid; t < n * nbg; t += blockDim.x) {
-        const int i = t % n, bg = t / n;
+    // DF: W's fp32 copy is staged again OS_CH rows at a time (fewer bytes of shared memory, more CTAs)
+    for (int i0 = 0; i0 < n; i0 += DF ? OS_CH : n) {
+    const int rows = DF ? min(OS_CH, n - i0) : n;
+    if (DF) {
+        __syncthreads();
+        for (int e = tid; e < rows * o; e += blockDim.x) {
+            const double2 x = Wp[(size_t)i0 * o + e];
+            wf[e] = make_float2((float)x.x, (float)x.y);
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < rows * nbg; t += blockDim.x) {
+        const int il = t % rows, bg = t / rows, i = i0 + il;
         float2 acc[BG];
 #pragma unroll
         for (int j = 0; j < BG; ++j) acc[j] = make_float2(0.f, 0.f);
         for (int a = 0; a < o; ++a) {
             float2 x;
             if (STAGE_W) {
-                x = wf[i * o + a];
+                x = wf[il * o + a];
             } else {
                 const double2 v = Wp[(size_t)i * o + a];
                 x = make_float2((float)v.x, (float)v.y);
@@ -649,6 +655,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             }
         }
     }
+    }
     if (!re_row) return;
     for (int e = n * o + tid; e < split.S; e += blockDim.x) {
         split_storef(re_row, split.S, e, 0.f, true, split.sec);
@@ -666,9 +673,9 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
     const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
     const size_t wbytes = (size_t)n * o * sizeof(float2);
     const size_t dfbytes = 2 * (size_t)OS_CH * o * sizeof(float2);
-    const bool df = cs && base + (wbytes > dfbytes ? wbytes : dfbytes) <= 160 * 1024;  // double-float m
+    const bool df = cs != nullptr;                          // double-float m, W staged in chunks
     const bool stage = df || base + wbytes <= 160 * 1024;  // else read W from global in the last loop
-    const size_t smem = base + (df ? (wbytes > dfbytes ? wbytes : dfbytes) : stage ? wbytes : 0);
+    const size_t smem = base + (df ? dfbytes : stage ? wbytes : 0);
     const int ag = 256 / o, ma = (o + ag - 1) / ag;
 #define AFQ_OS(MAV)                                                                                              \
     do {                                                                                                         \
