@@ -23,6 +23,11 @@ AFQ_PREC_FP64 = 0
 AFQ_PREC_MIXED = 1
 AFQ_PREC_MIXED_FAST = 2
 
+AFQ_CV_OFF = 0
+AFQ_CV_RECORD = 1
+AFQ_CV_ESTIMATE = 2
+AFQ_CV_FEATURES = 64
+
 
 class afq_dims(Structure):
     _fields_ = [("n_walkers", c_int32), ("norb", c_int32), ("nocc", c_int32), ("nchol", c_int32),
@@ -45,6 +50,13 @@ class afq_problem(Structure):
 class afq_state(Structure):
     _fields_ = [("walkers", c_void_p), ("weights", c_void_p), ("overlaps", c_void_p),
                 ("pop_control_ene_shift", c_void_p), ("e_estimate", c_void_p)]
+
+
+class afq_cv(Structure):
+    _fields_ = [("mode", c_int32), ("hidden", c_int32), ("n_sample", c_int32), ("pad_", c_int32),
+                ("net", c_void_p), ("feat_shift", c_void_p), ("feat_scale", c_void_p), ("y_shift", c_double),
+                ("y_scale", c_double), ("rec_features", c_void_p), ("rec_exchange", c_void_p),
+                ("stats", c_void_p)]
 
 
 P = c_void_p
@@ -87,6 +99,14 @@ _SIGS = {
     "afq_block_workspace": (c_size_t, [POINTER(afq_dims), c_int32]),
     "afq_block": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_double,
                             c_uint64, c_uint64, P, P, P, P, c_size_t, P]),
+    "afq_block_cv": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_double,
+                               c_uint64, c_uint64, P, P, P, POINTER(afq_cv), P, c_size_t, P]),
+    "afq_mlp_param_count": (c_size_t, [c_int32, c_int32]),
+    "afq_mlp_forward": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P]),
+    "afq_mlp_train_workspace": (c_size_t, [c_int32, c_int32, c_int32]),
+    "afq_mlp_train_step": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P, P, P, ctypes.c_float, c_int32, P,
+                                     c_size_t, P, P]),
+    "afq_mlp_sync": (c_int32, [c_int32, c_int32, P, P, P]),
     "afq_launch_count": (ctypes.c_longlong, []),
     "afq_timing_enable": (c_int32, [c_int32]),
     "afq_timing_report": (c_int32, [ctypes.c_char_p, c_size_t]),

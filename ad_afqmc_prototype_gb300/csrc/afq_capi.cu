@@ -167,6 +167,11 @@ struct BlockWS {
     double2* ocopy;      // W
     __nv_bfloat16* Bg;   // mixed energy: 2 o We x Kt_E
     float* F;            // mixed energy: G o x 2 o We
+    float* cv_feat;      // mixed: W x AFQ_CV_FEATURES
+    float* cv_y;         // mixed: W network outputs
+    double* cv_ebase;    // mixed: W energies without exchange
+    double* cv_u;        // mixed: 1 uniform
+    int* cv_off;         // mixed: sample offset
 };
 
 static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
@@ -181,6 +186,11 @@ static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
         b.partial = (double*)a.take<double2>(W * exchange_chunks(d->nchol) * 2);
         b.Bg = a.take<__nv_bfloat16>(2 * d->nocc * we * L.Kt_E);
         b.F = a.take<float>((size_t)d->nchol * d->nocc * 2 * d->nocc * we);
+        b.cv_feat = a.take<float>(W * AFQ_CV_FEATURES);
+        b.cv_y = a.take<float>(W);
+        b.cv_ebase = a.take<double>(W);
+        b.cv_u = a.take<double>(1);
+        b.cv_off = a.take<int>(1);
     } else {
         b.partial = (double*)a.take<double2>(energy_partial_count(d->n_walkers, d->nocc, d->nchol));
     }
@@ -766,11 +776,31 @@ size_t afq_block_workspace(const afq_dims* d, int32_t n_chunks) {
 int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields, double zeta,
               uint64_t seed, uint64_t counter, double* block_energy, double* block_weight, int32_t* sr_idx,
               void* workspace, size_t workspace_bytes, void* stream) {
+    return afq_block_cv(pb, p, st, fields, zeta, seed, counter, block_energy, block_weight, sr_idx, nullptr,
+                        workspace, workspace_bytes, stream);
+}
+
+int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields, double zeta,
+                 uint64_t seed, uint64_t counter, double* block_energy, double* block_weight, int32_t* sr_idx,
+                 const afq_cv* cv, void* workspace, size_t workspace_bytes, void* stream) {
     AFQ_TRY(check_problem(pb));
     AFQ_TRY(check_params(p));
     AFQ_TRY(check_state(st));
     AFQ_NOTNULL(block_energy); AFQ_NOTNULL(block_weight); AFQ_NOTNULL(workspace);
     const afq_dims* d = &pb->dims;
+    const int cvmode = cv ? cv->mode : AFQ_CV_OFF;
+    if (cvmode != AFQ_CV_OFF) {
+        if (cvmode != AFQ_CV_RECORD && cvmode != AFQ_CV_ESTIMATE)
+            return fail(AFQ_E_INVALID_ARGUMENT, "cv mode %d", cvmode);
+        if (!is_mixed(d->precision)) return fail(AFQ_E_UNSUPPORTED, "the control variate needs a mixed precision");
+        if (cvmode == AFQ_CV_RECORD) { AFQ_NOTNULL(cv->rec_features); AFQ_NOTNULL(cv->rec_exchange); }
+        if (cvmode == AFQ_CV_ESTIMATE) {
+            AFQ_NOTNULL(cv->net); AFQ_NOTNULL(cv->feat_shift); AFQ_NOTNULL(cv->feat_scale);
+            if (cv->n_sample < 1) return fail(AFQ_E_INVALID_ARGUMENT, "cv n_sample=%d < 1", cv->n_sample);
+            if (cv->hidden < 32 || cv->hidden > 1024 || cv->hidden % 32)
+                return fail(AFQ_E_INVALID_ARGUMENT, "cv hidden=%d (multiple of 32, <= 1024)", cv->hidden);
+        }
+    }
     Arena a(workspace, workspace_bytes);
     BlockWS ws = layout_block(a, d, p->n_chunks);
     AFQ_TRY(check_ws(a, workspace_bytes));
@@ -788,12 +818,65 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
     // prop/blocks.py:53-57, with the energy's Green's function from the same pass
     if (is_mixed(d->precision))
         AFQ_TRY(launch_split_c(n * o, (const double2*)pb->mo_coeff, ws.step.csplit, s));
-    AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green, is_mixed(d->precision) ? ws.step.csplit : nullptr));
-    // prop/blocks.py:59-79
-    AFQ_TRY(energy_impl(pb, st, ws, s, true));
-    { AFQ_PHASE("block_measure", s);
-    AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
-                                 st->pop_control_ene_shift, block_energy, block_weight, s)); }
+    if (cvmode == AFQ_CV_OFF) {
+        AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green,
+                                       is_mixed(d->precision) ? ws.step.csplit : nullptr));
+        // prop/blocks.py:59-79
+        AFQ_TRY(energy_impl(pb, st, ws, s, true));
+        AFQ_PHASE("block_measure", s);
+        AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
+                                     st->pop_control_ene_shift, block_energy, block_weight, s));
+    } else {
+        const LowpDims L = lowp_dims(d);
+        Arena la((void*)pb->lowp, (size_t)-1);
+        const LowpBufs lb = layout_lowp(la, d);
+        double2* walk = (double2*)st->walkers;
+        { AFQ_PHASE("qr", s); AFQ_TRY(launch_cholqr2(W, n, o, walk, walk, nullptr, s)); }
+        // overlaps, the Green's function and its force-bias operand in one pass; the GEMM gives c_g
+        { AFQ_PHASE("green", s);
+          AFQ_TRY(launch_overlap_split(W, n, o, (const double2*)pb->mo_coeff, walk, (double2*)st->overlaps,
+                                       fb_split(d, ws.step), s, ws.green, ws.step.csplit)); }
+        { AFQ_PHASE("fb_gemm", s);
+          AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.step.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.step.fbm, G,
+                                          ws.step.status, s)); }
+        const bool est = cvmode == AFQ_CV_ESTIMATE;
+        { AFQ_PHASE("cv_features", s);
+          AFQ_TRY(launch_cv_features(W, n, o, G, pb->h0, ws.green, (const double2*)pb->rot_h1, ws.step.fbm, G,
+                                     (const double2*)st->overlaps, est ? cv->feat_shift : nullptr,
+                                     est ? cv->feat_scale : nullptr, est ? ws.cv_feat : cv->rec_features,
+                                     ws.cv_ebase, s)); }
+        if (!est) {  // exact measurement, and the training data
+            AFQ_TRY(energy_impl(pb, st, ws, s, true));
+            AFQ_TRY(launch_cv_record(W, exchange_chunks(G), (const double2*)ws.partial, cv->rec_exchange, s));
+            AFQ_PHASE("block_measure", s);
+            AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
+                                         st->pop_control_ene_shift, block_energy, block_weight, s));
+        } else {
+            { AFQ_PHASE("cv_network", s);
+              AFQ_TRY(launch_mlp_forward(W, AFQ_CV_FEATURES, cv->hidden, (const __nv_bfloat16*)cv->net, ws.cv_feat,
+                                         ws.cv_y, nullptr, s)); }
+            const int stride = cv->n_sample >= W ? 1 : W / cv->n_sample;
+            const int m_max = (W + stride - 1) / stride;
+            // the sample's offset: its own Philox stream (seed offset by a constant), this block's counter
+            AFQ_TRY(launch_philox(1, seed ^ 0x9E3779B97F4A7C15ull, counter + p->n_prop_steps, 0, ws.cv_u, s));
+            AFQ_TRY(launch_cv_pick(ws.cv_u, stride, ws.cv_off, s));
+            const int We = energy_chunk(d), nch = exchange_chunks(G);
+            AFQ_PHASE("energy", s);
+            for (int s0 = 0; s0 < m_max; s0 += We) {
+                const int sc = m_max - s0 < We ? m_max - s0 : We;
+                AFQ_TRY(launch_cv_green_rows(sc, s0, ws.cv_off, stride, W, n, o, ws.green, ws.Bg, L.S_E, L.Kt_E,
+                                             L.sec, s));
+                AFQ_TRY(launch_tc_gemm_tn_drain(2 * o * sc, G * o, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.F,
+                                                (long long)G * o, ws.step.status, s));
+                AFQ_TRY(launch_exchange_reduce(sc, G, o, ws.F, (long long)G * o,
+                                               (double2*)ws.partial + (size_t)s0 * nch * 2, s));
+            }
+            AFQ_TRY(launch_cv_measure(W, p->dt, p->shift_ema, st->weights, ws.cv_ebase, ws.cv_y, cv->y_shift,
+                                      cv->y_scale, m_max, stride, ws.cv_off, nch, (const double2*)ws.partial,
+                                      st->e_estimate, st->pop_control_ene_shift, block_energy, block_weight,
+                                      ws.energy, cv->stats, s));
+        }
+    }
     AFQ_PHASE("comb", s);
     // prop/blocks.py:81-92
     if (zeta < 0.0) {
@@ -810,6 +893,51 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st, c
     AFQ_TRY(launch_gather(W, 1, ws.idx, ws.ocopy, (double2*)st->overlaps, ws.avg, nullptr, s));
     if (sr_idx) AFQ_CUDA(cudaMemcpyAsync(sr_idx, ws.idx, sizeof(int32_t) * W, cudaMemcpyDeviceToDevice, s));
     return AFQ_OK;
+}
+
+// ---------------------------------------------------------------- network
+size_t afq_mlp_param_count(int32_t n_features, int32_t hidden) {
+    if (n_features < 1 || hidden < 32 || hidden > 1024 || hidden % 32) return 0;
+    return mlp_param_count(n_features, hidden);
+}
+
+int afq_mlp_forward(int32_t batch, int32_t n_features, int32_t hidden, const void* params_bf16, const float* x,
+                    float* y, void* stream) {
+    if (!afq_mlp_param_count(n_features, hidden)) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: F=%d H=%d", n_features, hidden);
+    if (batch < 0) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: batch %d < 0", batch);
+    if ((size_t)32 * (n_features + hidden) * sizeof(float) > 200 * 1024)
+        return fail(AFQ_E_UNSUPPORTED, "mlp: F + H = %d too large", n_features + hidden);
+    AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(x); AFQ_NOTNULL(y);
+    return launch_mlp_forward(batch, n_features, hidden, (const __nv_bfloat16*)params_bf16, x, y, nullptr,
+                              as_stream(stream));
+}
+
+size_t afq_mlp_train_workspace(int32_t batch, int32_t n_features, int32_t hidden) {
+    const size_t P = afq_mlp_param_count(n_features, hidden);
+    if (!P || batch < 1) return 0;
+    return ((size_t)6 * batch * hidden + batch + P + 1) * sizeof(float);
+}
+
+int afq_mlp_train_step(int32_t batch, int32_t n_features, int32_t hidden, float* master, void* params_bf16,
+                       float* adam_m, float* adam_v, const float* x, const float* target, float lr, int32_t step,
+                       void* workspace, size_t workspace_bytes, float* loss_out, void* stream) {
+    const size_t need = afq_mlp_train_workspace(batch, n_features, hidden);
+    if (!need) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: batch=%d F=%d H=%d", batch, n_features, hidden);
+    if (workspace_bytes < need) return fail(AFQ_E_WORKSPACE, "mlp workspace %zu < %zu bytes", workspace_bytes, need);
+    if (step < 1) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: step %d < 1", step);
+    if ((size_t)32 * (n_features + hidden) * sizeof(float) > 200 * 1024)
+        return fail(AFQ_E_UNSUPPORTED, "mlp: F + H = %d too large", n_features + hidden);
+    AFQ_NOTNULL(master); AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(adam_m); AFQ_NOTNULL(adam_v);
+    AFQ_NOTNULL(x); AFQ_NOTNULL(target); AFQ_NOTNULL(workspace);
+    return launch_mlp_train_step(batch, n_features, hidden, master, (__nv_bfloat16*)params_bf16, adam_m, adam_v, x,
+                                 target, lr, step, (float*)workspace, loss_out, as_stream(stream));
+}
+
+int afq_mlp_sync(int32_t n_features, int32_t hidden, const float* master, void* params_bf16, void* stream) {
+    const size_t P = afq_mlp_param_count(n_features, hidden);
+    if (!P) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: F=%d H=%d", n_features, hidden);
+    AFQ_NOTNULL(master); AFQ_NOTNULL(params_bf16);
+    return launch_mlp_sync_bf16(P, master, (__nv_bfloat16*)params_bf16, as_stream(stream));
 }
 
 }  // extern "C"

@@ -244,6 +244,24 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
                          SplitOut split, cudaStream_t s, double2* green_out = nullptr, const float2* cs = nullptr);
 int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
+// k_cv.cu, k_mlp.cu
+int launch_cv_features(int W, int n, int o, int G, double h0, const double2* green, const double2* rot_h1,
+                       const float* fbm, long long ldf, const double2* ovlp, const float* shift, const float* scale,
+                       float* feat, double* ebase, cudaStream_t s);
+int launch_cv_pick(const double* u, int stride, int* off, cudaStream_t s);
+int launch_cv_green_rows(int sc, int s0, const int* off, int stride, int W, int n, int o, const double2* green,
+                         __nv_bfloat16* dst, int S, int Kt, int sec, cudaStream_t s);
+int launch_cv_record(int W, int nchunk, const double2* partial, double* xout, cudaStream_t s);
+int launch_cv_measure(int W, double dt, double alpha, const double* weights, const double* ebase, const float* ynn,
+                      double y_shift, double y_scale, int m_max, int stride, const int* off, int nchunk,
+                      const double2* partial, const double* e_est, double* pop_shift, double* block_energy,
+                      double* block_weight, double2* energy, double* stats, cudaStream_t s);
+size_t mlp_param_count(int F, int H);
+int launch_mlp_forward(int B, int F, int H, const __nv_bfloat16* p, const float* x, float* y, float* act,
+                       cudaStream_t s);
+int launch_mlp_train_step(int B, int F, int H, float* w, __nv_bfloat16* wb, float* m, float* v, const float* x,
+                          const float* t, float lr, int step, float* ws, float* loss_out, cudaStream_t s);
+int launch_mlp_sync_bf16(size_t n, const float* w, __nv_bfloat16* wb, cudaStream_t s);
 // k_trotter_tc.cu
 bool trotter_tc_supported(int n, int o);
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,

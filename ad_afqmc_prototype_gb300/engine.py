@@ -382,8 +382,9 @@ def step(prob: Problem, params, st: DeviceState, seed: int, counter: int, fields
 
 
 def block(prob: Problem, params, st: DeviceState, seed: int, counter: int, fields=None, zeta=None,
-          return_idx: bool = False):
-    """One afqmc_block on `st`, in place.  Returns device (energy, weight[, idx])."""
+          return_idx: bool = False, cv=None):
+    """One afqmc_block on `st`, in place.  Returns device (energy, weight[, idx]).
+    cv: an `afq_cv` structure (the control-variate measurement), or None."""
     W = st.walkers.shape[0]
     if fields is not None:
         fields = as_device(fields, F64)
@@ -401,9 +402,49 @@ def block(prob: Problem, params, st: DeviceState, seed: int, counter: int, field
     z = -1.0 if zeta is None else float(zeta)
     if zeta is not None and not (0.0 <= z < 1.0):
         raise ValueError("zeta must be in [0, 1)")
-    _lib.call("afq_block", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), ptr(fields), z,
-              int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), ptr(e), ptr(wsum), ptr(idx), wsp, wsn,
-              stream_ptr())
+    if cv is None:
+        _lib.call("afq_block", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), ptr(fields), z,
+                  int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), ptr(e), ptr(wsum), ptr(idx), wsp, wsn,
+                  stream_ptr())
+    else:
+        _lib.call("afq_block_cv", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), ptr(fields), z,
+                  int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), ptr(e), ptr(wsum), ptr(idx),
+                  ctypes.byref(cv), wsp, wsn, stream_ptr())
     if return_idx:
         return e, wsum, idx.long()
     return e, wsum
+
+
+# ------------------------------------------------------------- the network
+def mlp_param_count(n_features: int, hidden: int) -> int:
+    n = int(_lib.load().afq_mlp_param_count(int(n_features), int(hidden)))
+    if n == 0:
+        raise ValueError(f"network shape F={n_features} H={hidden} (H a multiple of 32, <= 1024)")
+    return n
+
+
+def mlp_forward(params_bf16: torch.Tensor, x: torch.Tensor, hidden: int) -> torch.Tensor:
+    """y (B,) fp32 = network(x (B, F) fp32) with the bf16 parameters."""
+    x = x.to(torch.float32).contiguous()
+    B, F = x.shape
+    y = torch.empty((B,), dtype=torch.float32, device=x.device)
+    _lib.call("afq_mlp_forward", int(B), int(F), int(hidden), ptr(params_bf16), ptr(x), ptr(y), stream_ptr())
+    return y
+
+
+def mlp_sync(master: torch.Tensor, params_bf16: torch.Tensor, n_features: int, hidden: int):
+    _lib.call("afq_mlp_sync", int(n_features), int(hidden), ptr(master), ptr(params_bf16), stream_ptr())
+
+
+def mlp_train_step(master, params_bf16, m, v, x, target, lr: float, step: int, hidden: int, ws=None):
+    """One Adam step on a batch; returns (device loss (1,), workspace tensor)."""
+    x = x.to(torch.float32).contiguous()
+    target = target.to(torch.float32).contiguous()
+    B, F = x.shape
+    need = int(_lib.load().afq_mlp_train_workspace(int(B), int(F), int(hidden)))
+    if ws is None or ws.numel() * 4 < need:
+        ws = torch.empty((need + 3) // 4, dtype=torch.float32, device=x.device)
+    loss = torch.empty((1,), dtype=torch.float32, device=x.device)
+    _lib.call("afq_mlp_train_step", int(B), int(F), int(hidden), ptr(master), ptr(params_bf16), ptr(m), ptr(v),
+              ptr(x), ptr(target), float(lr), int(step), ptr(ws), ws.numel() * 4, ptr(loss), stream_ptr())
+    return loss, ws

@@ -23,9 +23,12 @@ class block_obs(NamedTuple):
 
 def afqmc_block(state: prop_state, *, sys: system, params: afqmc_params, ham_data: ham_chol, trial_data: Any,
                 meas_ops: meas_ops, prop_ops: chol_afqmc_ops, prop_ctx: chol_afqmc_ctx, meas_ctx: Any,
-                fields: Any = None, zeta: Any = None, inplace: bool = False) -> tuple[prop_state, block_obs]:
+                fields: Any = None, zeta: Any = None, inplace: bool = False,
+                cv: Any = None) -> tuple[prop_state, block_obs]:
     """propagation + measurement.  ``fields`` (n_prop_steps, W, G) and the comb
-    uniform ``zeta`` may be injected; otherwise both are drawn from the key."""
+    uniform ``zeta`` may be injected; otherwise both are drawn from the key.
+    ``cv`` (a ``prop.cv.ExchangeControlVariate``, mixed precisions only)
+    selects the control-variate measurement of the exchange energy."""
     nw = wk.n_walkers(state.walkers)
     seed, counter = int(state.rng_key[0]), int(state.rng_key[1])
     key = torch.tensor([seed, counter + params.n_prop_steps + 1], dtype=torch.int64)
@@ -37,11 +40,16 @@ def afqmc_block(state: prop_state, *, sys: system, params: afqmc_params, ham_dat
         prob = None
     if prob is not None:
         st = device_state(state, inplace)
-        e, wsum = engine.block(prob, params, st, seed, counter, fields=fields, zeta=zeta)
+        cvs = cv.block_args(nw) if cv is not None else None
+        e, wsum = engine.block(prob, params, st, seed, counter, fields=fields, zeta=zeta, cv=cvs)
+        if cv is not None:
+            cv.after_block()
         new = prop_state(walkers=st.walkers, weights=st.weights, overlaps=st.overlaps, rng_key=key,
                          pop_control_ene_shift=st.pop_shift.reshape(()), e_estimate=st.e_estimate.reshape(()))
         return new, block_obs(scalars={"energy": e.reshape(()), "weight": wsum.reshape(())})
 
+    if cv is not None:
+        raise ValueError("the control-variate measurement needs the engine's restricted RHF path")
     kw = dict(params=params, ham_data=ham_data, trial_data=trial_data, meas_ops=meas_ops, prop_ops=prop_ops,
               prop_ctx=prop_ctx, meas_ctx=meas_ctx)
     for s in range(params.n_prop_steps):

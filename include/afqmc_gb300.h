@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define AFQ_ABI_VERSION 1
+#define AFQ_ABI_VERSION 2
 
 #define AFQ_OK 0
 #define AFQ_E_INVALID_ARGUMENT (-1) /* bad shape, null pointer, bad value */
@@ -272,6 +272,69 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st,
               const double* fields, double zeta, uint64_t seed, uint64_t counter,
               double* block_energy, double* block_weight, int32_t* sr_idx,
               void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- learned exchange control variate (no counterpart in the reference:
+ * an engine form beside the plain measurement of prop/blocks.py:59-79) ----
+ *
+ * Per walker, features x (AFQ_CV_FEATURES floats) from the Coulomb vectors
+ * c_g = tr(L~_g G_half^T) of the block-end Green's function: [0, 60) sums of
+ * |c_g|^2 over 60 contiguous blocks of g, [60] Re sum_g c_g^2, [61] Im
+ * sum_g c_g^2, [62] Re tr(rot_h1 G_half), [63] log|overlap|.  A network
+ * (afq_mlp_*) predicts each walker's exchange energy X_w = sum_g tr(f_g f_g)
+ * from them.  Modes of afq_block_cv:
+ *   AFQ_CV_RECORD: the exact measurement, plus the raw features and the exact
+ *     X_w of every walker (training data);
+ *   AFQ_CV_ESTIMATE: X_w predicted for every walker, exact X_w for the walkers
+ *     off + k * stride (stride = W / n_sample, off uniform in [0, stride) from
+ *     the block's random stream), and the block energy
+ *       sum_w w h(E_pred) + stride * sum_sampled w (h(E_exact) - h(E_pred))
+ *     divided by sum_w w, h = the sqrt(2/dt) clip: unbiased for the exact
+ *     block energy whatever the network predicts (every walker is sampled
+ *     with probability 1 / stride).  Mixed precisions only. */
+#define AFQ_CV_OFF 0
+#define AFQ_CV_RECORD 1
+#define AFQ_CV_ESTIMATE 2
+#define AFQ_CV_FEATURES 64
+
+typedef struct afq_cv {
+    int32_t mode;            /* AFQ_CV_* */
+    int32_t hidden;          /* network width (multiple of 32, <= 1024) */
+    int32_t n_sample;        /* ESTIMATE: walkers with exact exchange per block (>= 1) */
+    int32_t pad_;
+    const void* net;         /* ESTIMATE: bf16 parameters, afq_mlp_param_count entries */
+    const float* feat_shift; /* ESTIMATE: network input = (x - shift) * scale, device (64,) */
+    const float* feat_scale;
+    double y_shift, y_scale; /* X_pred = y_shift + y_scale * network output */
+    float* rec_features;     /* RECORD: device (W, 64) raw features */
+    double* rec_exchange;    /* RECORD: device (W,) exact X_w */
+    double* stats;           /* ESTIMATE, optional device (4,): sum w h(E_pred), stride * correction,
+                                sum w, walkers sampled */
+} afq_cv;
+
+/* afq_block with the measurement chosen by cv (NULL or AFQ_CV_OFF: afq_block). */
+int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st,
+                 const double* fields, double zeta, uint64_t seed, uint64_t counter,
+                 double* block_energy, double* block_weight, int32_t* sr_idx, const afq_cv* cv,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* The network: F -> H -> H -> 1, GELU, bf16 weights, fp32 arithmetic.
+ * Parameters (bf16 copy and fp32 master, same layout): W1 (H x F), b1 (H),
+ * W2 (H x H), b2 (H), w3 (H), b3 (1). */
+size_t afq_mlp_param_count(int32_t n_features, int32_t hidden);
+/* y (B,) = network(x (B, F) fp32), all device. */
+int afq_mlp_forward(int32_t batch, int32_t n_features, int32_t hidden, const void* params_bf16,
+                    const float* x, float* y, void* stream);
+/* One Adam step (beta 0.9 / 0.999, bias-corrected by `step` >= 1) on the
+ * loss mean (y - target)^2 / 2 of a batch: updates master, its bf16 copy and
+ * the moments m, v.  loss_out (optional, device) receives the batch loss
+ * before the update.  workspace: afq_mlp_train_workspace bytes. */
+size_t afq_mlp_train_workspace(int32_t batch, int32_t n_features, int32_t hidden);
+int afq_mlp_train_step(int32_t batch, int32_t n_features, int32_t hidden, float* master, void* params_bf16,
+                       float* adam_m, float* adam_v, const float* x, const float* target, float lr,
+                       int32_t step, void* workspace, size_t workspace_bytes, float* loss_out,
+                       void* stream);
+/* bf16 copy of the fp32 master parameters. */
+int afq_mlp_sync(int32_t n_features, int32_t hidden, const float* master, void* params_bf16, void* stream);
 
 /* ---- tracing (no counterpart in the reference, which only times blocks
  * with time.perf_counter, driver.py:83-147) --------------------------------- */

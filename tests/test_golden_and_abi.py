@@ -56,7 +56,7 @@ def test_library_exports_every_declared_function(engine_lib):
 
 
 def test_abi_version_and_status_strings(engine_lib):
-    assert engine_lib.afq_abi_version() == 1
+    assert engine_lib.afq_abi_version() == 2
     assert engine_lib.afq_status_string(0) == b"ok"
     assert engine_lib.afq_status_string(-4) == b"workspace too small"
 
