@@ -14,6 +14,7 @@ walker-steps/s = n_walkers * 10 / (seconds per block), summed over ranks.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -47,6 +48,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison block")
+    ap.add_argument("--no-cv", action="store_true", help="skip the control-variate line")
     return ap.parse_args()
 
 
@@ -279,6 +281,10 @@ def run_ours(args, rank, world):
     if not args.no_e2e:
         e2e = run_e2e(args, env, afqmc_block, W)
 
+    cvline = None
+    if args.precision in SPLIT_SECTIONS and not args.no_cv:
+        cvline = run_cv(args, env, st, W, world, seed, ctr)
+
     out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else
@@ -292,12 +298,79 @@ def run_ours(args, rank, world):
            "roofline": roof, "tensor_kernels": tc,
            "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
            "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
+    if cvline:
+        out["control_variate"] = cvline
     if compare:
         out["plain_fp64"] = compare
         out["ratio_vs_plain_fp64"] = round(value / compare["value"], 2)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     return out
+
+
+def run_cv(args, env, st, W, world, seed, ctr):
+    """The mixed + control-variate form: five recorded blocks (50 steps) train
+    the exchange network with the engine's kernels (not timed), then
+    args.steps blocks are timed with exact exchange on 1/8 of the walkers.
+    Its noise against the exact measurement of the same state, and against
+    the same sample without the network, from zero-step blocks."""
+    import torch
+    from ad_afqmc_prototype_gb300 import engine
+    from ad_afqmc_prototype_gb300.prop.cv import ExchangeControlVariate
+
+    prob, params = env["prob"], env["params"]
+    cv = ExchangeControlVariate(hidden=256, sample_fraction=1 / 8, seed=seed)
+    cv.mode = "record"
+    for _ in range(5):
+        engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
+        cv.after_block()
+        ctr += STEPS_PER_BLOCK + 1
+    t0 = time.time()
+    losses = cv.fit(epochs=20, batch=1024, lr=1e-3)
+    torch.cuda.synchronize()
+    fit_s = time.time() - t0
+    cv.mode = "estimate"
+    for _ in range(args.warmup):
+        engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
+        cv.after_block()
+        ctr += STEPS_PER_BLOCK + 1
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
+        cv.after_block()
+        ctr += STEPS_PER_BLOCK + 1
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+
+    # noise of one block's estimate on a fixed state (zero-step blocks)
+    z = dataclasses.replace(params, n_prop_steps=0)
+
+    def clone():
+        return engine.DeviceState(*[t.clone() for t in (st.walkers, st.weights, st.overlaps, st.pop_shift,
+                                                          st.e_estimate)])
+    exact = float(engine.block(prob, z, clone(), seed, 0, zeta=0.5)[0])
+
+    def draws(shift, scale, k=16):
+        out = []
+        for j in range(k):
+            a = cv.block_args(W)
+            a.y_shift, a.y_scale = shift, scale
+            out.append(float(engine.block(prob, z, clone(), seed + 7919 * (j + 1), 0, zeta=0.5, cv=a)[0]))
+            cv.after_block()
+        return np.array(out)
+    net, alone = draws(cv.y_shift, cv.y_scale), draws(0.0, 0.0)
+    return {"value": round(world * W * STEPS_PER_BLOCK / (ms / 1000.0), 3), "unit": UNIT, "ms_per_step": round(ms, 3),
+            "exact_exchange_fraction": 1 / 8, "network": "64-256-256-1 GELU, bf16 weights, fp32 arithmetic",
+            "training": {"blocks": 5, "samples": 5 * W, "epochs": 20, "seconds": round(fit_s, 2),
+                         "loss_first": round(losses[0], 5), "loss_last": round(losses[-1], 5)},
+            "noise_std_ha": float(net.std(ddof=1)), "noise_std_sample_alone_ha": float(alone.std(ddof=1)),
+            "variance_ratio": float(net.var(ddof=1) / max(alone.var(ddof=1), 1e-300)),
+            "mean_minus_exact_ha": float(net.mean() - exact),
+            "measured": "noise: 16 estimates of one block-end state's energy (zero-step blocks, different samples)"}
 
 
 def compare_with_fp64(env, st_mixed, W):
