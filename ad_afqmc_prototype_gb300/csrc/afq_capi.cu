@@ -895,6 +895,83 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
     return AFQ_OK;
 }
 
+// ------------------------------------------------------------- block loop
+size_t afq_run_blocks_workspace(const afq_dims* d, int32_t n_chunks) {
+    const size_t b = afq_block_workspace(d, n_chunks);
+    return b ? round_up(b, 256) + 256 : 0;
+}
+
+int afq_run_blocks(const afq_problem* pb, const afq_params* p, const afq_state* st, int32_t n_blocks, uint64_t seed,
+                   uint64_t* counter_dev, double* energies, double* weights, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_problem(pb));
+    AFQ_TRY(check_params(p));
+    AFQ_TRY(check_state(st));
+    AFQ_NOTNULL(counter_dev); AFQ_NOTNULL(energies); AFQ_NOTNULL(weights); AFQ_NOTNULL(workspace);
+    if (n_blocks < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_blocks=%d < 0", n_blocks);
+    const size_t need = afq_run_blocks_workspace(&pb->dims, p->n_chunks);
+    if (!need || workspace_bytes < need)
+        return fail(AFQ_E_WORKSPACE, "run workspace %zu < %zu bytes", workspace_bytes, need);
+    const size_t bws = round_up(afq_block_workspace(&pb->dims, p->n_chunks), 256);
+    double* slot = (double*)((char*)workspace + bws);  // e, w
+    int* idx = (int*)(slot + 2);
+    cudaStream_t s = as_stream(stream);
+    if (n_blocks == 0) return AFQ_OK;
+    const uint64_t inc = (uint64_t)p->n_prop_steps + 1;
+    struct Base {  // the device counter for this thread's launches, reset on every exit
+        Base(const uint64_t* c) { t_counter_base = c; }
+        ~Base() { t_counter_base = nullptr; }
+    } base(counter_dev);
+    AFQ_CUDA(cudaMemsetAsync(idx, 0, sizeof(int), s));
+    auto one = [&](cudaStream_t q) -> int {
+        AFQ_TRY(afq_block_cv(pb, p, st, nullptr, -1.0, seed, 0, slot, slot + 1, nullptr, nullptr, workspace, bws,
+                             q));
+        return launch_run_record(slot, slot + 1, energies, weights, idx, counter_dev, inc, q);
+    };
+    // the first block runs as is (it also performs every one-time setup)
+    AFQ_TRY(one(s));
+    if (n_blocks == 1) return AFQ_OK;
+    if (timing_enabled()) {  // per-phase events do not belong in a graph: plain launches
+        for (int b = 1; b < n_blocks; ++b) AFQ_TRY(one(s));
+        return AFQ_OK;
+    }
+    // the remaining blocks: one block captured into a CUDA graph, replayed
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int rc = AFQ_OK;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming) != cudaSuccess)
+        rc = fail(AFQ_E_CUDA, "run_blocks: stream / event creation failed");
+    if (rc == AFQ_OK && (cudaEventRecord(ev0, s) != cudaSuccess || cudaStreamWaitEvent(cs, ev0, 0) != cudaSuccess))
+        rc = fail(AFQ_E_CUDA, "run_blocks: stream ordering failed");
+    if (rc == AFQ_OK) {
+        if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            rc = fail(AFQ_E_CUDA, "run_blocks: stream capture failed to start");
+        } else {
+            const int brc = one(cs);
+            const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+            if (brc != AFQ_OK) rc = brc;
+            else if (ec != cudaSuccess || !graph) rc = fail(AFQ_E_CUDA, "run_blocks: capture failed (%s)", cudaGetErrorString(ec));
+        }
+    }
+    if (rc == AFQ_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+        rc = fail(AFQ_E_CUDA, "run_blocks: graph instantiation failed");
+    for (int b = 1; rc == AFQ_OK && b < n_blocks; ++b)
+        if (cudaGraphLaunch(exec, cs) != cudaSuccess) rc = fail(AFQ_E_CUDA, "run_blocks: graph launch failed");
+    if (cs && ev1 && (cudaEventRecord(ev1, cs) != cudaSuccess || cudaStreamWaitEvent(s, ev1, 0) != cudaSuccess) &&
+        rc == AFQ_OK)
+        rc = fail(AFQ_E_CUDA, "run_blocks: stream ordering failed");
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (cs) cudaStreamDestroy(cs);  // destroyed once its work completes
+    return rc;
+}
+
 // ---------------------------------------------------------------- network
 size_t afq_mlp_param_count(int32_t n_features, int32_t hidden) {
     if (n_features < 1 || hidden < 32 || hidden > 1024 || hidden % 32) return 0;

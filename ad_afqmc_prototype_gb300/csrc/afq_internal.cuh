@@ -207,6 +207,12 @@ int launch_gather(int W, int64_t row, const int32_t* idx, const double2* src, do
 int launch_block_measure(int W, double dt, double shift_ema, const double* weights,
                          const double2* energy, const double* e_est, double* pop_shift,
                          double* block_energy, double* block_weight, cudaStream_t s);
+// While non-null (one thread's captured block loop), Philox counters are
+// offsets from *t_counter_base on the device.
+extern thread_local const uint64_t* t_counter_base;
+bool timing_enabled();
+int launch_run_record(const double* e, const double* w, double* es, double* ws, int* idx, uint64_t* counter,
+                      uint64_t inc, cudaStream_t s);
 int launch_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, double* out,
                   cudaStream_t s);
 size_t sr_levels_size(int W);

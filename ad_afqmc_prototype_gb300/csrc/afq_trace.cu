@@ -39,6 +39,8 @@ cudaEvent_t take_event() {
 }
 }  // namespace
 
+bool timing_enabled() { return g_timing; }
+
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 Phase::Phase(const char* n, cudaStream_t s) : name(n), stream(s), start(nullptr) {

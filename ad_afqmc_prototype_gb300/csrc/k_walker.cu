@@ -871,6 +871,25 @@ __global__ void __launch_bounds__(1024) k_block_measure(int W, double dt, double
     }
 }
 
+// Files one block's energy and weight at the run's next index and advances
+// the run's Philox counter (the tail of a captured block).
+__global__ void k_run_record(const double* __restrict__ e, const double* __restrict__ w, double* __restrict__ es,
+                             double* __restrict__ ws, int* __restrict__ idx, uint64_t* __restrict__ counter,
+                             uint64_t inc) {
+    const int b = idx[0];
+    es[b] = e[0];
+    ws[b] = w[0];
+    idx[0] = b + 1;
+    counter[0] += inc;
+}
+
+int launch_run_record(const double* e, const double* w, double* es, double* ws, int* idx, uint64_t* counter,
+                      uint64_t inc, cudaStream_t s) {
+    k_run_record<<<1, 1, 0, s>>>(e, w, es, ws, idx, counter, inc);
+    AFQ_LAUNCHED("k_run_record");
+    return AFQ_OK;
+}
+
 int launch_block_measure(int W, double dt, double shift_ema, const double* weights, const double2* energy,
                          const double* e_est, double* pop_shift, double* block_energy, double* block_weight,
                          cudaStream_t s) {
@@ -902,9 +921,11 @@ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
     return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
-__global__ void k_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, double* __restrict__ out) {
+__global__ void k_philox(int64_t count, uint64_t seed, uint64_t counter0, int normal, double* __restrict__ out,
+                         const uint64_t* __restrict__ cbase) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (2 * e >= count) return;
+    const uint64_t counter = counter0 + (cbase ? cbase[0] : 0ull);
     const uint4 r = philox10(make_uint4((uint32_t)e, (uint32_t)((uint64_t)e >> 32), (uint32_t)counter,
                                         (uint32_t)(counter >> 32)),
                              make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
@@ -921,10 +942,14 @@ __global__ void k_philox(int64_t count, uint64_t seed, uint64_t counter, int nor
     if (2 * e + 1 < count) out[2 * e + 1] = b;
 }
 
+// Counter base read on the device, set for the duration of a captured block
+// loop (afq_run_blocks) on the calling thread; null otherwise.
+thread_local const uint64_t* t_counter_base = nullptr;
+
 int launch_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, double* out, cudaStream_t s) {
     if (count <= 0) return AFQ_OK;
     int64_t pairs = (count + 1) / 2;
-    k_philox<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(count, seed, counter, normal, out);
+    k_philox<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(count, seed, counter, normal, out, t_counter_base);
     AFQ_LAUNCHED("k_philox");
     return AFQ_OK;
 }

@@ -415,6 +415,27 @@ def block(prob: Problem, params, st: DeviceState, seed: int, counter: int, field
     return e, wsum
 
 
+def run_blocks(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int, counter):
+    """n_blocks afqmc_blocks on `st` in place (driver.py:22-38), the block
+    loop replayed as a CUDA graph.  `counter`: device (1,) int64 Philox
+    counter, advanced by n_prop_steps + 1 per block.  Returns device
+    (energies (n_blocks,), weights (n_blocks,))."""
+    W = st.walkers.shape[0]
+    if counter.dtype != torch.int64 or counter.numel() != 1 or not counter.is_cuda:
+        raise ValueError("counter must be a device (1,) int64 tensor")
+    d = make_dims(W, prob.norb, prob.nocc, prob.nchol, prob.trial_is_real, prob.precision)
+    lib = _lib.load()
+    wsp, wsn = workspace(lib.afq_run_blocks_workspace(ctypes.byref(d), int(params.n_chunks)))
+    p = make_params(params)
+    pb = prob.c()
+    cs = st.c()
+    e = torch.empty((max(n_blocks, 1),), dtype=F64, device=st.walkers.device)
+    w = torch.empty_like(e)
+    _lib.call("afq_run_blocks", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), int(n_blocks),
+              int(seed) & (2**64 - 1), ptr(counter), ptr(e), ptr(w), wsp, wsn, stream_ptr())
+    return e[:n_blocks], w[:n_blocks]
+
+
 # ------------------------------------------------------------- the network
 def mlp_param_count(n_features: int, hidden: int) -> int:
     n = int(_lib.load().afq_mlp_param_count(int(n_features), int(hidden)))

@@ -273,6 +273,20 @@ int afq_block(const afq_problem* pb, const afq_params* p, const afq_state* st,
               double* block_energy, double* block_weight, int32_t* sr_idx,
               void* workspace, size_t workspace_bytes, void* stream);
 
+/* run_afqmc_energy's block loop (driver.py:22-38: a jitted scan of
+ * block_fn over n_blocks) on the device: n_blocks afqmc_blocks with fields
+ * and comb uniforms drawn from the Philox stream (seed, *counter_dev), the
+ * device counter advancing by n_prop_steps + 1 per block, and block b's
+ * energy and weight written to energies[b], weights[b] (device f64).  The
+ * first block runs as is; the others replay a CUDA graph of one captured
+ * block (plain launches while afq_timing is on).  The same stream as
+ * afq_block with counter = *counter_dev gives the same results.
+ * workspace: afq_run_blocks_workspace bytes. */
+size_t afq_run_blocks_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_run_blocks(const afq_problem* pb, const afq_params* p, const afq_state* st, int32_t n_blocks,
+                   uint64_t seed, uint64_t* counter_dev, double* energies, double* weights,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- learned exchange control variate (no counterpart in the reference:
  * an engine form beside the plain measurement of prop/blocks.py:59-79) ----
  *
