@@ -104,6 +104,12 @@ _SIGS = {
     "afq_run_blocks_workspace": (c_size_t, [POINTER(afq_dims), c_int32]),
     "afq_run_blocks": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), c_int32, c_uint64,
                                  P, P, P, P, c_size_t, P]),
+    "afq_grad_tape_bytes": (c_size_t, [POINTER(afq_dims), c_int32, c_int32]),
+    "afq_grad_workspace": (c_size_t, [POINTER(afq_dims), POINTER(afq_params), c_int32]),
+    "afq_grad_forward": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), c_int32, c_uint64,
+                                   c_uint64, c_int32, P, P, P, P, P, c_size_t, P, c_size_t, P]),
+    "afq_grad_backward": (c_int32, [POINTER(afq_problem), POINTER(afq_params), P, c_int32, c_uint64, c_uint64,
+                                    c_int32, P, c_size_t, P, P, P, P, c_size_t, P]),
     "afq_mlp_param_count": (c_size_t, [c_int32, c_int32]),
     "afq_mlp_forward": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P]),
     "afq_mlp_train_workspace": (c_size_t, [c_int32, c_int32, c_int32]),

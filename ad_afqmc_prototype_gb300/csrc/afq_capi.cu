@@ -528,7 +528,10 @@ int afq_workspace_status(void* workspace, int32_t* status, void* stream) {
     *status = v;
     if (v != 0) {
         AFQ_CUDA(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));
-        return fail(AFQ_E_DEVICE_CHECK, "a bounded device-side wait expired (status %d)", v);
+        return fail(AFQ_E_DEVICE_CHECK, "device-side check failed (status %d: %s)", v,
+                    v == AFQ_STATUS_WAIT_EXPIRED ? "a bounded wait expired"
+                    : v == AFQ_STATUS_SINGULAR   ? "singular matrix in an adjoint kernel"
+                                                 : "comb indices out of order or range");
     }
     return AFQ_OK;
 }
@@ -894,6 +897,77 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
     if (sr_idx) AFQ_CUDA(cudaMemcpyAsync(sr_idx, ws.idx, sizeof(int32_t) * W, cudaMemcpyDeviceToDevice, s));
     return AFQ_OK;
 }
+
+// -------------------------------------------------------- taped block
+}  // extern "C"
+
+namespace afq {
+
+int block_op_count(const afq_params* p) {
+    int q = 0;
+    if (p->qr_every > 0)
+        for (int s = 0; s + 1 < p->n_prop_steps; ++s)
+            if ((s + 1) % p->qr_every == 0) ++q;
+    return p->n_prop_steps + q + 2;
+}
+
+size_t block_ws_bytes(const afq_dims* d, int n_chunks) { return afq_block_workspace(d, n_chunks); }
+
+static int snap_state(const afq_dims* d, const afq_state* st, const BlockSnap* snap, int k, cudaStream_t s) {
+    if (!snap) return AFQ_OK;
+    const size_t W = d->n_walkers, no = (size_t)d->norb * d->nocc;
+    AFQ_CUDA(cudaMemcpyAsync(snap->walkers + k * W * no, st->walkers, sizeof(double2) * W * no,
+                             cudaMemcpyDeviceToDevice, s));
+    AFQ_CUDA(cudaMemcpyAsync(snap->weights + k * W, st->weights, sizeof(double) * W, cudaMemcpyDeviceToDevice, s));
+    AFQ_CUDA(cudaMemcpyAsync(snap->overlaps + k * W, st->overlaps, sizeof(double2) * W, cudaMemcpyDeviceToDevice,
+                             s));
+    AFQ_CUDA(cudaMemcpyAsync(snap->pop + k, st->pop_control_ene_shift, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return AFQ_OK;
+}
+
+// The binary64 path of afq_block (fields and comb uniform from the Philox
+// stream), with each operation's input state copied to snap.
+int run_block_taped(const afq_problem* pb, const afq_params* p, const afq_state* st, uint64_t seed, uint64_t counter,
+                    const int32_t* forced_idx, int32_t* idx_out, double* block_energy, double* block_weight,
+                    const BlockSnap* snap, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    if (is_mixed(d->precision)) return fail(AFQ_E_UNSUPPORTED, "the taped block runs the binary64 form");
+    Arena a(workspace, workspace_bytes);
+    BlockWS ws = layout_block(a, d, p->n_chunks);
+    AFQ_TRY(check_ws(a, workspace_bytes));
+    const int W = d->n_walkers, n = d->norb, o = d->nocc;
+    int op = 0;
+    for (int st_i = 0; st_i < p->n_prop_steps; ++st_i) {
+        AFQ_TRY(snap_state(d, st, snap, op++, s));
+        AFQ_TRY(step_impl(pb, p, st, nullptr, seed, counter + st_i, ws.step, s));
+        if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps) {
+            AFQ_TRY(snap_state(d, st, snap, op++, s));
+            AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));
+        }
+    }
+    AFQ_TRY(snap_state(d, st, snap, op++, s));
+    AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green, nullptr));
+    AFQ_TRY(snap_state(d, st, snap, op++, s));
+    AFQ_TRY(energy_impl(pb, st, ws, s, true));
+    if (snap)
+        AFQ_CUDA(cudaMemcpyAsync(snap->energy, ws.energy, sizeof(double2) * W, cudaMemcpyDeviceToDevice, s));
+    AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
+                                 st->pop_control_ene_shift, block_energy, block_weight, s));
+    AFQ_TRY(launch_philox(1, seed, counter + p->n_prop_steps, 0, ws.zeta, s));
+    AFQ_TRY(launch_sr_scan_dev(W, st->weights, ws.zeta, ws.levels, ws.idx, ws.avg, s));
+    if (forced_idx)
+        AFQ_CUDA(cudaMemcpyAsync(ws.idx, forced_idx, sizeof(int32_t) * W, cudaMemcpyDeviceToDevice, s));
+    AFQ_CUDA(cudaMemcpyAsync(ws.wcopy, st->walkers, sizeof(double2) * (size_t)W * n * o, cudaMemcpyDeviceToDevice, s));
+    AFQ_CUDA(cudaMemcpyAsync(ws.ocopy, st->overlaps, sizeof(double2) * (size_t)W, cudaMemcpyDeviceToDevice, s));
+    AFQ_TRY(launch_gather(W, (int64_t)n * o, ws.idx, ws.wcopy, (double2*)st->walkers, ws.avg, st->weights, s));
+    AFQ_TRY(launch_gather(W, 1, ws.idx, ws.ocopy, (double2*)st->overlaps, ws.avg, nullptr, s));
+    if (idx_out) AFQ_CUDA(cudaMemcpyAsync(idx_out, ws.idx, sizeof(int32_t) * W, cudaMemcpyDeviceToDevice, s));
+    return AFQ_OK;
+}
+
+}  // namespace afq
+
+extern "C" {
 
 // ------------------------------------------------------------- block loop
 size_t afq_run_blocks_workspace(const afq_dims* d, int32_t n_chunks) {

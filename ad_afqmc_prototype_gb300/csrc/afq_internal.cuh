@@ -77,6 +77,34 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
     }
 }
 
+// Importance factor of one walker (prop/afqmc.py:116-125): imp_ph =
+// |exp(exponent) ratio| cos(theta) before the floor and cap, and
+// phi = exp(-sqrt_dt shift_term) ratio whose angle is theta.  Shared by the
+// weight update and its adjoint so that both see the same floor/cap masks.
+struct WeightFactor {
+    double imp_ph;
+    double2 phi;
+};
+__device__ __forceinline__ WeightFactor weight_factor(double dt, double sqrt_dt, double ps, double2 h0_prop,
+                                                      double2 st, double2 ft, double2 on, double2 op) {
+    const double2 ratio = cdiv(on, op);
+    const double2 ex = make_double2(-sqrt_dt * st.x + ft.x + dt * (ps + h0_prop.x),
+                                    -sqrt_dt * st.y + ft.y + dt * h0_prop.y);
+    double sn, cs;
+    sincos(ex.y, &sn, &cs);
+    const double er = exp(ex.x);
+    const double2 imp = cmul(make_double2(er * cs, er * sn), ratio);
+    // theta = angle(exp(-sqrt_dt shift_term) * ratio)
+    sincos(-sqrt_dt * st.y, &sn, &cs);
+    const double er2 = exp(-sqrt_dt * st.x);
+    const double2 ph = cmul(make_double2(er2 * cs, er2 * sn), ratio);
+    const double theta = atan2(ph.y, ph.x);
+    WeightFactor f;
+    f.imp_ph = hypot(imp.x, imp.y) * cos(theta);
+    f.phi = ph;
+    return f;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -278,6 +306,61 @@ int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
 int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
                       cudaStream_t s);
+
+// k_adjoint.cu : reverse-mode kernels of the binary64 step and block
+int launch_taylor_tape(int W, int n, int o, int K, double sqrt_dt, const double* E, const double2* V,
+                       const double2* win, double2* terms, double2* w2, cudaStream_t s);
+int launch_taylor_adj(int W, int n, int o, int K, double sqrt_dt, const double* E, const double2* V,
+                      const double2* wbar_post, double2* tbar, double2* wbar_pre, cudaStream_t s);
+int launch_vbar(int W, int n, int o, int K, double sqrt_dt, const double2* tbar, const double2* terms, double2* vbar,
+                cudaStream_t s);
+int ebar_splits(int W);
+int launch_ebar(int W, int n, int o, const double2* X, long long xs, const double2* Y, long long ys, double* partial,
+                cudaStream_t s);
+int launch_sum_partials(int count, int ns, const double* partial, double* out, cudaStream_t s);
+int launch_green_adj(int W, int n, int o, const double2* mo, const double2* walkers, const double2* gbar,
+                     const double2* ov, const double2* ovbar, double2* wbar, int* err, cudaStream_t s);
+int launch_qr_adj(int W, int n, int o, const double2* A, const double2* Q, const double2* qbar, double2* abar,
+                  int* err, cudaStream_t s);
+int launch_weight_adj(int W, const afq_params* p, double sqrt_dt, double dt, double2 h0_prop,
+                      const double2* shift_term, const double2* fb_term, const double* w_pre, const double2* ov_pre,
+                      const double* p_pre, const double* w_post, const double2* ov_post, double* wbar,
+                      double2* ovbar, double* pbar, double2* ovn_tot, double* fbt_bar, double2* shift_bar,
+                      cudaStream_t s);
+int launch_fs_adj(int W, int G, double sqrt_dt, const double* x, const double2* fb, const double2* mf,
+                  const double* fbt_bar, const double2* shift_bar, double2* xtb, cudaStream_t s);
+int launch_measure_adj(int W, double dt, double alpha, const double* weights, const double2* energy,
+                       const double* e_est, const double* e_block, const double* eb_bar, const double* wb_bar,
+                       double* pbar, double* wbar, double* ebar_w, cudaStream_t s);
+int launch_energy_gbar(int W, int on, const double* ebar_w, const double2* rot_h1, const double2* cl,
+                       const double2* y, double2* gbar, cudaStream_t s);
+int launch_sg_accum(int W, int on, const double* ebar_w, const double2* g, double2* sg, cudaStream_t s);
+int launch_block_transpose(int wc, int o, int G, const double2* F, double2* Ft, cudaStream_t s);
+int launch_sr_adj(int W, int no, const int32_t* idx, const double2* wk_in, const double2* ob_in, const double* wb_in,
+                  const double* weights, double* wsum, double2* wk_out, double2* ob_out, double* wb_out, int* err,
+                  cudaStream_t s);
+int launch_h1bar(int n, int o, double dt, const double* h1_eff, const double* ebar, const double2* mo,
+                 const double2* sg, double* h1bar, double* tmp, cudaStream_t s);
+
+// afq_capi.cu : one binary64 block with the inputs of each operation saved.
+// Operations of a block, in order: n_prop_steps steps with a QR after every
+// qr_every-th one that is not the last, the block-end QR and overlap
+// refresh, the measurement.  Snapshot slot k holds the input state of
+// operation k; slot n_ops - 1 (the measurement) is the state after the QR.
+struct BlockSnap {
+    double2* walkers = nullptr;   // n_ops x W n o
+    double* weights = nullptr;    // n_ops x W
+    double2* overlaps = nullptr;  // n_ops x W
+    double* pop = nullptr;        // n_ops
+    double2* energy = nullptr;    // W local energies of the measurement
+};
+int block_op_count(const afq_params* p);
+size_t block_ws_bytes(const afq_dims* d, int n_chunks);
+// forced_idx (optional): comb indices used instead of the comb's own.
+int run_block_taped(const afq_problem* pb, const afq_params* p, const afq_state* st, uint64_t seed,
+                    uint64_t counter, const int32_t* forced_idx, int32_t* idx_out, double* block_energy,
+                    double* block_weight, const BlockSnap* snap, void* workspace, size_t workspace_bytes,
+                    cudaStream_t s);
 
 inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 

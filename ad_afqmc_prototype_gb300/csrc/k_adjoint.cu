@@ -1,0 +1,864 @@
+// Adjoint (reverse-mode) kernels of the binary64 step and block, for the
+// differentiated energy dL/dh1 of a run of blocks (afq_grad_backward).
+//
+// Conventions: for a real loss L and a complex quantity z the adjoint is
+// zb = dL/dRe z + i dL/dIm z; a linear map z = A u pulls back as ub = A^H zb.
+// The forward arithmetic they differentiate:
+//   step   prop/afqmc.py:74-147   (force bias, field shifts, Trotter, weights)
+//   Taylor prop/utils.py:20-31    t_0 = E W, t_k = (i sqrt_dt / k) V t_{k-1}
+//   green  meas/rhf.py:15-24      G_half = (W m^-1)^T, ov = det(m)^2, m = C^H W
+//   energy meas/rhf.py:36-50
+//   QR     walkers.py:169-211     phase-fixed reduced QR, Q kept
+//   comb   walkers.py:243-265     gather by sorted indices, weights sum|w|/N
+#include "afq_internal.cuh"
+
+namespace afq {
+
+namespace {
+template <class K>
+int allow_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024)
+        AFQ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return AFQ_OK;
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ void set_err(int* err, int code) {
+    if (err) atomicCAS(err, 0, code);
+}
+}  // namespace
+
+// =====================================================================
+// Taylor series with its terms kept: t_0 = E W, t_k = (a/k) V t_{k-1},
+// W2 = sum_{k<=K} t_k, a = i sqrt_dt.  One CTA per walker; the current and
+// next term in shared memory.  terms (W, K, n, o): t_0 .. t_{K-1}.
+// =====================================================================
+__global__ void __launch_bounds__(256) k_taylor_tape(int n, int o, int K, double sqrt_dt, const double* __restrict__ E,
+                                                     const double2* __restrict__ V, const double2* __restrict__ win,
+                                                     double2* __restrict__ terms, double2* __restrict__ w2) {
+    extern __shared__ double2 sm2[];
+    const int w = blockIdx.x, no = n * o;
+    double2* cur = sm2;
+    double2* nxt = sm2 + no;
+    const double2* Ww = win + (size_t)w * no;
+    const double2* Vw = V + (size_t)w * n * n;
+    double2* Tw = terms + (size_t)w * K * no;
+    double2* S = w2 + (size_t)w * no;
+    for (int e = threadIdx.x; e < no; e += blockDim.x) nxt[e] = Ww[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < no; e += blockDim.x) {
+        const int i = e / o, a = e - i * o;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = 0; j < n; ++j) rfma(acc, E[(size_t)i * n + j], nxt[j * o + a]);
+        cur[e] = acc;
+        S[e] = acc;
+        if (K > 0) Tw[e] = acc;
+    }
+    __syncthreads();
+    for (int k = 1; k <= K; ++k) {
+        const double c = sqrt_dt / k;  // a/k = i c
+        for (int e = threadIdx.x; e < no; e += blockDim.x) {
+            const int i = e / o, a = e - i * o;
+            double2 acc = make_double2(0.0, 0.0);
+            const double2* vr = Vw + (size_t)i * n;
+            for (int j = 0; j < n; ++j) cfma(acc, vr[j], cur[j * o + a]);
+            const double2 t = make_double2(-c * acc.y, c * acc.x);
+            nxt[e] = t;
+            S[e] = cadd(S[e], t);
+            if (k < K) Tw[(size_t)k * no + e] = t;
+        }
+        __syncthreads();
+        double2* tmp = cur; cur = nxt; nxt = tmp;
+    }
+}
+
+int launch_taylor_tape(int W, int n, int o, int K, double sqrt_dt, const double* E, const double2* V,
+                       const double2* win, double2* terms, double2* w2, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    const size_t smem = 2 * sizeof(double2) * (size_t)n * o;
+    AFQ_TRY(allow_smem(k_taylor_tape, smem));
+    k_taylor_tape<<<W, 256, smem, s>>>(n, o, K, sqrt_dt, E, V, win, terms, w2);
+    AFQ_LAUNCHED("k_taylor_tape");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Reverse of the Taylor series and of the two E_half products:
+//   W2b = E^T W'b;  tb_K = W2b;  tb_k = W2b + conj(a/(k+1)) V^H tb_{k+1};
+//   Wb = E^T tb_0.
+// tbar (W, K+1, n, o) receives tb_0 .. tb_K; wbar_pre may alias wbar_post
+// (W'b is staged in shared memory before the first write).
+// =====================================================================
+__global__ void __launch_bounds__(256) k_taylor_adj(int n, int o, int K, double sqrt_dt, const double* __restrict__ E,
+                                                    const double2* __restrict__ V, const double2* wbar_post,
+                                                    double2* __restrict__ tbar, double2* wbar_pre) {
+    extern __shared__ double2 sm2[];
+    const int w = blockIdx.x, no = n * o;
+    double2* cur = sm2;
+    double2* nxt = sm2 + no;
+    const double2* Vw = V + (size_t)w * n * n;
+    double2* Tb = tbar + (size_t)w * (K + 1) * no;
+    for (int e = threadIdx.x; e < no; e += blockDim.x) nxt[e] = wbar_post[(size_t)w * no + e];
+    __syncthreads();
+    // W2b = E^T W'b
+    for (int e = threadIdx.x; e < no; e += blockDim.x) {
+        const int i = e / o, a = e - i * o;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = 0; j < n; ++j) rfma(acc, E[(size_t)j * n + i], nxt[j * o + a]);
+        cur[e] = acc;
+        Tb[(size_t)K * no + e] = acc;
+    }
+    __syncthreads();
+    for (int k = K - 1; k >= 0; --k) {
+        const double c = sqrt_dt / (k + 1);  // conj(a/(k+1)) = -i c
+        for (int e = threadIdx.x; e < no; e += blockDim.x) {
+            const int i = e / o, a = e - i * o;
+            double2 acc = make_double2(0.0, 0.0);
+            for (int j = 0; j < n; ++j) {
+                const double2 v = Vw[(size_t)j * n + i];
+                cfma(acc, cconj(v), cur[j * o + a]);
+            }
+            const double2 base = Tb[(size_t)K * no + e];
+            const double2 t = make_double2(base.x + c * acc.y, base.y - c * acc.x);
+            nxt[e] = t;
+            Tb[(size_t)k * no + e] = t;
+        }
+        __syncthreads();
+        double2* tmp = cur; cur = nxt; nxt = tmp;
+    }
+    // Wb = E^T tb_0
+    for (int e = threadIdx.x; e < no; e += blockDim.x) {
+        const int i = e / o, a = e - i * o;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = 0; j < n; ++j) rfma(acc, E[(size_t)j * n + i], cur[j * o + a]);
+        wbar_pre[(size_t)w * no + e] = acc;
+    }
+}
+
+int launch_taylor_adj(int W, int n, int o, int K, double sqrt_dt, const double* E, const double2* V,
+                      const double2* wbar_post, double2* tbar, double2* wbar_pre, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    const size_t smem = 2 * sizeof(double2) * (size_t)n * o;
+    AFQ_TRY(allow_smem(k_taylor_adj, smem));
+    k_taylor_adj<<<W, 256, smem, s>>>(n, o, K, sqrt_dt, E, V, wbar_post, tbar, wbar_pre);
+    AFQ_LAUNCHED("k_taylor_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Sums of outer products over (batch, column): 32 x 32 output tiles, 256
+// threads with 2 x 2 outputs each, 16 columns staged at a time.
+//   k_vbar:  Vb_w = sum_{k=1..K} conj(a/k) tb_k tb_{k-1}^H   (one walker per grid.z)
+//   k_ebar:  Eb[split] += Re sum_{w in split} X_w Y_w^H       (real, per split)
+// =====================================================================
+constexpr int OT = 32, OC = 16;
+
+__global__ void __launch_bounds__(256) k_vbar(int n, int o, int K, double sqrt_dt, const double2* __restrict__ tbar,
+                                              const double2* __restrict__ terms, double2* __restrict__ vbar) {
+    __shared__ double2 As[OC][OT + 1], Bs[OC][OT + 1];
+    const int w = blockIdx.z, no = n * o;
+    const int i0 = blockIdx.y * OT, j0 = blockIdx.x * OT;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double2 acc[2][2] = {};
+    for (int k = 1; k <= K; ++k) {
+        const double2* X = tbar + ((size_t)w * (K + 1) + k) * no;
+        const double2* Y = terms + ((size_t)w * K + (k - 1)) * no;
+        const double c = sqrt_dt / k;  // conj(a/k) = -i c
+        for (int a0 = 0; a0 < o; a0 += OC) {
+            for (int e = threadIdx.x; e < OC * OT; e += 256) {
+                const int r = e / OC, cc = e - r * OC;
+                const int i = i0 + r, j = j0 + r, a = a0 + cc;
+                double2 x = (i < n && a < o) ? X[i * o + a] : make_double2(0.0, 0.0);
+                As[cc][r] = make_double2(c * x.y, -c * x.x);
+                Bs[cc][r] = (j < n && a < o) ? cconj(Y[j * o + a]) : make_double2(0.0, 0.0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int cc = 0; cc < OC; ++cc) {
+                const double2 a_0 = As[cc][ty], a_1 = As[cc][ty + 16];
+                const double2 b_0 = Bs[cc][tx], b_1 = Bs[cc][tx + 16];
+                cfma(acc[0][0], a_0, b_0); cfma(acc[0][1], a_0, b_1);
+                cfma(acc[1][0], a_1, b_0); cfma(acc[1][1], a_1, b_1);
+            }
+            __syncthreads();
+        }
+    }
+    double2* Vb = vbar + (size_t)w * n * n;
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c2 = 0; c2 < 2; ++c2) {
+            const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c2;
+            if (i < n && j < n) Vb[(size_t)i * n + j] = acc[r][c2];
+        }
+}
+
+int launch_vbar(int W, int n, int o, int K, double sqrt_dt, const double2* tbar, const double2* terms, double2* vbar,
+                cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    dim3 grid((n + OT - 1) / OT, (n + OT - 1) / OT, W);
+    if (W > 65535) return fail(AFQ_E_UNSUPPORTED, "vbar: W=%d > 65535", W);
+    k_vbar<<<grid, 256, 0, s>>>(n, o, K, sqrt_dt, tbar, terms, vbar);
+    AFQ_LAUNCHED("k_vbar");
+    return AFQ_OK;
+}
+
+// X_w at X + w xs, Y_w at Y + w ys (each n x o); walkers [split*per, ...).
+__global__ void __launch_bounds__(256) k_ebar(int W, int n, int o, int per, const double2* __restrict__ X,
+                                              long long xs, const double2* __restrict__ Y, long long ys,
+                                              double* __restrict__ partial) {
+    __shared__ double2 As[OC][OT + 1], Bs[OC][OT + 1];
+    const int i0 = blockIdx.y * OT, j0 = blockIdx.x * OT;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int wa = blockIdx.z * per, wb = min(W, wa + per);
+    double acc[2][2] = {};
+    for (int w = wa; w < wb; ++w) {
+        const double2* Xw = X + (size_t)w * xs;
+        const double2* Yw = Y + (size_t)w * ys;
+        for (int a0 = 0; a0 < o; a0 += OC) {
+            for (int e = threadIdx.x; e < OC * OT; e += 256) {
+                const int r = e / OC, cc = e - r * OC;
+                const int i = i0 + r, j = j0 + r, a = a0 + cc;
+                As[cc][r] = (i < n && a < o) ? Xw[i * o + a] : make_double2(0.0, 0.0);
+                Bs[cc][r] = (j < n && a < o) ? Yw[j * o + a] : make_double2(0.0, 0.0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int cc = 0; cc < OC; ++cc) {
+                const double2 a_0 = As[cc][ty], a_1 = As[cc][ty + 16];
+                const double2 b_0 = Bs[cc][tx], b_1 = Bs[cc][tx + 16];
+                // Re(x conj(y)) = x.x y.x + x.y y.y
+                acc[0][0] = fma(a_0.x, b_0.x, fma(a_0.y, b_0.y, acc[0][0]));
+                acc[0][1] = fma(a_0.x, b_1.x, fma(a_0.y, b_1.y, acc[0][1]));
+                acc[1][0] = fma(a_1.x, b_0.x, fma(a_1.y, b_0.y, acc[1][0]));
+                acc[1][1] = fma(a_1.x, b_1.x, fma(a_1.y, b_1.y, acc[1][1]));
+            }
+            __syncthreads();
+        }
+    }
+    double* P = partial + (size_t)blockIdx.z * n * n;
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c2 = 0; c2 < 2; ++c2) {
+            const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c2;
+            if (i < n && j < n) P[(size_t)i * n + j] += acc[r][c2];
+        }
+}
+
+int ebar_splits(int W) { return W < 128 ? W : 128; }
+
+int launch_ebar(int W, int n, int o, const double2* X, long long xs, const double2* Y, long long ys, double* partial,
+                cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    const int ns = ebar_splits(W), per = (W + ns - 1) / ns;
+    dim3 grid((n + OT - 1) / OT, (n + OT - 1) / OT, ns);
+    k_ebar<<<grid, 256, 0, s>>>(W, n, o, per, X, xs, Y, ys, partial);
+    AFQ_LAUNCHED("k_ebar");
+    return AFQ_OK;
+}
+
+// out[i] = sum_s partial[s][i] (+ out[i] if accumulate), fixed order.
+__global__ void k_sum_partials(int count, int ns, const double* __restrict__ partial, double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    double v = 0.0;
+    for (int s = 0; s < ns; ++s) v += partial[(size_t)s * count + e];
+    out[e] = v;
+}
+
+int launch_sum_partials(int count, int ns, const double* partial, double* out, cudaStream_t s) {
+    k_sum_partials<<<(count + 255) / 256, 256, 0, s>>>(count, ns, partial, out);
+    AFQ_LAUNCHED("k_sum_partials");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Per-walker o x o algebra shared by the Green's-function and QR adjoints.
+// =====================================================================
+// Gauss-Jordan inverse with partial pivoting of the o x o matrix in aug
+// (row stride 2o, left half), result in the right half.  Returns false if a
+// pivot is zero.
+__device__ bool gj_inverse(int o, double2* aug) {
+    const int ld = 2 * o;
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const int r = e / o, c = e - r * o;
+        aug[r * ld + o + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+    }
+    __shared__ int piv;
+    __shared__ bool bad;
+    if (threadIdx.x == 0) bad = false;
+    __syncthreads();
+    for (int k = 0; k < o; ++k) {
+        if (threadIdx.x == 0) {
+            int best = k;
+            double bv = cabs2(aug[k * ld + k]);
+            for (int r = k + 1; r < o; ++r) {
+                const double v = cabs2(aug[r * ld + k]);
+                if (v > bv) { bv = v; best = r; }
+            }
+            piv = best;
+            if (!(bv > 0.0)) bad = true;
+        }
+        __syncthreads();
+        if (bad) return false;
+        if (piv != k)
+            for (int c = threadIdx.x; c < ld; c += blockDim.x) {
+                const double2 t = aug[k * ld + c];
+                aug[k * ld + c] = aug[piv * ld + c];
+                aug[piv * ld + c] = t;
+            }
+        __syncthreads();
+        const double2 inv = cdiv(make_double2(1.0, 0.0), aug[k * ld + k]);
+        __syncthreads();
+        for (int c = threadIdx.x; c < ld; c += blockDim.x) aug[k * ld + c] = cmul(aug[k * ld + c], inv);
+        __syncthreads();
+        for (int e = threadIdx.x; e < o * ld; e += blockDim.x) {
+            const int r = e / ld, c = e - r * ld;
+            if (r == k) continue;
+            const double2 f = aug[r * ld + k];
+            if (c == k) continue;
+            aug[r * ld + c] = csub(aug[r * ld + c], cmul(f, aug[k * ld + c]));
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < o; r += blockDim.x)
+            if (r != k) aug[r * ld + k] = make_double2(0.0, 0.0);
+        __syncthreads();
+    }
+    return true;
+}
+
+// out[i, b] (+)= sum_c (X[i, c] + sum_d Y[i, d] P[d, c]) conj(N[b, c]),
+// i < n, rows staged RT at a time.  X[i, c] = XT ? X[c * n + i] : X[i * o + c].
+constexpr int RT = 32;
+template <bool XT>
+__device__ void rows_phase(int n, int o, const double2* X, const double2* Y, const double2* P, int ldp,
+                           const double2* N, int ldn, double2* out, bool accumulate, double2* zt) {
+    for (int i0 = 0; i0 < n; i0 += RT) {
+        const int rows = min(RT, n - i0);
+        for (int e = threadIdx.x; e < rows * o; e += blockDim.x) {
+            const int r = e / o, c = e - r * o, i = i0 + r;
+            double2 z = X ? (XT ? X[(size_t)c * n + i] : X[(size_t)i * o + c]) : make_double2(0.0, 0.0);
+            for (int d = 0; d < o; ++d) cfma(z, Y[(size_t)i * o + d], P[d * ldp + c]);
+            zt[r * o + c] = z;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < rows * o; e += blockDim.x) {
+            const int r = e / o, b = e - r * o, i = i0 + r;
+            double2 acc = make_double2(0.0, 0.0);
+            for (int c = 0; c < o; ++c) cfma(acc, zt[r * o + c], cconj(N[b * ldn + c]));
+            if (accumulate) out[(size_t)i * o + b] = cadd(out[(size_t)i * o + b], acc);
+            else out[(size_t)i * o + b] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// =====================================================================
+// Adjoint of G_half and of the overlap at walkers W (one CTA per walker):
+//   Wb += [Gb^T + C (kappa I - conj(G) Gb^T)] m^-H,  kappa = 2 conj(ov) ovb,
+// with conj(G) Gb^T = m^-H (W^H Gb^T).  gbar (W, o, n) and (ov, ovbar) may
+// be null.  A singular m sets *err = AFQ_STATUS_SINGULAR and leaves Wb as is.
+// =====================================================================
+__global__ void __launch_bounds__(256) k_green_adj(int n, int o, const double2* __restrict__ mo,
+                                                   const double2* __restrict__ walkers,
+                                                   const double2* __restrict__ gbar, const double2* __restrict__ ov,
+                                                   const double2* __restrict__ ovbar, double2* __restrict__ wbar,
+                                                   int* err) {
+    extern __shared__ double2 sm2[];
+    double2* aug = sm2;               // o x 2o
+    double2* T = aug + 2 * o * o;     // o x o
+    double2* P = T + o * o;           // o x o
+    double2* zt = P + o * o;          // RT x o
+    const int w = blockIdx.x, no = n * o;
+    const double2* Ww = walkers + (size_t)w * no;
+    const double2* Gb = gbar ? gbar + (size_t)w * no : nullptr;
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const int a = e / o, b = e - a * o;
+        double2 m = make_double2(0.0, 0.0), t = make_double2(0.0, 0.0);
+        for (int i = 0; i < n; ++i) {
+            cfma(m, cconj(mo[(size_t)i * o + a]), Ww[(size_t)i * o + b]);
+            if (Gb) cfma(t, cconj(Ww[(size_t)i * o + a]), Gb[(size_t)b * n + i]);
+        }
+        aug[a * 2 * o + b] = m;
+        T[a * o + b] = t;  // T[c, b] = sum_j conj(W[j, c]) Gb[b, j]
+    }
+    __syncthreads();
+    if (!gj_inverse(o, aug)) {
+        if (threadIdx.x == 0) set_err(err, AFQ_STATUS_SINGULAR);
+        return;
+    }
+    const double2* mi = aug + o;  // minv[r, c] at mi[r * 2o + c]
+    double2 kappa = make_double2(0.0, 0.0);
+    if (ov && ovbar) {
+        const double2 v = ov[w], vb = ovbar[w];
+        kappa = cscale(cmulc(v, vb), 2.0);
+    }
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const int a = e / o, b = e - a * o;
+        double2 p = (a == b) ? kappa : make_double2(0.0, 0.0);
+        for (int c = 0; c < o; ++c) p = csub(p, cmulc(mi[c * 2 * o + a], T[c * o + b]));
+        P[a * o + b] = p;
+    }
+    __syncthreads();
+    rows_phase<true>(n, o, Gb, mo, P, o, mi, 2 * o, wbar + (size_t)w * no, true, zt);
+}
+
+int launch_green_adj(int W, int n, int o, const double2* mo, const double2* walkers, const double2* gbar,
+                     const double2* ov, const double2* ovbar, double2* wbar, int* err, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    if (o > 32) return fail(AFQ_E_UNSUPPORTED, "green adjoint: nocc=%d > 32", o);
+    const size_t smem = sizeof(double2) * ((size_t)4 * o * o + (size_t)RT * o);
+    AFQ_TRY(allow_smem(k_green_adj, smem));
+    k_green_adj<<<W, 256, smem, s>>>(n, o, mo, walkers, gbar, ov, ovbar, wbar, err);
+    AFQ_LAUNCHED("k_green_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Adjoint of the phase-fixed reduced QR, Q only (one CTA per walker):
+//   Ab = [Qb + Q (Kb - B)] R^-H,  B = Q^H Qb,  S = B - B^H,
+//   Kb = tril(S, -1) + diag(S) / 2,  R = Q^H A (upper triangle).
+// qbar and abar may alias.
+// =====================================================================
+__global__ void __launch_bounds__(256) k_qr_adj(int n, int o, const double2* __restrict__ A,
+                                                const double2* __restrict__ Q, const double2* qbar, double2* abar,
+                                                int* err) {
+    extern __shared__ double2 sm2[];
+    double2* R = sm2;            // o x o
+    double2* Ri = R + o * o;     // o x o  (R^-1)
+    double2* B = Ri + o * o;     // o x o
+    double2* M = B + o * o;      // o x o
+    double2* zt = M + o * o;     // RT x o
+    const int w = blockIdx.x, no = n * o;
+    const double2* Aw = A + (size_t)w * no;
+    const double2* Qw = Q + (size_t)w * no;
+    const double2* Qb = qbar + (size_t)w * no;
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const int a = e / o, b = e - a * o;
+        double2 r = make_double2(0.0, 0.0), bb = make_double2(0.0, 0.0);
+        for (int i = 0; i < n; ++i) {
+            const double2 q = cconj(Qw[(size_t)i * o + a]);
+            if (a <= b) cfma(r, q, Aw[(size_t)i * o + b]);
+            cfma(bb, q, Qb[(size_t)i * o + b]);
+        }
+        R[a * o + b] = r;
+        B[a * o + b] = bb;
+        Ri[a * o + b] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    // R^-1 by back substitution, one thread per column
+    for (int b = threadIdx.x; b < o; b += blockDim.x) {
+        if (!(cabs2(R[b * o + b]) > 0.0)) { set_err(err, AFQ_STATUS_SINGULAR); continue; }
+        Ri[b * o + b] = cdiv(make_double2(1.0, 0.0), R[b * o + b]);
+        for (int a = b - 1; a >= 0; --a) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int c = a + 1; c <= b; ++c) cfma(s, R[a * o + c], Ri[c * o + b]);
+            Ri[a * o + b] = cdiv(make_double2(-s.x, -s.y), R[a * o + a]);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
+        const int a = e / o, b = e - a * o;
+        double2 kb = make_double2(0.0, 0.0);
+        if (a > b) kb = csub(B[a * o + b], cconj(B[b * o + a]));
+        else if (a == b) kb = make_double2(0.0, B[a * o + a].y);  // (B - B^H)_aa / 2 = i Im B_aa
+        M[a * o + b] = csub(kb, B[a * o + b]);
+    }
+    __syncthreads();
+    rows_phase<false>(n, o, Qb, Qw, M, o, Ri, o, abar + (size_t)w * no, false, zt);
+}
+
+int launch_qr_adj(int W, int n, int o, const double2* A, const double2* Q, const double2* qbar, double2* abar,
+                  int* err, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    if (o > 32) return fail(AFQ_E_UNSUPPORTED, "QR adjoint: nocc=%d > 32", o);
+    const size_t smem = sizeof(double2) * ((size_t)4 * o * o + (size_t)RT * o);
+    AFQ_TRY(allow_smem(k_qr_adj, smem));
+    k_qr_adj<<<W, 256, smem, s>>>(n, o, A, Q, qbar, abar, err);
+    AFQ_LAUNCHED("k_qr_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Adjoint of the weight update and population shift of one step (one CTA).
+// imp_ph is recomputed with the forward's arithmetic (weight_factor), so the
+// floor / cap masks are the forward's.  In: wbar (W'b), ovbar (ov'b), pbar
+// (p'b); out in place: wbar (wb), ovbar (ovb), pbar (pb); per walker:
+// ovn_tot (total ov'b), fbt_bar (adjoint of Re fb_term), shift_bar.
+//   imp_ph = rfac Re(phi),  rfac = exp(Re fb_term + dt (p + Re h0p)),
+//   phi = exp(-sqrt_dt shift_term) ov' / ov.
+// =====================================================================
+__global__ void __launch_bounds__(1024) k_weight_adj(
+    int W, double dt, double sqrt_dt, double damping, double w_floor, double w_cap, double2 h0_prop,
+    const double2* __restrict__ shift_term, const double2* __restrict__ fb_term, const double* __restrict__ w_pre,
+    const double2* __restrict__ ov_pre, const double* __restrict__ p_pre, const double* __restrict__ w_post,
+    const double2* __restrict__ ov_post, double* wbar, double2* ovbar, double* pbar, double2* __restrict__ ovn_tot,
+    double* __restrict__ fbt_bar, double2* __restrict__ shift_bar) {
+    __shared__ double red[32];
+    __shared__ double s_sum, s_pbar;
+    const double ps = p_pre[0];
+    double local = 0.0;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) local += w_post[w];
+    local = warp_sum(local);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) { s_sum = v; s_pbar = pbar[0]; }
+    }
+    __syncthreads();
+    const double sum = s_sum;
+    const double pop_w = (sum / W < 1.0e-300) ? 0.0 : s_pbar * (-damping / dt) / sum;
+    double pacc = 0.0;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        const double2 on = ov_post[w], op = ov_pre[w];
+        const WeightFactor f = weight_factor(dt, sqrt_dt, ps, h0_prop, shift_term[w], fb_term[w], on, op);
+        double imp_ph = f.imp_ph;
+        bool alive = !(imp_ph < w_floor) && !(imp_ph > w_cap);
+        if (!alive) imp_ph = 0.0;
+        const double wp = w_pre[w];
+        if (wp * imp_ph > w_cap) alive = false;
+        double wbn = wbar[w] + pop_w;
+        if (!alive) wbn = 0.0;
+        const double ib = wbn * wp;
+        pacc += ib * dt * imp_ph;
+        const double rfac = exp(fb_term[w].x + dt * (ps + h0_prop.x));
+        const double phib = ib * rfac;  // real
+        const double2 phi = f.phi;
+        // shift_bar = conj(-sqrt_dt phi) phib;  ov'b += conj(phi / ov') phib;  ovb = conj(-phi / ov) phib
+        shift_bar[w] = make_double2(-sqrt_dt * phi.x * phib, sqrt_dt * phi.y * phib);
+        const double2 r1 = cdiv(phi, on), r0 = cdiv(phi, op);
+        ovn_tot[w] = make_double2(ovbar[w].x + r1.x * phib, ovbar[w].y - r1.y * phib);
+        ovbar[w] = make_double2(-r0.x * phib, r0.y * phib);
+        fbt_bar[w] = ib * imp_ph;
+        wbar[w] = wbn * imp_ph;
+    }
+    pacc = warp_sum(pacc);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = pacc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) pbar[0] = v;
+    }
+}
+
+int launch_weight_adj(int W, const afq_params* p, double sqrt_dt, double dt, double2 h0_prop,
+                      const double2* shift_term, const double2* fb_term, const double* w_pre, const double2* ov_pre,
+                      const double* p_pre, const double* w_post, const double2* ov_post, double* wbar,
+                      double2* ovbar, double* pbar, double2* ovn_tot, double* fbt_bar, double2* shift_bar,
+                      cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    k_weight_adj<<<1, 1024, 0, s>>>(W, dt, sqrt_dt, p->pop_control_damping, p->weight_floor, p->weight_cap, h0_prop,
+                                    shift_term, fb_term, w_pre, ov_pre, p_pre, w_post, ov_post, wbar, ovbar, pbar,
+                                    ovn_tot, fbt_bar, shift_bar);
+    AFQ_LAUNCHED("k_weight_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Field-shift adjoint (W x G elementwise), in place on xtb:
+//   fsb = conj(x - fs) fbt_bar - conj(mf) shift_bar - xtb;  fbb = i sqrt_dt fsb,
+// fs = -sqrt_dt (i fb - mf) recomputed from fb as the forward does.
+// =====================================================================
+__global__ void k_fs_adj(int W, int G, double sqrt_dt, const double* __restrict__ x, const double2* __restrict__ fb,
+                         const double2* __restrict__ mf, const double* __restrict__ fbt_bar,
+                         const double2* __restrict__ shift_bar, double2* xtb) {
+    const long long total = (long long)W * G;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(e / G), g = (int)(e - (long long)w * G);
+        const double2 f = fb[e], m = mf[g];
+        const double2 fs = make_double2(-sqrt_dt * (-f.y - m.x), -sqrt_dt * (f.x - m.y));
+        const double tb = fbt_bar[w];
+        const double2 sb = shift_bar[w];
+        const double2 cm = cmulc(m, sb);  // conj(mf) shift_bar
+        const double2 v = xtb[e];
+        const double2 fsb = make_double2((x[e] - fs.x) * tb - cm.x - v.x, fs.y * tb - cm.y - v.y);
+        xtb[e] = make_double2(-sqrt_dt * fsb.y, sqrt_dt * fsb.x);
+    }
+}
+
+int launch_fs_adj(int W, int G, double sqrt_dt, const double* x, const double2* fb, const double2* mf,
+                  const double* fbt_bar, const double2* shift_bar, double2* xtb, cudaStream_t s) {
+    const long long total = (long long)W * G;
+    if (total <= 0) return AFQ_OK;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_fs_adj<<<(unsigned)blocks, 256, 0, s>>>(W, G, sqrt_dt, x, fb, mf, fbt_bar, shift_bar, xtb);
+    AFQ_LAUNCHED("k_fs_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Block measurement adjoint (prop/blocks.py:59-79; one CTA):
+//   p = (1 - alpha) p_prev + alpha e_b;  e_b = sum w E_c / sum w;  W_b = sum w;
+//   E_c = E if |E - e_est| <= sqrt(2/dt) else e_est.
+// In: ebar_b, wbar_b (the loss's adjoints of block b), pbar (in/out),
+// wbar (in/out); out: ebar_w (W) = dL/dE_w.
+// =====================================================================
+__global__ void __launch_bounds__(1024) k_measure_adj(int W, double dt, double alpha, const double* __restrict__ weights,
+                                                      const double2* __restrict__ energy,
+                                                      const double* __restrict__ e_est,
+                                                      const double* __restrict__ e_block,
+                                                      const double* __restrict__ eb_bar,
+                                                      const double* __restrict__ wb_bar, double* pbar, double* wbar,
+                                                      double* __restrict__ ebar_w) {
+    __shared__ double red[32];
+    __shared__ double s_sum, s_pb;
+    double local = 0.0;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) local += weights[w];
+    local = warp_sum(local);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) { s_sum = v; s_pb = pbar[0]; }
+    }
+    __syncthreads();
+    const double sum = s_sum, pb = s_pb;
+    const double eb = eb_bar[0] + alpha * pb;
+    const double eref = e_est[0], thresh = sqrt(2.0 / dt), ebk = e_block[0], wbb = wb_bar[0];
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        const double e = energy[w].x;
+        const bool clipped = fabs(e - eref) > thresh;
+        const double ec = clipped ? eref : e;
+        double wb = wbar[w] + wbb;
+        double ew = 0.0;
+        if (sum != 0.0) {
+            wb += eb * (ec - ebk) / sum;
+            if (!clipped) ew = eb * weights[w] / sum;
+        }
+        wbar[w] = wb;
+        ebar_w[w] = ew;
+    }
+    if (threadIdx.x == 0) pbar[0] = (1.0 - alpha) * pb;
+}
+
+int launch_measure_adj(int W, double dt, double alpha, const double* weights, const double2* energy,
+                       const double* e_est, const double* e_block, const double* eb_bar, const double* wb_bar,
+                       double* pbar, double* wbar, double* ebar_w, cudaStream_t s) {
+    k_measure_adj<<<1, 1024, 0, s>>>(W, dt, alpha, weights, energy, e_est, e_block, eb_bar, wb_bar, pbar, wbar,
+                                     ebar_w);
+    AFQ_LAUNCHED("k_measure_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Energy adjoint with respect to G_half (W x o x n elementwise):
+//   Gb = Eb_w conj(2 rot_h1 + 4 sum_g c_g L~_g - 2 sum_g f_g L~_g),
+// cl = sum_g c_g L~_g and y = sum_g f_g L~_g from the GEMMs.
+// =====================================================================
+__global__ void k_energy_gbar(int W, int on, const double* __restrict__ ebar_w, const double2* __restrict__ rot_h1,
+                              const double2* __restrict__ cl, const double2* __restrict__ y,
+                              double2* __restrict__ gbar) {
+    const long long total = (long long)W * on;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(e / on), k = (int)(e - (long long)w * on);
+        const double eb = ebar_w[w];
+        const double2 r = rot_h1[k], c = cl[e], v = y[e];
+        const double dx = 2.0 * r.x + 4.0 * c.x - 2.0 * v.x, dy = 2.0 * r.y + 4.0 * c.y - 2.0 * v.y;
+        gbar[e] = make_double2(eb * dx, -eb * dy);
+    }
+}
+
+int launch_energy_gbar(int W, int on, const double* ebar_w, const double2* rot_h1, const double2* cl,
+                       const double2* y, double2* gbar, cudaStream_t s) {
+    const long long total = (long long)W * on;
+    if (total <= 0) return AFQ_OK;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_energy_gbar<<<(unsigned)blocks, 256, 0, s>>>(W, on, ebar_w, rot_h1, cl, y, gbar);
+    AFQ_LAUNCHED("k_energy_gbar");
+    return AFQ_OK;
+}
+
+// sg[split][k] += sum_{w in split} ebar_w G[w, k]  (complex, o n entries)
+__global__ void k_sg_accum(int W, int on, int per, const double* __restrict__ ebar_w, const double2* __restrict__ g,
+                           double2* __restrict__ sg) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= on) return;
+    const int wa = blockIdx.y * per, wb = min(W, wa + per);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int w = wa; w < wb; ++w) rfma(acc, ebar_w[w], g[(size_t)w * on + k]);
+    double2* out = sg + (size_t)blockIdx.y * on + k;
+    *out = cadd(*out, acc);
+}
+
+int launch_sg_accum(int W, int on, const double* ebar_w, const double2* g, double2* sg, cudaStream_t s) {
+    const int ns = ebar_splits(W), per = (W + ns - 1) / ns;
+    dim3 grid((on + 127) / 128, ns);
+    k_sg_accum<<<grid, 128, 0, s>>>(W, on, per, ebar_w, g, sg);
+    AFQ_LAUNCHED("k_sg_accum");
+    return AFQ_OK;
+}
+
+// Ft[(w, p), (g, q)] = F[(w, q), (g, p)] for o x o blocks; rows of length G o.
+__global__ void k_block_transpose(int wc, int o, int G, const double2* __restrict__ F, double2* __restrict__ Ft) {
+    const long long go = (long long)G * o;
+    const long long total = (long long)wc * o * go;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long row = e / go, col = e - row * go;
+        const int w = (int)(row / o), p = (int)(row - (long long)w * o);
+        const int g = (int)(col / o), q = (int)(col - (long long)g * o);
+        Ft[e] = F[((long long)w * o + q) * go + (long long)g * o + p];
+    }
+}
+
+int launch_block_transpose(int wc, int o, int G, const double2* F, double2* Ft, cudaStream_t s) {
+    const long long total = (long long)wc * o * G * o;
+    if (total <= 0) return AFQ_OK;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_block_transpose<<<(unsigned)blocks, 256, 0, s>>>(wc, o, G, F, Ft);
+    AFQ_LAUNCHED("k_block_transpose");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// Comb adjoint (walkers.py:243-265): walkers and overlaps were gathered by
+// non-decreasing indices, weights set to sum|w| / N.  k_sr_sum checks the
+// indices and sums the weight adjoints; k_sr_adj scatters (one CTA per
+// source walker j, its copies k in [lo, hi) found by binary search).
+// =====================================================================
+__global__ void __launch_bounds__(1024) k_sr_sum(int W, const int32_t* __restrict__ idx, const double* __restrict__ wbar,
+                                                 double* __restrict__ sum_out, int* err) {
+    __shared__ double red[32];
+    double local = 0.0;
+    for (int k = threadIdx.x; k < W; k += blockDim.x) {
+        local += wbar[k];
+        const int v = idx[k];
+        if (v < 0 || v >= W || (k + 1 < W && idx[k + 1] < v)) set_err(err, AFQ_STATUS_BAD_INDEX);
+    }
+    local = warp_sum(local);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) sum_out[0] = v;
+    }
+}
+
+__device__ __forceinline__ int lower_bound_idx(const int32_t* idx, int W, int v) {
+    int lo = 0, hi = W;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (idx[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(128) k_sr_adj(int W, int no, const int32_t* __restrict__ idx,
+                                                const double2* __restrict__ wk_in, const double2* __restrict__ ob_in,
+                                                const double* __restrict__ weights, const double* __restrict__ wsum,
+                                                double2* __restrict__ wk_out, double2* __restrict__ ob_out,
+                                                double* __restrict__ wb_out) {
+    const int j = blockIdx.x;
+    const int lo = lower_bound_idx(idx, W, j), hi = lower_bound_idx(idx, W, j + 1);
+    for (int e = threadIdx.x; e < no; e += blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int k = lo; k < hi; ++k) acc = cadd(acc, wk_in[(size_t)k * no + e]);
+        wk_out[(size_t)j * no + e] = acc;
+    }
+    if (threadIdx.x == 0) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int k = lo; k < hi; ++k) acc = cadd(acc, ob_in[k]);
+        ob_out[j] = acc;
+        const double wj = weights[j];
+        const double sg = wj > 0.0 ? 1.0 : (wj < 0.0 ? -1.0 : 0.0);
+        wb_out[j] = sg * wsum[0] / W;
+    }
+}
+
+int launch_sr_adj(int W, int no, const int32_t* idx, const double2* wk_in, const double2* ob_in, const double* wb_in,
+                  const double* weights, double* wsum, double2* wk_out, double2* ob_out, double* wb_out, int* err,
+                  cudaStream_t s) {
+    k_sr_sum<<<1, 1024, 0, s>>>(W, idx, wb_in, wsum, err);
+    AFQ_LAUNCHED("k_sr_sum");
+    k_sr_adj<<<W, 128, 0, s>>>(W, no, idx, wk_in, ob_in, weights, wsum, wk_out, ob_out, wb_out);
+    AFQ_LAUNCHED("k_sr_adj");
+    return AFQ_OK;
+}
+
+// =====================================================================
+// dL/dh1 from dL/dE_half (E_half = expm(s h1_eff), s = -dt/2) and from the
+// one-body energy term:
+//   h1b = s L_exp(s h1_eff^T, Eb) + 2 Re(conj(C) S_G),
+// the Frechet derivative as the upper-right block of expm(s M),
+// M = [[A^T, Eb / (s eta)], [0, A^T]] (eta rescales Eb to the size of A).
+// =====================================================================
+__global__ void k_frechet_build(int n, const double* __restrict__ A, const double* __restrict__ Eb, double coef,
+                                double* __restrict__ M) {
+    const int m = 2 * n;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m * m) return;
+    const int r = e / m, c = e - r * m;
+    double v = 0.0;
+    if (r < n && c < n) v = A[c * n + r];
+    else if (r >= n && c >= n) v = A[(c - n) * n + (r - n)];
+    else if (r < n && c >= n) v = coef * Eb[r * n + (c - n)];
+    M[e] = v;
+}
+
+__global__ void k_h1bar_finish(int n, int o, double coef, const double* __restrict__ X, const double2* __restrict__ mo,
+                               const double2* __restrict__ sg, double* __restrict__ h1bar) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * n) return;
+    const int i = e / n, j = e - i * n;
+    double v = coef * X[(size_t)i * 2 * n + n + j];
+    double re = 0.0;
+    for (int a = 0; a < o; ++a) {
+        const double2 c = mo[(size_t)i * o + a], g = sg[(size_t)a * n + j];
+        re += c.x * g.x + c.y * g.y;  // Re(conj(c) g)
+    }
+    h1bar[e] = v + 2.0 * re;
+}
+
+__global__ void k_absmax(int count, const double* __restrict__ a, double* out) {
+    __shared__ double sm[256];
+    double best = 0.0;
+    for (int e = threadIdx.x; e < count; e += blockDim.x) best = fmax(best, fabs(a[e]));
+    sm[threadIdx.x] = best;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = sm[0];
+}
+
+// tmp: 5 (2n)^2 doubles + 2.  Reads two norms back to the host.
+int launch_h1bar(int n, int o, double dt, const double* h1_eff, const double* ebar, const double2* mo,
+                 const double2* sg, double* h1bar, double* tmp, cudaStream_t s) {
+    const int m = 2 * n;
+    double* M = tmp;
+    double* X = M + (size_t)m * m;
+    double* t0 = X + (size_t)m * m;
+    double* t1 = t0 + (size_t)m * m;
+    double* t2 = t1 + (size_t)m * m;
+    double* nrm = t2 + (size_t)m * m;
+    k_absmax<<<1, 256, 0, s>>>(n * n, ebar, nrm);
+    k_absmax<<<1, 256, 0, s>>>(n * n, h1_eff, nrm + 1);
+    AFQ_LAUNCHED("k_absmax");
+    double h[2] = {0.0, 0.0};
+    AFQ_CUDA(cudaMemcpyAsync(h, nrm, sizeof(h), cudaMemcpyDeviceToHost, s));
+    AFQ_CUDA(cudaStreamSynchronize(s));
+    const double sc = -0.5 * dt;
+    double eta = h[0] / (h[1] > 0.0 ? h[1] : 1.0);
+    if (!(eta > 0.0)) eta = 1.0;
+    k_frechet_build<<<(m * m + 255) / 256, 256, 0, s>>>(n, h1_eff, ebar, 1.0 / (sc * eta), M);
+    AFQ_LAUNCHED("k_frechet_build");
+    AFQ_TRY(launch_expm(m, sc, M, X, t0, t1, t2, nrm, s));
+    k_h1bar_finish<<<(n * n + 255) / 256, 256, 0, s>>>(n, o, sc * eta, X, mo, sg, h1bar);
+    AFQ_LAUNCHED("k_h1bar_finish");
+    return AFQ_OK;
+}
+
+}  // namespace afq

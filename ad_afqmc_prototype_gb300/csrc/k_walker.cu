@@ -392,20 +392,7 @@ __global__ void __launch_bounds__(1024) k_weight_update(
     double local = 0.0;
     for (int w = threadIdx.x; w < W; w += blockDim.x) {
         const double2 on = ovlp_new[w];
-        const double2 ratio = cdiv(on, overlaps[w]);
-        const double2 st = shift_term[w], ft = fb_term[w];
-        const double2 ex = make_double2(-sqrt_dt * st.x + ft.x + dt * (ps + h0_prop.x),
-                                        -sqrt_dt * st.y + ft.y + dt * h0_prop.y);
-        double sn, cs;
-        sincos(ex.y, &sn, &cs);
-        const double er = exp(ex.x);
-        const double2 imp = cmul(make_double2(er * cs, er * sn), ratio);
-        // theta = angle(exp(-sqrt_dt shift_term) * ratio)
-        sincos(-sqrt_dt * st.y, &sn, &cs);
-        const double er2 = exp(-sqrt_dt * st.x);
-        const double2 ph = cmul(make_double2(er2 * cs, er2 * sn), ratio);
-        const double theta = atan2(ph.y, ph.x);
-        double imp_ph = hypot(imp.x, imp.y) * cos(theta);
+        double imp_ph = weight_factor(dt, sqrt_dt, ps, h0_prop, shift_term[w], fb_term[w], on, overlaps[w]).imp_ph;
         if (imp_ph < w_floor) imp_ph = 0.0;
         if (imp_ph > w_cap) imp_ph = 0.0;
         double wn = weights[w] * imp_ph;

@@ -436,6 +436,55 @@ def run_blocks(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int,
     return e[:n_blocks], w[:n_blocks]
 
 
+# ------------------------------------------------- differentiated energy
+def grad_forward(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int, counter: int,
+                 checkpoint_blocks: int, sr_fixed: Optional[torch.Tensor] = None):
+    """n_blocks binary64 blocks on `st` in place with the tape kept for
+    grad_backward.  Returns device (energies (B,), weights (B,), comb
+    indices (B, W) int32, tape)."""
+    W = st.walkers.shape[0]
+    d = make_dims(W, prob.norb, prob.nocc, prob.nchol, prob.trial_is_real, prob.precision)
+    p = make_params(params)
+    lib = _lib.load()
+    tb = int(lib.afq_grad_tape_bytes(ctypes.byref(d), int(n_blocks), int(checkpoint_blocks)))
+    tape = torch.empty((max(tb, 256),), dtype=torch.uint8, device=st.walkers.device)
+    wsp, wsn = workspace(lib.afq_grad_workspace(ctypes.byref(d), ctypes.byref(p), 0))
+    if sr_fixed is not None:
+        sr_fixed = sr_fixed.to(device=st.walkers.device, dtype=torch.int32).contiguous()
+        if sr_fixed.shape != (n_blocks, W):
+            raise ValueError(f"sr_fixed must be (n_blocks, n_walkers) = ({n_blocks}, {W})")
+    e = torch.empty((n_blocks,), dtype=F64, device=st.walkers.device)
+    w = torch.empty_like(e)
+    idx = torch.empty((n_blocks, W), dtype=torch.int32, device=st.walkers.device)
+    pb = prob.c()
+    cs = st.c()
+    _lib.call("afq_grad_forward", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), int(n_blocks),
+              int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), int(checkpoint_blocks), ptr(sr_fixed), ptr(e),
+              ptr(w), ptr(idx), ptr(tape), tape.numel(), wsp, wsn, stream_ptr())
+    return e, w, idx, tape
+
+
+def grad_backward(prob: Problem, params, h1: torch.Tensor, n_blocks: int, seed: int, counter: int,
+                  checkpoint_blocks: int, tape: torch.Tensor, energies_bar: torch.Tensor,
+                  weights_bar: torch.Tensor) -> torch.Tensor:
+    """dL/dh1 (n, n) from dL/de_b and dL/dW_b of the run grad_forward taped."""
+    d = make_dims(prob.n_walkers, prob.norb, prob.nocc, prob.nchol, prob.trial_is_real, prob.precision)
+    p = make_params(params)
+    lib = _lib.load()
+    wsp, wsn = workspace(lib.afq_grad_workspace(ctypes.byref(d), ctypes.byref(p), int(checkpoint_blocks)))
+    eb = as_device(energies_bar, F64)
+    wb = as_device(weights_bar, F64)
+    if eb.shape != (n_blocks,) or wb.shape != (n_blocks,):
+        raise ValueError("energies_bar and weights_bar must be (n_blocks,)")
+    h1 = as_device(h1, F64)
+    out = torch.empty((prob.norb, prob.norb), dtype=F64, device=h1.device)
+    pb = prob.c()
+    _lib.call("afq_grad_backward", ctypes.byref(pb), ctypes.byref(p), ptr(h1), int(n_blocks),
+              int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), int(checkpoint_blocks), ptr(tape), tape.numel(),
+              ptr(eb), ptr(wb), ptr(out), wsp, wsn, stream_ptr())
+    return out
+
+
 # ------------------------------------------------------------- the network
 def mlp_param_count(n_features: int, hidden: int) -> int:
     n = int(_lib.load().afq_mlp_param_count(int(n_features), int(hidden)))

@@ -144,9 +144,12 @@ int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda
                      int64_t ldb, float* C, int64_t ldc, int32_t* err, int32_t accumulate,
                      void* stream);
 
-/* Device status word of a step / block workspace: synchronises `stream`,
- * copies the word to *status (0 = fine, 1 = a bounded device wait expired)
+/* Device status word of a step / block / gradient workspace: synchronises
+ * `stream`, copies the word to *status (0 = fine, AFQ_STATUS_* otherwise)
  * and clears it.  Returns AFQ_E_DEVICE_CHECK when the word was set. */
+#define AFQ_STATUS_WAIT_EXPIRED 1 /* a bounded device-side wait expired */
+#define AFQ_STATUS_SINGULAR 2     /* adjoint: a singular overlap matrix or QR factor R */
+#define AFQ_STATUS_BAD_INDEX 3    /* adjoint: comb indices out of range or not non-decreasing */
 int afq_workspace_status(void* workspace, int32_t* status, void* stream);
 
 /* ---- per-walker kernels, batched over walkers --------------------------- */
@@ -349,6 +352,46 @@ int afq_mlp_train_step(int32_t batch, int32_t n_features, int32_t hidden, float*
                        void* stream);
 /* bf16 copy of the fp32 master parameters. */
 int afq_mlp_sync(int32_t n_features, int32_t hidden, const float* master, void* params_bf16, void* stream);
+
+/* ---- differentiated energy (no counterpart in the reference, which ships
+ * no gradient of the energy) ----------------------------------------------
+ *
+ * dL/dh1 of a run of n_blocks binary64 blocks for any loss L of the block
+ * energies and weights, by reverse-mode adjoint kernels; dL/dlam for
+ * h1 + lam D is sum_ij dL/dh1[i,j] D[i,j].  The derivative is the pathwise
+ * one that jax.grad of a wrapper around afqmc_block (prop/blocks.py:22-95)
+ * gives on the same fields: the comb's indices (walkers.py:233-265), the
+ * weight floor/cap (prop/afqmc.py:127-134) and the energy clip
+ * (prop/blocks.py:59-66) are held at their values; the initial state is a
+ * constant.  Fields and comb uniforms come from the Philox stream (seed,
+ * counter + b (n_prop_steps + 1) + step) as in afq_run_blocks.  Binary64
+ * form, real trial orbitals, nocc <= 32.
+ *
+ * afq_grad_forward runs the blocks like afq_block (state updated in place;
+ * block b's energy and weight to block_energies[b], block_weights[b], its
+ * comb indices to sr_idx[b W ...] when sr_idx is given), keeping in `tape`
+ * the state every checkpoint_blocks blocks, the comb indices and the block
+ * results.  sr_fixed (optional, n_blocks x W non-decreasing indices) replaces
+ * the comb's own indices (finite differences of the same function).
+ * afq_grad_backward replays each checkpoint segment and runs the adjoint
+ * from energies_bar = dL/de_b, weights_bar = dL/dW_b (device, n_blocks) to
+ * h1_bar (device n x n): pb, p, h1 (the h1 pb was built from), seed, counter,
+ * n_blocks and checkpoint_blocks as in the forward.  The backward reads two
+ * scalars back to the host (scaling of the Frechet derivative of expm).
+ * A singular overlap matrix or unsorted indices set the workspace status.
+ * Workspace: afq_grad_workspace(d, p, checkpoint_blocks) bytes for the
+ * backward; the forward needs afq_grad_workspace(d, p, 0) bytes (a prefix
+ * of the backward's layout). */
+size_t afq_grad_tape_bytes(const afq_dims* d, int32_t n_blocks, int32_t checkpoint_blocks);
+size_t afq_grad_workspace(const afq_dims* d, const afq_params* p, int32_t checkpoint_blocks);
+int afq_grad_forward(const afq_problem* pb, const afq_params* p, const afq_state* st, int32_t n_blocks,
+                     uint64_t seed, uint64_t counter, int32_t checkpoint_blocks, const int32_t* sr_fixed,
+                     double* block_energies, double* block_weights, int32_t* sr_idx, void* tape,
+                     size_t tape_bytes, void* workspace, size_t workspace_bytes, void* stream);
+int afq_grad_backward(const afq_problem* pb, const afq_params* p, const double* h1, int32_t n_blocks,
+                      uint64_t seed, uint64_t counter, int32_t checkpoint_blocks, const void* tape,
+                      size_t tape_bytes, const double* energies_bar, const double* weights_bar, double* h1_bar,
+                      void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- tracing (no counterpart in the reference, which only times blocks
  * with time.perf_counter, driver.py:83-147) --------------------------------- */
