@@ -183,13 +183,22 @@ int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, uint64_t counter) {
     const double2* Wpre = slot(sn.walkers, (size_t)W * no, op);
     const double2* Wpost = slot(sn.walkers, (size_t)W * no, op + 1);
     // forward recomputation (the block's own kernels: the same fields, force bias and shifts)
-    AFQ_TRY(launch_philox((int64_t)W * G, c.seed, counter, 1, g.fields, s));
-    AFQ_TRY(launch_green(W, n, o, mo, 1, Wpre, nullptr, g.green, s));
-    AFQ_TRY(launch_zgemm(W, G, no, 2.0, g.green, no, pb->rot_chol, no, false, true, g.fb, G, s));
-    AFQ_TRY(launch_field_shift(W, G, pb->sqrt_dt, g.fields, g.fb, (const double2*)pb->mf_shifts, g.xs,
-                               g.shift_term, g.fb_term, s));
-    AFQ_TRY(launch_zgemm(W, n * n, G, 1.0, g.xs, G, pb->chol, (int64_t)n * n, false, false, g.V, (int64_t)n * n, s));
-    AFQ_TRY(launch_taylor_tape(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, Wpre, g.terms, g.w2, s));
+    {
+        AFQ_PHASE("adj_recompute", s);
+        AFQ_TRY(launch_philox((int64_t)W * G, c.seed, counter, 1, g.fields, s));
+        AFQ_TRY(launch_green(W, n, o, mo, 1, Wpre, nullptr, g.green, s));
+        AFQ_TRY(launch_zgemm(W, G, no, 2.0, g.green, no, pb->rot_chol, no, false, true, g.fb, G, s));
+        AFQ_TRY(launch_field_shift(W, G, pb->sqrt_dt, g.fields, g.fb, (const double2*)pb->mf_shifts, g.xs,
+                                   g.shift_term, g.fb_term, s));
+    }
+    {
+        AFQ_PHASE("adj_vbuild_gemm", s);
+        AFQ_TRY(launch_zgemm(W, n * n, G, 1.0, g.xs, G, pb->chol, (int64_t)n * n, false, false, g.V,
+                             (int64_t)n * n, s));
+    }
+    { AFQ_PHASE("adj_taylor_tape", s);
+      AFQ_TRY(launch_taylor_tape(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, Wpre, g.terms, g.w2, s)); }
+    AFQ_PHASE("adj_step_rest", s);
     // weights, population shift and overlap ratio
     AFQ_TRY(launch_weight_adj(W, c.p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                               g.shift_term, g.fb_term, slot(sn.weights, W, op), slot(sn.overlaps, W, op),
@@ -199,12 +208,16 @@ int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, uint64_t counter) {
     AFQ_TRY(launch_green_adj(W, n, o, mo, Wpost, nullptr, slot(sn.overlaps, W, op + 1), g.ovn_tot, g.wk, g.status,
                              s));
     // W' = E W2: dL/dE += Re W'b W2^H; Taylor reverse; W1 = E W: dL/dE += Re W1b W^H
-    AFQ_TRY(launch_ebar(W, n, o, g.wk, no, g.w2, no, g.ebar_part, s));
-    AFQ_TRY(launch_taylor_adj(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, g.wk, g.tbar, g.wk, s));
-    AFQ_TRY(launch_ebar(W, n, o, g.tbar, (long long)(K + 1) * no, Wpre, no, g.ebar_part, s));
+    { AFQ_PHASE("adj_ebar", s); AFQ_TRY(launch_ebar(W, n, o, g.wk, no, g.w2, no, g.ebar_part, s)); }
+    { AFQ_PHASE("adj_taylor", s);
+      AFQ_TRY(launch_taylor_adj(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, g.wk, g.tbar, g.wk, s)); }
+    { AFQ_PHASE("adj_ebar", s);
+      AFQ_TRY(launch_ebar(W, n, o, g.tbar, (long long)(K + 1) * no, Wpre, no, g.ebar_part, s)); }
     // V = sum_g x~_g L_g: x~b = Vb . L^T
-    AFQ_TRY(launch_vbar(W, n, o, K, pb->sqrt_dt, g.tbar, g.terms, g.V, s));
-    AFQ_TRY(launch_zgemm(W, G, n * n, 1.0, g.V, (int64_t)n * n, pb->chol, (int64_t)n * n, false, true, g.xtb, G, s));
+    { AFQ_PHASE("adj_vbar", s); AFQ_TRY(launch_vbar(W, n, o, K, pb->sqrt_dt, g.tbar, g.terms, g.V, s)); }
+    { AFQ_PHASE("adj_xbar_gemm", s);
+      AFQ_TRY(launch_zgemm(W, G, n * n, 1.0, g.V, (int64_t)n * n, pb->chol, (int64_t)n * n, false, true, g.xtb, G,
+                           s)); }
     // field shifts, then the force bias fb = 2 L~ vec(G_half)
     AFQ_TRY(launch_fs_adj(W, G, pb->sqrt_dt, g.fields, g.fb, (const double2*)pb->mf_shifts, g.fbt_bar, g.shift_bar,
                           g.xtb, s));
@@ -231,6 +244,7 @@ int block_adjoint(const Ctx& c, const BlockSnap& sn, const TapeLayout& t, int b,
     std::swap(g.wk, g.wk2);
     std::swap(g.ob, g.ob2);
     std::swap(g.wb, g.wb2);
+    AFQ_PHASE("adj_block_end", s);
     // measurement and population-shift EMA
     AFQ_TRY(launch_measure_adj(W, p->dt, p->shift_ema, wm, sn.energy, g.e_est, t.be + b, eb_bar + b, wb_bar + b,
                                g.pb, g.wb, g.ebar_w, s));
@@ -384,6 +398,7 @@ int afq_grad_backward(const afq_problem* pb, const afq_params* p, const double* 
             return x;
         };
         for (int b = b0; b < b1; ++b) {
+            AFQ_PHASE("adj_replay", s);
             const BlockSnap x = snap_of(b);
             AFQ_TRY(run_block_taped(pb, p, &wst, seed, block_counter(counter, p, b), t.idx + (size_t)b * W, nullptr,
                                     g.be, g.bw, &x, g.block, g.block_bytes, s));

@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison block")
     ap.add_argument("--no-cv", action="store_true", help="skip the control-variate line")
+    ap.add_argument("--no-grad", action="store_true", help="skip the differentiated-energy line")
     return ap.parse_args()
 
 
@@ -300,12 +301,82 @@ def run_ours(args, rank, world):
            "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
     if cvline:
         out["control_variate"] = cvline
+    if rank == 0 and not args.no_grad:
+        out["differentiation"] = run_grad()
     if compare:
         out["plain_fp64"] = compare
         out["ratio_vs_plain_fp64"] = round(value / compare["value"], 2)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     return out
+
+
+def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20, eps=1e-4):
+    """The differentiated energy on the 60-orbital workload: E = sum_b W_b e_b
+    / sum_b W_b over 20 blocks (200 steps, QR every 5, checkpoints every 20
+    steps) with h1 + lam D at lam = 0; dE/dlam by the adjoint kernels against
+    central differences at lam = +-eps on the same fields, the comb held at
+    the unperturbed run's indices (and, for information, left free)."""
+    import torch
+    from ad_afqmc_prototype_gb300 import synth
+    from ad_afqmc_prototype_gb300.core.system import system
+    from ad_afqmc_prototype_gb300.grad import block_energies, mixed_energy
+    from ad_afqmc_prototype_gb300.ham.chol import ham_chol
+    from ad_afqmc_prototype_gb300.meas.rhf import make_rhf_meas_ops
+    from ad_afqmc_prototype_gb300.prop.afqmc import init_prop_state
+    from ad_afqmc_prototype_gb300.prop.types import afqmc_params
+    from ad_afqmc_prototype_gb300.trial.rhf import make_rhf_trial_ops, rhf_trial
+    wl = synth.WORKLOADS[workload]
+    H = synth.make_workload(wl)
+    sys_ = system(norb=wl.nbasis, nelec=(wl.nocc, wl.nocc), walker_kind="restricted")
+    ham = ham_chol(h0=H["h0"], h1=H["h1"], chol=H["chol"])
+    trial = rhf_trial(H["mo_coeff"])
+    params = afqmc_params(dt=0.005, n_walkers=wl.n_walkers, seed=wl.seed, n_prop_steps=STEPS_PER_BLOCK,
+                          qr_every=QR_EVERY)
+    st0 = init_prop_state(sys=sys_, n_walkers=wl.n_walkers, seed=wl.seed, ham_data=ham,
+                          trial_ops_=make_rhf_trial_ops(sys_), trial_data=trial, meas_ops=make_rhf_meas_ops(sys_))
+    D = torch.as_tensor(H["D"], device="cuda")
+    kw = dict(ham_data=ham, trial_data=trial, params=params, state=st0, n_blocks=n_blocks, seed=17, counter=0,
+              checkpoint_every=checkpoint_every)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.no_grad():  # warm-up
+        block_energies(ham.h1, **{**kw, "n_blocks": 1})
+    torch.cuda.synchronize()
+    h1 = ham.h1.clone().requires_grad_(True)
+    runs = []
+    ev[0].record(stream)
+    e, w = block_energies(h1, run_out=runs, **kw)
+    E = mixed_energy(e, w)
+    ev[1].record(stream)
+    E.backward()
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms, bwd_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    adj = float((h1.grad * D).sum())
+    idx = runs[0].sr_idx
+
+    def central(sr):
+        vals, moved = [], 0
+        with torch.no_grad():
+            for s in (1.0, -1.0):
+                r = []
+                ee, ww = block_energies(ham.h1 + s * eps * D, sr_fixed=sr, run_out=r, **kw)
+                vals.append(float(mixed_energy(ee, ww)))
+                moved += int((r[0].sr_idx != idx).sum())
+        return (vals[0] - vals[1]) / (2 * eps), moved
+
+    fd, _ = central(idx)
+    free, moved = central(None)
+    return {"workload": workload, "n_blocks": n_blocks, "steps": n_blocks * STEPS_PER_BLOCK,
+            "checkpoint_every_steps": checkpoint_every, "precision": "fp64",
+            "energy": round(float(E), 10), "dE_dlambda_adjoint": adj, "dE_dlambda_fd_fixed_comb": fd,
+            "rel_diff": abs(adj - fd) / abs(fd), "fd_eps": eps,
+            "dE_dlambda_fd_free_comb": free, "free_comb_indices_moved": moved,
+            "forward_ms": round(fwd_ms, 2), "backward_ms": round(bwd_ms, 2),
+            "backward_over_forward": round(bwd_ms / fwd_ms, 2),
+            "walker_steps_per_s_forward_backward": round(wl.n_walkers * n_blocks * STEPS_PER_BLOCK
+                                                        / ((fwd_ms + bwd_ms) / 1000.0), 1)}
 
 
 def run_cv(args, env, st, W, world, seed, ctr):
