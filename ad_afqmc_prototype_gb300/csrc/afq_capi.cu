@@ -65,6 +65,8 @@ struct LowpDims {
     int S_E, Kt_E;   // energy:     L~ (G o x n)      . G_half rows (2 o W x n)
     int sec;         // sections per split row (6 or 3)
     long long ldv;   // row stride of V (fp32)
+    bool xf;         // exchange contracted in the energy GEMM's epilogue (24 < nocc <= 32)
+    int Pe;          // rows per (walker, part) block and per Cholesky vector in the energy GEMM
 };
 
 static LowpDims lowp_dims(const afq_dims* d) {
@@ -78,8 +80,15 @@ static LowpDims lowp_dims(const afq_dims* d) {
     L.S_E = n;
     L.Kt_E = (int)round_up((long long)L.sec * n, 64);
     L.ldv = round_up((long long)n * n, 4);
+    // blocks padded to 32 rows cost (32/o)^2 more GEMM work, and save writing and
+    // reading F (G o x 2 o fp32 per walker): worth it for o close to 32
+    L.xf = o > 24 && o <= 32;
+    L.Pe = L.xf ? 32 : o;
     return L;
 }
+
+// Exchange partials per walker of the mixed energy (one with the fused GEMM).
+static int exch_chunks(const afq_dims* d) { return lowp_dims(d).xf ? 1 : exchange_chunks(d->nchol); }
 
 struct LowpBufs {
     __nv_bfloat16* Bv;  // n^2 x Kt_V   right operand [hi lo hi] of chol^T
@@ -93,7 +102,8 @@ static LowpBufs layout_lowp(Arena& a, const afq_dims* d) {
     LowpBufs b;
     b.Bv = a.take<__nv_bfloat16>(n * n * L.Kt_V);
     b.Bf = a.take<__nv_bfloat16>(G * L.Kt_F);
-    b.Le = a.take<__nv_bfloat16>(G * o * L.Kt_E);
+    b.Le = a.take<__nv_bfloat16>(G * L.Pe * L.Kt_E);
+    (void)o;
     return b;
 }
 
@@ -145,9 +155,11 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
     return s;
 }
 
-// walkers per energy GEMM in the mixed form: F (G o x 2 o We fp32) <= 2 GiB
+// walkers per energy GEMM in the mixed form: F (G o x 2 o We fp32) <= 2 GiB,
+// or with the fused exchange the Green's-function rows (2 x 32 x Kt_E bf16)
 static int energy_chunk(const afq_dims* d) {
-    const long long per = (long long)d->nchol * d->nocc * 2 * d->nocc * 4;
+    const LowpDims L = lowp_dims(d);
+    const long long per = L.xf ? 2LL * 32 * L.Kt_E * 2 : (long long)d->nchol * d->nocc * 2 * d->nocc * 4;
     long long we = (2LL << 30) / (per > 0 ? per : 1);
     if (we < 1) we = 1;
     if (we > d->n_walkers) we = d->n_walkers;
@@ -166,7 +178,9 @@ struct BlockWS {
     double2* wcopy;      // W*n*o
     double2* ocopy;      // W
     __nv_bfloat16* Bg;   // mixed energy: 2 o We x Kt_E
-    float* F;            // mixed energy: G o x 2 o We
+    float* F;            // mixed energy: G o x 2 o We (not with the fused exchange)
+    float* xsum;         // fused exchange: We x exchange_halves(G) x 2
+    float* ctr;          // fused exchange: We x G x 2 traces of f_g
     float* cv_feat;      // mixed: W x AFQ_CV_FEATURES
     float* cv_y;         // mixed: W network outputs
     double* cv_ebase;    // mixed: W energies without exchange
@@ -183,9 +197,14 @@ static BlockWS layout_block(Arena& a, const afq_dims* d, int n_chunks) {
     if (is_mixed(d->precision)) {
         const LowpDims L = lowp_dims(d);
         const size_t we = energy_chunk(d);
-        b.partial = (double*)a.take<double2>(W * exchange_chunks(d->nchol) * 2);
-        b.Bg = a.take<__nv_bfloat16>(2 * d->nocc * we * L.Kt_E);
-        b.F = a.take<float>((size_t)d->nchol * d->nocc * 2 * d->nocc * we);
+        b.partial = (double*)a.take<double2>(W * exch_chunks(d) * 2);
+        b.Bg = a.take<__nv_bfloat16>(2 * L.Pe * we * L.Kt_E);
+        if (L.xf) {
+            b.xsum = a.take<float>(we * exchange_halves(d->nchol) * 2);
+            b.ctr = a.take<float>(we * d->nchol * 2);
+        } else {
+            b.F = a.take<float>((size_t)d->nchol * d->nocc * 2 * d->nocc * we);
+        }
         b.cv_feat = a.take<float>(W * AFQ_CV_FEATURES);
         b.cv_y = a.take<float>(W);
         b.cv_ebase = a.take<double>(W);
@@ -341,12 +360,21 @@ static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS
     const LowpDims L = lowp_dims(d);
     Arena la((void*)pb->lowp, (size_t)-1);
     const LowpBufs lb = layout_lowp(la, d);
-    const int We = energy_chunk(d), nch = exchange_chunks(G);
+    const int We = energy_chunk(d), nch = exch_chunks(d);
     double2* partial = (double2*)ws.partial;
     for (int w0 = 0; w0 < W; w0 += We) {
         const int wc = W - w0 < We ? W - w0 : We;
         { AFQ_PHASE("e_green_rows", s);
-          AFQ_TRY(launch_green_rows(wc, n, o, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, L.sec, s)); }
+          AFQ_TRY(launch_green_rows(wc, n, o, L.Pe, ws.green + (size_t)w0 * o * n, ws.Bg, L.S_E, L.Kt_E, L.sec,
+                                    s)); }
+        if (L.xf) {
+            { AFQ_PHASE("e_gemm", s);
+              AFQ_TRY(launch_tc_gemm_exchange(wc, G, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.xsum, ws.ctr,
+                                              ws.step.status, s)); }
+            { AFQ_PHASE("e_exchange", s);
+              AFQ_TRY(launch_exchange_finish(wc, G, ws.xsum, ws.ctr, partial + (size_t)w0 * nch * 2, s)); }
+            continue;
+        }
         // F[(w, part, k), (g, i)]: the six sections of Bg (left) and Le
         // (right) pair up as hh + hm + mh + hl + lh + mm
         { AFQ_PHASE("e_gemm", s);
@@ -559,8 +587,14 @@ int afq_prepare_lowp(const afq_dims* d, const double* chol, const double* rot_ch
     AFQ_TRY(launch_split_rows(n * n, (int)G, L.S_V, L.Kt_V, chol, 1, n * n, b.Bv, 0, L.sec, s));
     // rot_chol_flat: row g over (p, j)              (right operand of the force bias)
     AFQ_TRY(launch_split_rows(G, (int)(o * n), L.S_F, L.Kt_F, rot_chol, o * n, 1, b.Bf, 0, L.sec, s));
-    // rot_chol rows (g, p) over j                   (left operand of the energy)
-    AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, L.sec, s));
+    // rot_chol rows (g, p) over j                   (left operand of the energy);
+    // with the fused exchange, blocks of 32 rows per g (rows p >= o zero)
+    if (L.xf) {
+        AFQ_CUDA(cudaMemsetAsync(b.Le, 0, sizeof(__nv_bfloat16) * (size_t)G * L.Pe * L.Kt_E, s));
+        AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, L.sec, s, (int)o, L.Pe));
+    } else {
+        AFQ_TRY(launch_split_rows(G * o, (int)n, L.S_E, L.Kt_E, rot_chol, n, 1, b.Le, 1, L.sec, s));
+    }
     return AFQ_OK;
 }
 
@@ -850,7 +884,7 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
                                      ws.cv_ebase, s)); }
         if (!est) {  // exact measurement, and the training data
             AFQ_TRY(energy_impl(pb, st, ws, s, true));
-            AFQ_TRY(launch_cv_record(W, exchange_chunks(G), (const double2*)ws.partial, cv->rec_exchange, s));
+            AFQ_TRY(launch_cv_record(W, exch_chunks(d), (const double2*)ws.partial, cv->rec_exchange, s));
             AFQ_PHASE("block_measure", s);
             AFQ_TRY(launch_block_measure(W, p->dt, p->shift_ema, st->weights, ws.energy, st->e_estimate,
                                          st->pop_control_ene_shift, block_energy, block_weight, s));
@@ -863,12 +897,19 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
             // the sample's offset: its own Philox stream (seed offset by a constant), this block's counter
             AFQ_TRY(launch_philox(1, seed ^ 0x9E3779B97F4A7C15ull, counter + p->n_prop_steps, 0, ws.cv_u, s));
             AFQ_TRY(launch_cv_pick(ws.cv_u, stride, ws.cv_off, s));
-            const int We = energy_chunk(d), nch = exchange_chunks(G);
+            const int We = energy_chunk(d), nch = exch_chunks(d);
             AFQ_PHASE("energy", s);
             for (int s0 = 0; s0 < m_max; s0 += We) {
                 const int sc = m_max - s0 < We ? m_max - s0 : We;
-                AFQ_TRY(launch_cv_green_rows(sc, s0, ws.cv_off, stride, W, n, o, ws.green, ws.Bg, L.S_E, L.Kt_E,
-                                             L.sec, s));
+                AFQ_TRY(launch_cv_green_rows(sc, s0, ws.cv_off, stride, W, n, o, L.Pe, ws.green, ws.Bg, L.S_E,
+                                             L.Kt_E, L.sec, s));
+                if (L.xf) {
+                    AFQ_TRY(launch_tc_gemm_exchange(sc, G, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.xsum, ws.ctr,
+                                                    ws.step.status, s));
+                    AFQ_TRY(launch_exchange_finish(sc, G, ws.xsum, ws.ctr,
+                                                   (double2*)ws.partial + (size_t)s0 * nch * 2, s));
+                    continue;
+                }
                 AFQ_TRY(launch_tc_gemm_tn_drain(2 * o * sc, G * o, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.F,
                                                 (long long)G * o, ws.step.status, s));
                 AFQ_TRY(launch_exchange_reduce(sc, G, o, ws.F, (long long)G * o,

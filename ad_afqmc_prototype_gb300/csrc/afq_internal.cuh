@@ -266,7 +266,7 @@ int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const doubl
 
 // k_mixed.cu
 int launch_split_rows(long long rows, int K, int S, int Kt, const double* src, long long rs, long long ks,
-                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s);
+                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s, int grp = 0, int grp_pad = 0);
 int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s);
 int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
                              const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
@@ -283,7 +283,7 @@ int launch_cv_features(int W, int n, int o, int G, double h0, const double2* gre
                        const float* fbm, long long ldf, const double2* ovlp, const float* shift, const float* scale,
                        float* feat, double* ebase, cudaStream_t s);
 int launch_cv_pick(const double* u, int stride, int* off, cudaStream_t s);
-int launch_cv_green_rows(int sc, int s0, const int* off, int stride, int W, int n, int o, const double2* green,
+int launch_cv_green_rows(int sc, int s0, const int* off, int stride, int W, int n, int o, int P, const double2* green,
                          __nv_bfloat16* dst, int S, int Kt, int sec, cudaStream_t s);
 int launch_cv_record(int W, int nchunk, const double2* partial, double* xout, cudaStream_t s);
 int launch_cv_measure(int W, double dt, double alpha, const double* weights, const double* ebase, const float* ynn,
@@ -304,8 +304,16 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
 int launch_e_minus_i_split(int n, const double* E, __nv_bfloat16* eh, __nv_bfloat16* em, cudaStream_t s);
 int exchange_chunks(int G);
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s);
-int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
+int launch_green_rows(int wc, int n, int o, int P, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
                       cudaStream_t s);
+// k_tc_gemm.cu : the energy GEMM with the exchange contraction in its epilogue
+// (nocc <= 32 padded to 32-row blocks): A = the Green's-function rows of nw
+// walkers (2 x 32 rows each), B = L~ rows (32 per Cholesky vector); writes
+// x (nw x exchange_halves(G) x 2) and c (nw x G x 2) fp32 instead of F.
+int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
+                            float* x, float* c, int* err, cudaStream_t s);
+int exchange_halves(int G);
+int launch_exchange_finish(int nw, int G, const float* x, const float* c, double2* partial, cudaStream_t s);
 
 // k_adjoint.cu : reverse-mode kernels of the binary64 step and block
 int launch_taylor_tape(int W, int n, int o, int K, double sqrt_dt, const double* E, const double2* V,

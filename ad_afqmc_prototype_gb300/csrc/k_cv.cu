@@ -94,12 +94,12 @@ int launch_cv_pick(const double* u, int stride, int* off, cudaStream_t s) {
 }
 
 // Energy-GEMM rows of sampled walkers s0 .. s0 + sc - 1 (walker off + s
-// stride; rows of walkers past W are zero): row (s_local 2 + part) o + k
-// holds split(G_part[w, k, :]), as k_green_rows.
-__global__ void k_cv_green_rows(int sc, int s0, const int* __restrict__ off, int stride, int W, int n, int o,
+// stride; rows of walkers past W are zero): row (s_local 2 + part) P + k
+// holds split(G_part[w, k, :]) (zero for k >= o), as k_green_rows.
+__global__ void k_cv_green_rows(int sc, int s0, const int* __restrict__ off, int stride, int W, int n, int o, int P,
                                 const double2* __restrict__ green, __nv_bfloat16* __restrict__ dst, int S, int Kt,
                                 int sec) {
-    const long long rows = (long long)sc * o * 2;
+    const long long rows = (long long)sc * P * 2;
     const long long total = rows * (long long)Kt;
     const int o0 = off[0];
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -107,11 +107,11 @@ __global__ void k_cv_green_rows(int sc, int s0, const int* __restrict__ off, int
         const long long r = e / Kt;
         const int kk = (int)(e % Kt);
         __nv_bfloat16* row = dst + r * Kt;
-        const int k = (int)(r % o), part = (int)((r / o) % 2), sl = (int)(r / (2 * o));
+        const int k = (int)(r % P), part = (int)((r / P) % 2), sl = (int)(r / (2 * P));
         const int w = o0 + (s0 + sl) * stride;
         if (kk < S) {
             double x = 0.0;
-            if (kk < n && w < W) {
+            if (kk < n && w < W && k < o) {
                 const double2 v = green[((size_t)w * o + k) * n + kk];
                 x = part ? v.y : v.x;
             }
@@ -122,12 +122,12 @@ __global__ void k_cv_green_rows(int sc, int s0, const int* __restrict__ off, int
     }
 }
 
-int launch_cv_green_rows(int sc, int s0, const int* off, int stride, int W, int n, int o, const double2* green,
+int launch_cv_green_rows(int sc, int s0, const int* off, int stride, int W, int n, int o, int P, const double2* green,
                          __nv_bfloat16* dst, int S, int Kt, int sec, cudaStream_t s) {
-    const long long total = (long long)sc * o * 2 * Kt;
+    const long long total = (long long)sc * P * 2 * Kt;
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_cv_green_rows<<<(unsigned)blocks, 256, 0, s>>>(sc, s0, off, stride, W, n, o, green, dst, S, Kt, sec);
+    k_cv_green_rows<<<(unsigned)blocks, 256, 0, s>>>(sc, s0, off, stride, W, n, o, P, green, dst, S, Kt, sec);
     AFQ_LAUNCHED("k_cv_green_rows");
     return AFQ_OK;
 }

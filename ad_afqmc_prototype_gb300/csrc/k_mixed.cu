@@ -16,15 +16,18 @@ namespace afq {
 // ------------------------------------------------------ operand preparation
 // dst row r (Kt entries): sections at 0, S, 2S of split(src(r, k)), k < K;
 // entries [3S, Kt) and [K, S) of each section are zero.
-// src(r, k) = src[r * rs + k * ks].
+// src(r, k) = src[r * rs + k * ks].  With grp > 0 source row r goes to dst
+// row (r / grp) grp_pad + r % grp (groups padded to grp_pad rows; the pad
+// rows are not written).
 __global__ void k_split_rows(long long rows, int K, int S, int Kt, const double* __restrict__ src, long long rs,
-                             long long ks, __nv_bfloat16* __restrict__ dst, int left, int sec) {
+                             long long ks, __nv_bfloat16* __restrict__ dst, int left, int sec, int grp, int grp_pad) {
     const long long total = rows * (long long)Kt;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const long long r = e % rows;  // rows fastest: coalesced reads of column-major sources
         const int kk = (int)(e / rows);
-        __nv_bfloat16* row = dst + r * Kt;
+        const long long dr = grp > 0 ? (r / grp) * grp_pad + r % grp : r;
+        __nv_bfloat16* row = dst + dr * Kt;
         if (kk < S) {
             const double x = kk < K ? src[r * rs + (long long)kk * ks] : 0.0;
             split_store(row, S, kk, x, left != 0, sec);
@@ -35,11 +38,11 @@ __global__ void k_split_rows(long long rows, int K, int S, int Kt, const double*
 }
 
 int launch_split_rows(long long rows, int K, int S, int Kt, const double* src, long long rs, long long ks,
-                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s) {
+                      __nv_bfloat16* dst, int left, int sec, cudaStream_t s, int grp, int grp_pad) {
     const long long total = rows * (long long)Kt;
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_split_rows<<<(unsigned)blocks, 256, 0, s>>>(rows, K, S, Kt, src, rs, ks, dst, left, sec);
+    k_split_rows<<<(unsigned)blocks, 256, 0, s>>>(rows, K, S, Kt, src, rs, ks, dst, left, sec, grp, grp_pad);
     AFQ_LAUNCHED("k_split_rows");
     return AFQ_OK;
 }
@@ -993,6 +996,39 @@ __global__ void __launch_bounds__(256) k_exchange_reduce(int G, int o, const flo
 
 int exchange_chunks(int G) { return (G + EX_G - 1) / EX_G; }
 
+// The exchange-fused energy GEMM's outputs (launch_tc_gemm_exchange) to the
+// partials of k_exchange_reduce with one chunk: partial[w 2] = sum_g c_g^2,
+// partial[w 2 + 1] = (sum_g Re sum_ik f_g[i,k] f_g[k,i], 0); one warp per
+// walker, fixed summation order.  Only the real part of the exchange is
+// formed: the block measurement reads Re E_loc (prop/blocks.py:63).
+__global__ void k_exchange_finish(int nw, int G, int nhalf, const float* __restrict__ x, const float* __restrict__ c,
+                                  double2* __restrict__ partial) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (w >= nw) return;
+    double cr = 0.0, ci = 0.0, xr = 0.0;
+    for (int g = lane; g < G; g += 32) {
+        const double tr = c[((size_t)w * G + g) * 2], ti = c[((size_t)w * G + g) * 2 + 1];
+        cr += tr * tr - ti * ti;
+        ci += 2.0 * tr * ti;
+    }
+    for (int h = lane; h < nhalf; h += 32)
+        xr += (double)x[((size_t)w * nhalf + h) * 2] - (double)x[((size_t)w * nhalf + h) * 2 + 1];
+    cr = warp_sum(cr);
+    ci = warp_sum(ci);
+    xr = warp_sum(xr);
+    if (lane == 0) {
+        partial[(size_t)w * 2] = make_double2(cr, ci);
+        partial[(size_t)w * 2 + 1] = make_double2(xr, 0.0);
+    }
+}
+
+int launch_exchange_finish(int nw, int G, const float* x, const float* c, double2* partial, cudaStream_t s) {
+    if (nw <= 0) return AFQ_OK;
+    k_exchange_finish<<<(nw + 7) / 8, 256, 0, s>>>(nw, G, exchange_halves(G), x, c, partial);
+    AFQ_LAUNCHED("k_exchange_finish");
+    return AFQ_OK;
+}
+
 int launch_exchange_reduce(int wc, int G, int o, const float* F, long long ldf, double2* partial, cudaStream_t s) {
     if (wc <= 0) return AFQ_OK;
     const size_t smem = (size_t)2 * o * (EX_G * o + 4) * sizeof(float);
@@ -1020,21 +1056,22 @@ int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s) {
     return AFQ_OK;
 }
 
-// Green's function rows for the energy GEMM: row (w*2 + part)*o + k holds
-// split(G_part[w, k, :]) with K = n in sections of S.
-__global__ void k_green_rows(int wc, int n, int o, const double2* __restrict__ green, __nv_bfloat16* __restrict__ dst,
-                             int S, int Kt, int sec) {
-    const long long rows = (long long)wc * o * 2;
+// Green's function rows for the energy GEMM: row (w*2 + part)*P + k holds
+// split(G_part[w, k, :]) with K = n in sections of S; rows k >= o (P > o,
+// the exchange-fused layout) are zero.
+__global__ void k_green_rows(int wc, int n, int o, int P, const double2* __restrict__ green,
+                             __nv_bfloat16* __restrict__ dst, int S, int Kt, int sec) {
+    const long long rows = (long long)wc * P * 2;
     const long long total = rows * (long long)Kt;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const long long r = e / Kt;
         const int kk = (int)(e % Kt);
         __nv_bfloat16* row = dst + r * Kt;
-        const int k = (int)(r % o), part = (int)((r / o) % 2), w = (int)(r / (2 * o));
+        const int k = (int)(r % P), part = (int)((r / P) % 2), w = (int)(r / (2 * P));
         if (kk < S) {
             double x = 0.0;
-            if (kk < n) {
+            if (kk < n && k < o) {
                 const double2 v = green[((size_t)w * o + k) * n + kk];
                 x = part ? v.y : v.x;
             }
@@ -1045,12 +1082,12 @@ __global__ void k_green_rows(int wc, int n, int o, const double2* __restrict__ g
     }
 }
 
-int launch_green_rows(int wc, int n, int o, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
+int launch_green_rows(int wc, int n, int o, int P, const double2* green, __nv_bfloat16* dst, int S, int Kt, int sec,
                       cudaStream_t s) {
-    const long long total = (long long)wc * o * 2 * Kt;
+    const long long total = (long long)wc * P * 2 * Kt;
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_green_rows<<<(unsigned)blocks, 256, 0, s>>>(wc, n, o, green, dst, S, Kt, sec);
+    k_green_rows<<<(unsigned)blocks, 256, 0, s>>>(wc, n, o, P, green, dst, S, Kt, sec);
     AFQ_LAUNCHED("k_green_rows");
     return AFQ_OK;
 }

@@ -224,14 +224,37 @@ struct Drain {
 };
 static_assert(Drain<128>::STG * Drain<128>::STAGE + 1024 + 256 <= 227 * 1024, "drained GEMM shared memory");
 
-// SPLIT: instead of fp32 C, write the two-piece bf16 split of each sum to
-// Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.
-template <int BNT, bool SPLIT>
+// Epilogue of the exchange-fused energy GEMM (MODE 2): a 32 x 33 fp32
+// transpose buffer per epilogue warp after the barriers.
+constexpr int XT_BYTES = 8 * 32 * 33 * 4;
+static_assert(Drain<128>::SMEM + XT_BYTES <= 227 * 1024, "exchange-fused GEMM shared memory");
+
+// Outputs of MODE 2 (the local energy's exchange, meas/rhf.py:36-50).  Rows
+// of the product are (walker, part, k) with 32 rows per part (k >= nocc zero)
+// and columns (g, i) with 32 per Cholesky vector, so a 128 x 128 tile holds
+// the Re and Im planes of f_g[i, k] for two walkers and four vectors.
+//   x[(w nhalf + h) 2 + part] = sum over the 64-column half h of
+//                               sum_{i,k} F_part[k, i] F_part[i, k]
+//   c[(w G + g) 2 + part]     = sum_k F_part[k, k]   (the trace of f_g)
+struct ExchOut {
+    float* x = nullptr;
+    float* c = nullptr;
+    int G = 0;       // Cholesky vectors
+    int nw = 0;      // walkers in this product
+    int nhalf = 0;   // 64-column halves per row = 2 x column tiles
+};
+
+// MODE 0: fp32 C.  MODE 1 (split): the two-piece bf16 split of each sum to
+// Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
+// exchange contraction of each 32 x 32 block (ExchOut) instead of C.
+template <int BNT, int MODE>
 __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
-                    int N, int K, long long ldc, int kd, int* __restrict__ err) {
+                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
     using D = Drain<BNT>;
+    constexpr bool SPLIT = MODE == 1;
+    static_assert(MODE != 2 || BNT == 128, "the exchange epilogue takes 128-column tiles");
     constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -383,6 +406,40 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
                 if (++slot == SLOTS) { slot = 0; slot_phase ^= 1; }
             }
             if (!ok) break;
+            if constexpr (MODE == 2) {
+                // this warp's 32 rows are (walker wl, part) rows k = lane of four 32 x 32 blocks;
+                // the thread's 64 columns are the blocks of two Cholesky vectors
+                float* tr = (float*)(smem + STG * D::STAGE + 256) + (warp - D::EW0) * 32 * 33;
+                const int wl = mb * 2 + (q >> 1), part = q & 1;
+                float ex = 0.f;
+#pragma unroll
+                for (int jj = 0; jj < 2; ++jj) {
+                    const int g = (nb * BNT + cb) / 32 + jj;
+#pragma unroll
+                    for (int i = 0; i < 32; i += 2) {
+                        tr[lane * 33 + i] = acc[jj * 16 + i / 2].x;
+                        tr[lane * 33 + i + 1] = acc[jj * 16 + i / 2].y;
+                    }
+                    __syncwarp();
+                    float e2 = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 32; i += 2) {
+                        e2 = fmaf(acc[jj * 16 + i / 2].x, tr[i * 33 + lane], e2);
+                        e2 = fmaf(acc[jj * 16 + i / 2].y, tr[(i + 1) * 33 + lane], e2);
+                    }
+                    ex += e2;
+                    float d = tr[lane * 33 + lane];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+                    if (lane == 0 && wl < xo.nw && g < xo.G) xo.c[((size_t)wl * xo.G + g) * 2 + part] = d;
+                    __syncwarp();
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) ex += __shfl_xor_sync(0xffffffffu, ex, off);
+                if (lane == 0 && wl < xo.nw)
+                    xo.x[((size_t)wl * xo.nhalf + nb * 2 + cb / CW) * 2 + part] = ex;
+                continue;
+            }
             const int row = mb * BM + q * 32 + lane;
             const int col0 = nb * BNT + cb;
             if (row < M && SPLIT) {
@@ -465,24 +522,24 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     return AFQ_OK;
 }
 
-template <int BNT, bool SPLIT>
+template <int BNT, int MODE>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
-                        __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s) {
+                        __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
+                        tc::ExchOut xo = tc::ExchOut{}) {
     using namespace tc;
     static bool attr = false;
+    constexpr int SMEM = Drain<BNT>::SMEM + (MODE == 2 ? XT_BYTES : 0);
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
     AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT));
     if (!attr) {
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Drain<BNT>::SMEM));
+        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
         attr = true;
     }
     const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
     const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    k_gemm_tn_drain<BNT, SPLIT><<<grid, Drain<BNT>::THREADS, Drain<BNT>::SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc,
-                                                                                  kd, err);
-    AFQ_LAUNCHED("k_gemm_tn_drain");
+    k_gemm_tn_drain<BNT, MODE><<<grid, Drain<BNT>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo);
+    AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }
 
@@ -504,7 +561,7 @@ int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, c
                             long long ldc, int* err, cudaStream_t s, int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<128, false>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
+    return launch_drain<128, 0>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
 }
 
 int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb,
@@ -512,7 +569,23 @@ int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long 
                                   int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<128, true>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
+    return launch_drain<128, 1>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
 }
+
+int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
+                            float* x, float* c, int* err, cudaStream_t s) {
+    if (nw <= 0 || G <= 0) return AFQ_OK;
+    AFQ_TRY(drain_prologue(K, 1));
+    const int M = 64 * nw, N = 32 * G;
+    tc::ExchOut xo;
+    xo.x = x;
+    xo.c = c;
+    xo.G = G;
+    xo.nw = nw;
+    xo.nhalf = 2 * ((N + 127) / 128);
+    return launch_drain<128, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, 1, err, s, xo);
+}
+
+int exchange_halves(int G) { return 2 * ((32 * G + 127) / 128); }
 
 }  // namespace afq
