@@ -110,6 +110,18 @@ _SIGS = {
                                    c_uint64, c_int32, P, P, P, P, P, c_size_t, P, c_size_t, P]),
     "afq_grad_backward": (c_int32, [POINTER(afq_problem), POINTER(afq_params), P, c_int32, c_uint64, c_uint64,
                                     c_int32, P, c_size_t, P, P, P, P, c_size_t, P]),
+    "afq_u_workspace": (c_size_t, [POINTER(afq_dims), c_int32]),
+    "afq_overlap_u": (c_int32, [POINTER(afq_dims), P, P, P, P, c_size_t, P]),
+    "afq_force_bias_u": (c_int32, [POINTER(afq_dims), P, P, P, P, P, c_size_t, P]),
+    "afq_energy_u": (c_int32, [POINTER(afq_dims), c_double, P, P, P, P, P, P, c_size_t, P]),
+    "afq_apply_trotter_u": (c_int32, [POINTER(afq_dims), c_int32, c_double, c_int32, P, P, P, P, P, P, c_size_t, P]),
+    "afq_stochastic_reconfiguration_u": (c_int32, [POINTER(afq_dims), P, c_double, P, P, P, P, P, c_size_t, P]),
+    "afq_step_u": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_uint64, c_uint64,
+                             P, c_size_t, P]),
+    "afq_block_u": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_double,
+                              c_uint64, c_uint64, P, P, P, P, c_size_t, P]),
+    "afq_modified_cholesky_workspace": (c_size_t, [c_int32, c_int32]),
+    "afq_modified_cholesky": (c_int32, [c_int32, P, c_double, c_int32, P, POINTER(c_int32), P, c_size_t, P]),
     "afq_mlp_param_count": (c_size_t, [c_int32, c_int32]),
     "afq_mlp_forward": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P]),
     "afq_mlp_train_workspace": (c_size_t, [c_int32, c_int32, c_int32]),

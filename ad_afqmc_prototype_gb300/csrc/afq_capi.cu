@@ -27,8 +27,6 @@ int check_cuda(cudaError_t e, const char* what) {
 }
 
 size_t energy_partial_count(int W, int o, int G);
-int launch_sr_scan_dev(int W, const double* weights, const double* zeta_dev, double* levels, int32_t* idx,
-                       double* avg_out, cudaStream_t s);
 
 static int check_dims(const afq_dims* d, bool need_chol = true) {
     if (!d) return fail(AFQ_E_INVALID_ARGUMENT, "dims is NULL");

@@ -244,6 +244,8 @@ int launch_run_record(const double* e, const double* w, double* es, double* ws, 
 int launch_philox(int64_t count, uint64_t seed, uint64_t counter, int normal, double* out,
                   cudaStream_t s);
 size_t sr_levels_size(int W);
+int launch_sr_scan_dev(int W, const double* weights, const double* zeta_dev, double* levels, int32_t* idx,
+                       double* avg_out, cudaStream_t s);
 
 // k_tc_gemm.cu : C (M x N fp32) = A (M x K bf16) . B (N x K bf16)^T on tcgen05
 int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
@@ -259,7 +261,14 @@ int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long 
 
 // k_walker.cu : Green's function with an optional split (bf16) output
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
-                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s);
+                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s, int ov_square = 1);
+// det(C^H W) per walker (not squared: the unrestricted overlap's per-spin factor)
+int launch_green_det(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                     double2* det_out, double2* green_out, cudaStream_t s);
+// the energy's per-chunk partials (sum c^2, sum exchange) without the finish
+int energy_partial_chunks(int o, int G);
+int launch_energy_partial(int W, int n, int o, int G, const double2* green, const void* rot_chol, int trial_real,
+                          double* partial, cudaStream_t s);
 size_t energy_partial_count(int W, int o, int G);
 int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const double2* green, const double2* rot_h1,
                          const double2* partial, double2* energy, cudaStream_t s);

@@ -25,7 +25,7 @@ template <bool CR, int MA>
 __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __restrict__ mo,
                                                const double2* __restrict__ walkers,
                                                double2* __restrict__ ovlp_out,
-                                               double2* __restrict__ green_out, SplitOut split) {
+                                               double2* __restrict__ green_out, SplitOut split, int ov_square) {
     extern __shared__ double2 sm[];
     double2* m = sm;          // o x o
     double2* inv = sm + o * o;  // o x o
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
         }
         __syncthreads();
     }
-    if (ovlp_out && tid == 0) ovlp_out[w] = cmul(s_det, s_det);
+    if (ovlp_out && tid == 0) ovlp_out[w] = ov_square ? cmul(s_det, s_det) : s_det;
     if (!green_out && !split.ptr) return;
     // G_half[b, i] = sum_a W[i, a] inv[a, b]
     if (green_out) {
@@ -192,14 +192,14 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
 }
 
 int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
-                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s) {
+                       double2* ovlp_out, double2* green_out, SplitOut split, cudaStream_t s, int ov_square) {
     if (W <= 0) return AFQ_OK;
     size_t smem = 2 * (size_t)o * o * sizeof(double2) + (split.ptr ? (size_t)o * o * sizeof(float2) : 0);
     const int ag = 256 / o, ma = (o + ag - 1) / ag;  // rows of m per thread
 #define AFQ_GREEN(CRV, MAV)                                                                  \
     do {                                                                                     \
         AFQ_TRY(set_smem(k_green<CRV, MAV>, smem));                                          \
-        k_green<CRV, MAV><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split); \
+        k_green<CRV, MAV><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, green_out, split, ov_square); \
     } while (0)
 #define AFQ_GREEN_MA(CRV)                \
     do {                                 \
@@ -219,7 +219,12 @@ int launch_green_split(int W, int n, int o, const double2* mo, int trial_real, c
 
 int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
                  double2* ovlp_out, double2* green_out, cudaStream_t s) {
-    return launch_green_split(W, n, o, mo, trial_real, walkers, ovlp_out, green_out, SplitOut{}, s);
+    return launch_green_split(W, n, o, mo, trial_real, walkers, ovlp_out, green_out, SplitOut{}, s, 1);
+}
+
+int launch_green_det(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
+                     double2* det_out, double2* green_out, cudaStream_t s) {
+    return launch_green_split(W, n, o, mo, trial_real, walkers, det_out, green_out, SplitOut{}, s, 0);
 }
 
 // =====================================================================
@@ -558,8 +563,21 @@ size_t energy_partial_count(int W, int o, int G) {  // number of double2
     return (size_t)W * ((G + ng - 1) / ng) * 2;
 }
 
+int energy_partial_chunks(int o, int G) {
+    const int ng = energy_ng(o, G);
+    return (G + ng - 1) / ng;
+}
+
 int launch_energy(int W, int n, int o, int G, double h0, const double2* green, const void* rot_chol,
                   int trial_real, const double2* rot_h1, double* partial_d, double2* energy, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    AFQ_TRY(launch_energy_partial(W, n, o, G, green, rot_chol, trial_real, partial_d, s));
+    return launch_energy_finish(W, n, o, energy_partial_chunks(o, G), h0, green, rot_h1, (const double2*)partial_d,
+                                energy, s);
+}
+
+int launch_energy_partial(int W, int n, int o, int G, const double2* green, const void* rot_chol, int trial_real,
+                          double* partial_d, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     if (o * o > EN_R * EN_THREADS) return fail(AFQ_E_UNSUPPORTED, "energy: nocc=%d > 64", o);
     const int ng = energy_ng(o, G);
@@ -577,7 +595,7 @@ int launch_energy(int W, int n, int o, int G, double h0, const double2* green, c
         k_energy_partial<false><<<grid, EN_THREADS, smem, s>>>(n, o, G, ng, green, rot_chol, partial);
     }
     AFQ_LAUNCHED("k_energy_partial");
-    return launch_energy_finish(W, n, o, nchunk, h0, green, rot_h1, partial, energy, s);
+    return AFQ_OK;
 }
 
 int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const double2* green, const double2* rot_h1,

@@ -436,6 +436,146 @@ def run_blocks(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int,
     return e[:n_blocks], w[:n_blocks]
 
 
+# ------------------------------------------------- unrestricted walkers
+def as_pair(w) -> torch.Tensor:
+    """(2, W, n, o) complex128 device tensor of a (w_up, w_dn) pair; no copy
+    when the two are the halves of one such tensor (as as_pair returns and
+    pair_views splits), else the two are stacked."""
+    if isinstance(w, torch.Tensor):
+        if w.dim() != 4 or w.shape[0] != 2:
+            raise ValueError(f"unrestricted walkers must be (2, W, n, o) or a pair; got {tuple(w.shape)}")
+        return as_device(w, C128)
+    if not (isinstance(w, (tuple, list)) and len(w) == 2):
+        raise ValueError("unrestricted walkers must be a pair (w_up, w_dn)")
+    wu, wd = w
+    if isinstance(wu, torch.Tensor) and isinstance(wd, torch.Tensor) and wu.is_cuda and wd.is_cuda:
+        base = getattr(wu, "_base", None)
+        if (base is not None and base is getattr(wd, "_base", None) and base.dim() == 4 and base.shape[0] == 2
+                and base.dtype == C128 and base.is_contiguous() and wu.data_ptr() == base.data_ptr()
+                and wd.data_ptr() == base[1].data_ptr()):
+            return base
+    wu, wd = as_device(wu, C128), as_device(wd, C128)
+    if wu.shape != wd.shape:
+        raise ValueError(f"up and down walkers differ in shape: {tuple(wu.shape)} vs {tuple(wd.shape)}")
+    return torch.stack([wu, wd]).contiguous()
+
+
+def pair_views(p: torch.Tensor):
+    """(w_up, w_dn) views of a (2, W, n, o) tensor."""
+    return p[0], p[1]
+
+
+def _u_dims(p: torch.Tensor, nchol: int, trial_is_real: bool):
+    return make_dims(p.shape[1], p.shape[2], p.shape[3], nchol, trial_is_real)
+
+
+def _u_ws(d, n_chunks: int = 1):
+    return workspace(_lib.load().afq_u_workspace(ctypes.byref(d), int(n_chunks)))
+
+
+def overlap_u(walkers, mo: torch.Tensor, trial_is_real: bool) -> torch.Tensor:
+    """det(C^H W_up) det(C^H W_dn) per pair (meas/rhf.py:53-57)."""
+    p = as_pair(walkers)
+    d = _u_dims(p, 1, trial_is_real)
+    out = torch.empty((p.shape[1],), dtype=C128, device=p.device)
+    wsp, wsn = _u_ws(d)
+    _lib.call("afq_overlap_u", ctypes.byref(d), ptr(mo), ptr(p), ptr(out), wsp, wsn, stream_ptr())
+    return out
+
+
+def force_bias_u(walkers, mo, rot_chol, trial_is_real: bool) -> torch.Tensor:
+    """L~_flat vec(G_up + G_dn) per pair (meas/rhf.py:60-72)."""
+    p = as_pair(walkers)
+    d = _u_dims(p, rot_chol.shape[0], trial_is_real)
+    out = torch.empty((p.shape[1], rot_chol.shape[0]), dtype=C128, device=p.device)
+    wsp, wsn = _u_ws(d)
+    _lib.call("afq_force_bias_u", ctypes.byref(d), ptr(mo), ptr(rot_chol), ptr(p), ptr(out), wsp, wsn,
+              stream_ptr())
+    return out
+
+
+def energy_u(walkers, h0: float, mo, rot_h1, rot_chol, trial_is_real: bool) -> torch.Tensor:
+    """Local energy of each pair (meas/rhf.py:75-100)."""
+    p = as_pair(walkers)
+    d = _u_dims(p, rot_chol.shape[0], trial_is_real)
+    out = torch.empty((p.shape[1],), dtype=C128, device=p.device)
+    wsp, wsn = _u_ws(d)
+    _lib.call("afq_energy_u", ctypes.byref(d), float(h0), ptr(mo), ptr(rot_h1), ptr(rot_chol), ptr(p), ptr(out),
+              wsp, wsn, stream_ptr())
+    return out
+
+
+def apply_trotter_u(walkers, shifted_fields, chol, exp_h1_half, sqrt_dt: float, n_terms: int,
+                    n_chunks: int = 1) -> torch.Tensor:
+    """Both spins propagated with the same V (prop/chol_afqmc_ops.py:118-183);
+    returns a new (2, W, n, o) tensor."""
+    p = as_pair(walkers)
+    xs = as_device(shifted_fields, C128)
+    d = _u_dims(p, chol.shape[0], True)
+    out = torch.empty_like(p)
+    wsp, wsn = _u_ws(d, n_chunks)
+    _lib.call("afq_apply_trotter_u", ctypes.byref(d), int(n_terms), float(sqrt_dt), int(n_chunks), ptr(chol),
+              ptr(exp_h1_half), ptr(p), ptr(xs), ptr(out), wsp, wsn, stream_ptr())
+    return out
+
+
+def stochastic_reconfiguration_u(walkers, weights, zeta: float):
+    """Comb with one set of indices for both spins (walkers.py:243-265).
+    Returns ((2, W, n, o), weights, idx)."""
+    p = as_pair(walkers)
+    w = as_device(weights, F64)
+    d = _u_dims(p, 1, True)
+    out = torch.empty_like(p)
+    wout = torch.empty_like(w)
+    idx = torch.empty((p.shape[1],), dtype=torch.int32, device=p.device)
+    wsp, wsn = _u_ws(d)
+    _lib.call("afq_stochastic_reconfiguration_u", ctypes.byref(d), ptr(w), float(zeta), ptr(p), ptr(out),
+              ptr(wout), ptr(idx), wsp, wsn, stream_ptr())
+    return out, wout, idx
+
+
+def step_u(prob: Problem, params, st: DeviceState, seed: int, counter: int, fields=None):
+    """One afqmc_step of unrestricted walkers (st.walkers (2, W, n, o)), in place."""
+    W = st.walkers.shape[1]
+    if fields is not None:
+        fields = as_device(fields, F64)
+        if fields.shape != (W, prob.nchol):
+            raise ValueError("fields shape mismatch")
+    pb = prob.c()
+    p = make_params(params)
+    wsp, wsn = _u_ws(pb.dims, int(params.n_chunks))
+    cs = st.c()
+    _lib.call("afq_step_u", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), ptr(fields),
+              int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), wsp, wsn, stream_ptr())
+
+
+def block_u(prob: Problem, params, st: DeviceState, seed: int, counter: int, fields=None, zeta=None,
+            return_idx: bool = False):
+    """One afqmc_block of unrestricted walkers, in place.  Returns device
+    (energy, weight[, idx])."""
+    W = st.walkers.shape[1]
+    if fields is not None:
+        fields = as_device(fields, F64)
+        if fields.shape != (params.n_prop_steps, W, prob.nchol):
+            raise ValueError("fields must be (n_prop_steps, n_walkers, nchol)")
+    pb = prob.c()
+    p = make_params(params)
+    wsp, wsn = _u_ws(pb.dims, int(params.n_chunks))
+    cs = st.c()
+    e = torch.empty((1,), dtype=F64, device=st.walkers.device)
+    wsum = torch.empty((1,), dtype=F64, device=st.walkers.device)
+    idx = torch.empty((W,), dtype=torch.int32, device=st.walkers.device) if return_idx else None
+    z = -1.0 if zeta is None else float(zeta)
+    if zeta is not None and not (0.0 <= z < 1.0):
+        raise ValueError("zeta must be in [0, 1)")
+    _lib.call("afq_block_u", ctypes.byref(pb), ctypes.byref(p), ctypes.byref(cs), ptr(fields), z,
+              int(seed) & (2**64 - 1), int(counter) & (2**64 - 1), ptr(e), ptr(wsum), ptr(idx), wsp, wsn,
+              stream_ptr())
+    if return_idx:
+        return e, wsum, idx.long()
+    return e, wsum
+
+
 # ------------------------------------------------- differentiated energy
 def grad_forward(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int, counter: int,
                  checkpoint_blocks: int, sr_fixed: Optional[torch.Tensor] = None):

@@ -13,7 +13,7 @@ from .. import engine
 from ..core.ops import k_energy, k_force_bias, meas_ops
 from ..core.system import system
 from ..ham.chol import ham_chol
-from ..trial.rhf import overlap_r, rhf_trial
+from ..trial.rhf import overlap_r, overlap_u, rhf_trial
 
 
 @dataclass(frozen=True)
@@ -63,12 +63,47 @@ def energy_kernel_r(walker, ham_data: ham_chol, meas_ctx: rhf_meas_ctx, trial_da
 energy_kernel_r.batched = _energy_batched
 
 
+def _pair1(walker):
+    wu, wd = walker
+    return (torch.as_tensor(wu)[None], torch.as_tensor(wd)[None])
+
+
+def _fb_u_batched(walkers, _ham, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    return engine.force_bias_u(walkers, trial_data.mo_coeff, meas_ctx.rot_chol, trial_data.is_real)
+
+
+def force_bias_kernel_u(walker, _ham: Any, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    """L~_flat vec(G_up + G_dn) for one pair (meas/rhf.py:60-72)."""
+    return _fb_u_batched(_pair1(walker), _ham, meas_ctx, trial_data)[0]
+
+
+force_bias_kernel_u.batched = _fb_u_batched
+
+
+def _energy_u_batched(walkers, ham_data: ham_chol, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    return engine.energy_u(walkers, ham_data.h0, trial_data.mo_coeff, meas_ctx.rot_h1, meas_ctx.rot_chol,
+                           trial_data.is_real)
+
+
+def energy_kernel_u(walker, ham_data: ham_chol, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    """h0 + e1 + [sum_g (c_up + c_dn)^2 - exc_up - exc_dn] / 2 for one pair
+    (meas/rhf.py:75-100)."""
+    return _energy_u_batched(_pair1(walker), ham_data, meas_ctx, trial_data)[0]
+
+
+energy_kernel_u.batched = _energy_u_batched
+
+
 def make_rhf_meas_ops(sys: system) -> meas_ops:
-    """meas/rhf.py:153-176; only restricted walkers run on the CUDA engine."""
+    """meas/rhf.py:153-176; restricted and unrestricted walkers run on the
+    CUDA engine (generalized walkers are not built)."""
     wk = sys.walker_kind.lower()
     if wk == "restricted":
         return meas_ops(overlap=overlap_r, build_meas_ctx=build_meas_ctx,
                         kernels={k_force_bias: force_bias_kernel_r, k_energy: energy_kernel_r})
-    if wk in ("unrestricted", "generalized"):
-        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    if wk == "unrestricted":
+        return meas_ops(overlap=overlap_u, build_meas_ctx=build_meas_ctx,
+                        kernels={k_force_bias: force_bias_kernel_u, k_energy: energy_kernel_u})
+    if wk == "generalized":
+        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
     raise ValueError(f"unknown walker_kind: {sys.walker_kind}")

@@ -18,8 +18,8 @@ from .. import walkers as wk
 from ..core.ops import k_energy, k_force_bias, meas_ops
 from ..core.system import system
 from ..ham.chol import ham_chol
-from ..meas.rhf import energy_kernel_r, force_bias_kernel_r, rhf_meas_ctx
-from ..trial.rhf import overlap_r, rhf_trial
+from ..meas.rhf import energy_kernel_r, energy_kernel_u, force_bias_kernel_r, force_bias_kernel_u, rhf_meas_ctx
+from ..trial.rhf import overlap_r, overlap_u, rhf_trial
 from .chol_afqmc_ops import chol_afqmc_ctx, chol_afqmc_ops
 from .types import PRNGKey, afqmc_params, prop_state, split
 
@@ -35,7 +35,10 @@ def init_prop_state(*, sys: system, n_walkers: int, seed: int, ham_data: ham_cho
     weights = torch.ones((n_walkers,), dtype=engine.F64, device=engine.device())
     if initial_walkers is None:
         initial_walkers = wk.init_walkers(sys=sys, rdm1=trial_ops_.get_rdm1(trial_data), n_walkers=n_walkers)
-    walkers = engine.as_device(initial_walkers, engine.C128)
+    if isinstance(initial_walkers, (tuple, list)):
+        walkers = engine.pair_views(engine.as_pair(initial_walkers))
+    else:
+        walkers = engine.as_device(initial_walkers, engine.C128)
     overlaps = wk.apply_chunked(walkers, trial_ops_.overlap, 1, trial_data=trial_data)
     if initial_e_estimate is not None:
         e_est = engine.as_device(torch.as_tensor(initial_e_estimate).reshape(()), engine.F64)
@@ -48,23 +51,30 @@ def init_prop_state(*, sys: system, n_walkers: int, seed: int, ham_data: ham_cho
                       pop_control_ene_shift=e_est.clone(), e_estimate=e_est)
 
 
+_KIND_OPS = {"restricted": (overlap_r, force_bias_kernel_r, energy_kernel_r),
+             "unrestricted": (overlap_u, force_bias_kernel_u, energy_kernel_u)}
+
+
 def engine_problem(*, params, ham_data, trial_data, meas_ops, prop_ops, prop_ctx, meas_ctx, n_walkers: int,
-                   need_energy: bool = False) -> Optional[engine.Problem]:
+                   need_energy: bool = False, walker_kind: str = "restricted") -> Optional[engine.Problem]:
     """The fused-engine view of the arguments, or None when any op is not
-    one of this package's RHF/Cholesky ops."""
+    one of this package's RHF/Cholesky ops for `walker_kind`."""
     if not isinstance(trial_data, rhf_trial) or not isinstance(meas_ctx, rhf_meas_ctx):
         return None
     if not isinstance(prop_ctx, chol_afqmc_ctx) or not isinstance(ham_data, ham_chol):
         return None
-    if meas_ops.overlap is not overlap_r or meas_ops.kernels.get(k_force_bias) is not force_bias_kernel_r:
+    ov, fb, en = _KIND_OPS[walker_kind]
+    if meas_ops.overlap is not ov or meas_ops.kernels.get(k_force_bias) is not fb:
         return None
-    if need_energy and meas_ops.kernels.get(k_energy) is not energy_kernel_r:
+    if need_energy and meas_ops.kernels.get(k_energy) is not en:
         return None
     if getattr(prop_ops.apply_trotter, "ham_data", None) is not ham_data:
         return None
     prec = _PREC.get(str(getattr(params, "precision", "fp64")).lower())
     if prec is None:
         raise ValueError(f"unknown precision {params.precision!r}; expected 'fp64', 'mixed' or 'mixed_fast'")
+    if walker_kind == "unrestricted" and prec != _lib.AFQ_PREC_FP64:
+        raise ValueError("unrestricted walkers run the binary64 form (precision='fp64')")
     lowp = None
     if prec != _lib.AFQ_PREC_FP64:
         # cached on the measurement context: it depends on chol, rot_chol and the precision only
@@ -87,7 +97,12 @@ def device_state(state: prop_state, inplace: bool) -> engine.DeviceState:
     def own(t, dtype):
         t = engine.as_device(t, dtype)
         return t if inplace else t.clone()
-    return engine.DeviceState(walkers=own(state.walkers, engine.C128), weights=own(state.weights, engine.F64),
+    if wk.is_unrestricted(state.walkers):
+        p = engine.as_pair(state.walkers)
+        walk = p if inplace else p.clone()
+    else:
+        walk = own(state.walkers, engine.C128)
+    return engine.DeviceState(walkers=walk, weights=own(state.weights, engine.F64),
                               overlaps=own(state.overlaps, engine.C128),
                               pop_shift=own(torch.as_tensor(state.pop_control_ene_shift).reshape(1), engine.F64),
                               e_estimate=engine.as_device(torch.as_tensor(state.e_estimate).reshape(1), engine.F64))
@@ -101,6 +116,17 @@ def afqmc_step(state: prop_state, *, params: afqmc_params, ham_data: ham_chol, t
     key, subkey = split(state.rng_key)
     seed, counter = int(subkey[0]), int(subkey[1])
     nw = wk.n_walkers(state.walkers)
+    if wk.is_unrestricted(state.walkers):
+        prob = engine_problem(params=params, ham_data=ham_data, trial_data=trial_data, meas_ops=meas_ops,
+                              prop_ops=prop_ops, prop_ctx=prop_ctx, meas_ctx=meas_ctx, n_walkers=nw,
+                              walker_kind="unrestricted")
+        if prob is None:
+            raise ValueError("unrestricted walkers run with this package's RHF/Cholesky ops only")
+        st = device_state(state, inplace)
+        engine.step_u(prob, params, st, seed, counter, fields=fields)
+        return prop_state(walkers=engine.pair_views(st.walkers), weights=st.weights, overlaps=st.overlaps,
+                          rng_key=key, pop_control_ene_shift=st.pop_shift.reshape(()),
+                          e_estimate=st.e_estimate.reshape(()))
     prob = engine_problem(params=params, ham_data=ham_data, trial_data=trial_data, meas_ops=meas_ops,
                           prop_ops=prop_ops, prop_ctx=prop_ctx, meas_ctx=meas_ctx, n_walkers=nw)
     if prob is not None:

@@ -32,6 +32,20 @@ def afqmc_block(state: prop_state, *, sys: system, params: afqmc_params, ham_dat
     nw = wk.n_walkers(state.walkers)
     seed, counter = int(state.rng_key[0]), int(state.rng_key[1])
     key = torch.tensor([seed, counter + params.n_prop_steps + 1], dtype=torch.int64)
+    if sys.walker_kind.lower() == "unrestricted":
+        if cv is not None:
+            raise ValueError("the control-variate measurement needs restricted walkers")
+        prob = engine_problem(params=params, ham_data=ham_data, trial_data=trial_data, meas_ops=meas_ops,
+                              prop_ops=prop_ops, prop_ctx=prop_ctx, meas_ctx=meas_ctx, n_walkers=nw,
+                              need_energy=True, walker_kind="unrestricted")
+        if prob is None:
+            raise ValueError("unrestricted walkers run with this package's RHF/Cholesky ops only")
+        st = device_state(state, inplace)
+        e, wsum = engine.block_u(prob, params, st, seed, counter, fields=fields, zeta=zeta)
+        new = prop_state(walkers=engine.pair_views(st.walkers), weights=st.weights, overlaps=st.overlaps,
+                         rng_key=key, pop_control_ene_shift=st.pop_shift.reshape(()),
+                         e_estimate=st.e_estimate.reshape(()))
+        return new, block_obs(scalars={"energy": e.reshape(()), "weight": wsum.reshape(())})
     if sys.walker_kind.lower() == "restricted":
         prob = engine_problem(params=params, ham_data=ham_data, trial_data=trial_data, meas_ops=meas_ops,
                               prop_ops=prop_ops, prop_ctx=prop_ctx, meas_ctx=meas_ctx, n_walkers=nw,

@@ -52,8 +52,27 @@ def make_chol_afqmc_ops(ham_data: ham_chol, walker_kind: str) -> chol_afqmc_ops:
         raise ValueError("ham_data.basis='generalized' requires walker_kind='generalized'")
     if walker_kind not in ("restricted", "unrestricted", "generalized"):
         raise ValueError(f"unknown walker_kind: {walker_kind}")
-    if ham_data.basis != "restricted" or walker_kind != "restricted":
-        raise ValueError("the CUDA engine propagates restricted walkers with a restricted-basis Hamiltonian only")
+    if ham_data.basis != "restricted" or walker_kind == "generalized":
+        raise ValueError("the CUDA engine propagates restricted and unrestricted walkers with a restricted-basis "
+                         "Hamiltonian only")
+
+    if walker_kind == "unrestricted":
+        def apply_trotter_u_batched(walkers, fields, ctx: chol_afqmc_ctx, n_terms: int, n_chunks: int = 1):
+            """Both spins with the same V (:118-183); returns the (up, down) pair."""
+            p = engine.apply_trotter_u(walkers, fields, ham_data.chol, ctx.exp_h1_half, float(ctx.sqrt_dt),
+                                       int(n_terms), n_chunks=n_chunks)
+            return engine.pair_views(p)
+
+        def apply_trotter_u(w, field, ctx: chol_afqmc_ctx, n_terms: int):
+            wu, wd = w
+            f = torch.as_tensor(field)[None].to(torch.complex128)
+            pu, pd = apply_trotter_u_batched((torch.as_tensor(wu)[None], torch.as_tensor(wd)[None]), f, ctx,
+                                             n_terms)
+            return (pu[0], pd[0])
+
+        apply_trotter_u.batched = apply_trotter_u_batched
+        apply_trotter_u.ham_data = ham_data
+        return chol_afqmc_ops(n_fields_, build_prop_ctx, apply_trotter_u)
 
     def apply_trotter_batched(walkers, fields, ctx: chol_afqmc_ctx, n_terms: int, n_chunks: int = 1):
         """E_half exp(i sqrt_dt V(x)) E_half W for a batch (:173-183)."""

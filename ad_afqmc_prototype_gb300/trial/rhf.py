@@ -55,13 +55,29 @@ def overlap_r(walker, trial_data: rhf_trial):
 overlap_r.batched = _overlap_batched
 
 
+def _overlap_u_batched(walkers, trial_data: rhf_trial):
+    return engine.overlap_u(walkers, trial_data.mo_coeff, trial_data.is_real)
+
+
+def overlap_u(walker, trial_data: rhf_trial):
+    """det(C^H W_up) det(C^H W_dn) for one pair (trial/rhf.py:40-44)."""
+    wu, wd = walker
+    return _overlap_u_batched((torch.as_tensor(wu)[None], torch.as_tensor(wd)[None]), trial_data)[0]
+
+
+overlap_u.batched = _overlap_u_batched
+
+
 def make_rhf_trial_ops(sys: system) -> trial_ops:
-    """trial/rhf.py:56-71; only restricted walkers run on the CUDA engine."""
+    """trial/rhf.py:56-71; restricted and unrestricted walkers run on the
+    CUDA engine (generalized walkers are not built)."""
     if sys.nup != sys.ndn:
         raise ValueError("RHF requires nelec[0] == nelec[1].")
     wk = sys.walker_kind.lower()
     if wk == "restricted":
         return trial_ops(overlap=overlap_r, get_rdm1=get_rdm1)
-    if wk in ("unrestricted", "generalized"):
-        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    if wk == "unrestricted":
+        return trial_ops(overlap=overlap_u, get_rdm1=get_rdm1)
+    if wk == "generalized":
+        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
     raise ValueError(f"unknown walker_kind: {sys.walker_kind}")

@@ -1,5 +1,10 @@
 """Walker batches and population operations (walkers.py:1-265 of the
-reference), restricted walkers on the CUDA engine."""
+reference), restricted and unrestricted walkers on the CUDA engine.
+
+Unrestricted walkers are the reference's pair (w_up, w_dn); this package
+returns the pair as the two halves of one (2, W, n, o) device tensor
+(engine.as_pair / engine.pair_views), which the engine reads without a
+copy."""
 from __future__ import annotations
 
 from typing import Any, Callable
@@ -30,8 +35,20 @@ def init_walkers(sys: system, rdm1, n_walkers: int):
         dm_tot = engine.as_device(rdm1[0] + rdm1[1], engine.C128)
         w0 = _natorbs(dm_tot, sys.nup).to(engine.C128)
         return w0.unsqueeze(0).expand(n_walkers, *w0.shape).contiguous()
-    if wk in ("unrestricted", "generalized"):
-        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    if wk == "unrestricted":
+        if rdm1.dim() != 3 or rdm1.shape[0] != 2:
+            raise ValueError("For walker_kind in {'restricted','unrestricted'}, rdm1 must be spin-block "
+                             "(2, norb, norb).")
+        if sys.nup != sys.ndn:
+            raise ValueError("unrestricted walkers with the RHF trial need nelec[0] == nelec[1]")
+        dev_dm = engine.as_device(rdm1, engine.C128)
+        wu = _natorbs(dev_dm[0], sys.nup).to(engine.C128)
+        wd = _natorbs(dev_dm[1], sys.ndn).to(engine.C128)
+        pair = torch.stack([wu.unsqueeze(0).expand(n_walkers, *wu.shape),
+                            wd.unsqueeze(0).expand(n_walkers, *wd.shape)]).contiguous()
+        return engine.pair_views(pair)
+    if wk == "generalized":
+        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
     raise ValueError(f"unknown walker_kind: {wk}")
 
 
@@ -56,6 +73,12 @@ def _run(fn: Callable, chunk_args, extra_args, kwargs):
     return torch.func.vmap(lambda *xs: fn(*xs, *extra_args, **kwargs))(*chunk_args)
 
 
+def _take(w, a: int, b: int):
+    if is_unrestricted(w):
+        return (w[0][a:b], w[1][a:b])
+    return w[a:b]
+
+
 def apply_chunked(w, apply_fn: Callable, n_chunks: int, *args, **kwargs):
     """apply_fn(walker_i, *args) over all walkers, in n_chunks sequential
     chunks (walkers.py:94-127).  Engine kernels run a chunk per launch."""
@@ -63,7 +86,7 @@ def apply_chunked(w, apply_fn: Callable, n_chunks: int, *args, **kwargs):
     if n_chunks == 1:
         return _run(apply_fn, (w,), args, kwargs)
     cs = _chunk_size(nw, n_chunks)
-    outs = [_run(apply_fn, (w[i * cs:(i + 1) * cs],), args, kwargs) for i in range(n_chunks)]
+    outs = [_run(apply_fn, (_take(w, i * cs, (i + 1) * cs),), args, kwargs) for i in range(n_chunks)]
     return torch.cat(outs, dim=0)
 
 
@@ -73,20 +96,29 @@ def apply_chunked_prop(w, fields, prop_fn: Callable, n_chunks: int, *args, **kwa
     if n_chunks == 1:
         return _run(prop_fn, (w, fields), args, kwargs)
     cs = _chunk_size(nw, n_chunks)
-    outs = [_run(prop_fn, (w[i * cs:(i + 1) * cs], fields[i * cs:(i + 1) * cs]), args, kwargs)
+    outs = [_run(prop_fn, (_take(w, i * cs, (i + 1) * cs), fields[i * cs:(i + 1) * cs]), args, kwargs)
             for i in range(n_chunks)]
+    if is_unrestricted(w):
+        pair = torch.cat([engine.as_pair(o) for o in outs], dim=1).contiguous()
+        return engine.pair_views(pair)
     return torch.cat(outs, dim=0)
 
 
 def orthogonalize(w, walker_kind: str):
-    """QR with diag(R) >= 0; returns (Q, det(R)^2) for restricted walkers
-    (walkers.py:183-203)."""
+    """QR with diag(R) >= 0 (walkers.py:183-203); returns (Q, det(R)^2) for
+    restricted walkers, ((Q_up, Q_dn), det(R_up) det(R_dn)) for
+    unrestricted ones."""
     wk = walker_kind.lower()
     if wk == "restricted":
         q, det_r = engine.orthogonalize(w)
         return q, det_r * det_r
-    if wk in ("unrestricted", "generalized"):
-        raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+    if wk == "unrestricted":
+        p = engine.as_pair(w)
+        W = p.shape[1]
+        q, det_r = engine.orthogonalize(p.reshape(2 * W, *p.shape[2:]))
+        return engine.pair_views(q.reshape(p.shape)), det_r[:W] * det_r[W:]
+    if wk == "generalized":
+        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
     raise ValueError(f"unknown walker_kind: {walker_kind}")
 
 
@@ -118,9 +150,12 @@ def _sr_indices(weights, zeta: float, n_walkers: int):
 def stochastic_reconfiguration(w, weights, zeta: float, walker_kind: str):
     """walkers.py:243-265: returns (walkers, weights)."""
     wk = walker_kind.lower()
+    if wk == "unrestricted":
+        p, weights_new, _ = engine.stochastic_reconfiguration_u(w, weights, float(zeta))
+        return engine.pair_views(p), weights_new
     if wk != "restricted":
-        if wk in ("unrestricted", "generalized"):
-            raise ValueError(f"walker_kind '{wk}' is not supported by the CUDA engine (restricted only)")
+        if wk == "generalized":
+            raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
         raise ValueError(f"unknown walker_kind: {walker_kind}")
     w_new, weights_new, _ = engine.stochastic_reconfiguration(w, weights, float(zeta))
     return w_new, weights_new

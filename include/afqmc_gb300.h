@@ -393,6 +393,53 @@ int afq_grad_backward(const afq_problem* pb, const afq_params* p, const double* 
                       size_t tape_bytes, const double* energies_bar, const double* weights_bar, double* h1_bar,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- unrestricted walkers (walker_kind "unrestricted" with the RHF trial:
+ * meas/rhf.py:53-100, prop/chol_afqmc_ops.py:118-183, walkers.py:183-265) ---
+ *
+ * Walkers (2, W, n, o) complex128: all up-spin walkers, then all down-spin
+ * walkers (the reference's tuple (w_up, w_dn) stored contiguously);
+ * d->n_walkers = W pairs; binary64 form.  Overlap det(C^H W_up) det(C^H
+ * W_dn); force bias L~ vec(G_up + G_dn); energy h0 + sum (G_up + G_dn) o
+ * rot_h1 + [sum_g (c_up + c_dn)^2 - exc_up - exc_dn] / 2; Trotter with one
+ * V_w for both spins; comb indices shared by both spins.  afq_orthogonalize
+ * with n_walkers = 2W orthonormalises both spins.  Fields (W, G) as for
+ * restricted walkers.  workspace: afq_u_workspace bytes for every call. */
+size_t afq_u_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_overlap_u(const afq_dims* d, const double* mo_coeff, const double* walkers, double* overlaps,
+                  void* workspace, size_t workspace_bytes, void* stream);
+int afq_force_bias_u(const afq_dims* d, const double* mo_coeff, const double* rot_chol, const double* walkers,
+                     double* force_bias, void* workspace, size_t workspace_bytes, void* stream);
+int afq_energy_u(const afq_dims* d, double h0, const double* mo_coeff, const double* rot_h1,
+                 const double* rot_chol, const double* walkers, double* energy, void* workspace,
+                 size_t workspace_bytes, void* stream);
+int afq_apply_trotter_u(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_t n_chunks,
+                        const double* chol, const double* exp_h1_half, const double* walkers,
+                        const double* shifted_fields, double* walkers_out, void* workspace,
+                        size_t workspace_bytes, void* stream);
+int afq_stochastic_reconfiguration_u(const afq_dims* d, const double* weights, double zeta,
+                                     const double* walkers, double* walkers_out, double* weights_out,
+                                     int32_t* idx, void* workspace, size_t workspace_bytes, void* stream);
+int afq_step_u(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
+               uint64_t seed, uint64_t counter, void* workspace, size_t workspace_bytes, void* stream);
+int afq_block_u(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
+                double zeta, uint64_t seed, uint64_t counter, double* block_energy, double* block_weight,
+                int32_t* sr_idx, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- integrals (integrals.py:3-46) ---------------------------------------
+ *
+ * modified_cholesky: pivoted Cholesky vectors of the 4-fold symmetric ERI
+ * matrix mat (size x size device f64, size = n (n + 1) / 2, pairs i >= j in
+ * row-major triangle order), the reference's loop and stopping rule
+ * (|residual pivot| > max_error), at most min(size, max_vectors) - 1 vectors
+ * kept.  chol_out (device, max_vectors x n x n f64) receives the *nchol_out
+ * vectors unpacked to symmetric n x n matrices.  Synchronises the stream
+ * (the loop's exit is read back every 32 iterations).
+ * workspace: afq_modified_cholesky_workspace bytes. */
+size_t afq_modified_cholesky_workspace(int32_t size, int32_t max_vectors);
+int afq_modified_cholesky(int32_t size, const double* mat, double max_error, int32_t max_vectors,
+                          double* chol_out, int32_t* nchol_out, void* workspace, size_t workspace_bytes,
+                          void* stream);
+
 /* ---- tracing (no counterpart in the reference, which only times blocks
  * with time.perf_counter, driver.py:83-147) --------------------------------- */
 

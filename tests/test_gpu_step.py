@@ -216,9 +216,9 @@ def test_generic_block_path_equals_fused(api):
 
 
 def test_api_errors(api):
-    sys_u = api["system"](norb=4, nelec=(2, 2), walker_kind="unrestricted")
+    sys_g = api["system"](norb=4, nelec=(2, 2), walker_kind="generalized")
     with pytest.raises(ValueError):
-        api["make_rhf_meas_ops"](sys_u)
+        api["make_rhf_meas_ops"](sys_g)
     with pytest.raises(ValueError):
         api["make_rhf_trial_ops"](api["system"](norb=4, nelec=(2, 1), walker_kind="restricted"))
     with pytest.raises(ValueError):
