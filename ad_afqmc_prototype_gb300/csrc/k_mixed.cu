@@ -507,9 +507,15 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
     if (tid == 0) s_det = make_double2(1.0, 0.0);
     __syncthreads();
 
-    // binary64 LU with partial pivoting: det(m) only
-    for (int k = 0; k < o; ++k) {
-        if (wid == 0) {
+    // One pivot loop for both factorisations of m, three barriers a step:
+    //   binary64 LU with partial pivoting (det(m) only), pivots by warp 0;
+    //   fp32 Gauss-Jordan inverse of the copy, pivots by warp 1; its pivot
+    //   row k is scaled by 1/pivot in the next step's first phase (rows
+    //   r != k eliminate with the unscaled row times 1/pivot meanwhile).
+    __shared__ int s_piv2;
+    __shared__ float2 s_rpf2[2];
+    for (int k = 0; k <= o; ++k) {
+        if (k < o && wid == 0) {
             double best = -1.0;
             int bi = k;
             for (int r = k + lane; r < o; r += 32) {
@@ -529,30 +535,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
                 s_det = (bi != k) ? make_double2(-d.x, -d.y) : d;
                 s_rp = cdiv(make_double2(1.0, 0.0), piv);
             }
-        }
-        __syncthreads();
-        const int p = s_piv;
-        if (p != k)
-            for (int j = tid; j < o; j += blockDim.x) {
-                const double2 t = m[k * o + j];
-                m[k * o + j] = m[p * o + j];
-                m[p * o + j] = t;
-            }
-        __syncthreads();
-        const double2 rp = s_rp;
-        const int rem = o - k - 1;
-        for (int e = tid; e < rem * rem; e += blockDim.x) {
-            const int r = k + 1 + e / rem, j = k + 1 + e % rem;
-            const double2 l = cmul(m[r * o + k], rp);
-            m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
-        }
-        __syncthreads();
-    }
-    if (tid == 0 && ovlp_out) ovlp_out[w] = cmul(s_det, s_det);
-
-    // fp32 Gauss-Jordan inverse of the copy
-    for (int k = 0; k < o; ++k) {
-        if (wid == 0) {
+        } else if (k < o && wid == 1) {
             float best = -1.f;
             int bi = k;
             for (int r = k + lane; r < o; r += 32) {
@@ -567,44 +550,63 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
             if (lane == 0) {
-                s_piv = bi;
+                s_piv2 = bi;
                 const float2 v = mf[bi * o + k];
                 const float den = v.x * v.x + v.y * v.y;
-                s_rpf = make_float2(v.x / den, -v.y / den);
+                s_rpf2[k & 1] = make_float2(v.x / den, -v.y / den);
             }
-        }
-        __syncthreads();
-        const int p = s_piv;
-        if (p != k)
-            for (int j = tid; j < 2 * o; j += blockDim.x) {
+        } else if (k > 0 && tid >= 64) {
+            // scale the previous Gauss-Jordan pivot row (columns > k-1 of the copy, all of the inverse)
+            const float2 rp = s_rpf2[(k - 1) & 1];
+            for (int j = tid - 64; j < 2 * o; j += blockDim.x - 64) {
                 float2* X = j < o ? mf : invf;
                 const int jj = j < o ? j : j - o;
-                const float2 t = X[k * o + jj];
-                X[k * o + jj] = X[p * o + jj];
-                X[p * o + jj] = t;
+                if (j < o && jj <= k - 1) continue;
+                const float2 v = X[(k - 1) * o + jj];
+                X[(k - 1) * o + jj] = make_float2(v.x * rp.x - v.y * rp.y, v.x * rp.y + v.y * rp.x);
             }
-        __syncthreads();
-        const float2 rp = s_rpf;
-        for (int j = tid; j < 2 * o; j += blockDim.x) {
-            float2* X = j < o ? mf : invf;
-            const int jj = j < o ? j : j - o;
-            if (j < o && jj <= k) continue;
-            const float2 v = X[k * o + jj];
-            X[k * o + jj] = make_float2(v.x * rp.x - v.y * rp.y, v.x * rp.y + v.y * rp.x);
         }
         __syncthreads();
+        if (k == o) break;
+        const int p = s_piv, p2 = s_piv2;
+        for (int j = tid; j < 3 * o; j += blockDim.x) {
+            if (j < o) {
+                if (p != k) {
+                    const double2 t = m[k * o + j];
+                    m[k * o + j] = m[p * o + j];
+                    m[p * o + j] = t;
+                }
+            } else if (p2 != k) {
+                float2* X = j < 2 * o ? mf : invf;
+                const int jj = j < 2 * o ? j - o : j - 2 * o;
+                const float2 t = X[k * o + jj];
+                X[k * o + jj] = X[p2 * o + jj];
+                X[p2 * o + jj] = t;
+            }
+        }
+        __syncthreads();
+        const double2 rp = s_rp;
+        const float2 rpf = s_rpf2[k & 1];
+        const int rem = o - k - 1;
+        for (int e = tid; e < rem * rem; e += blockDim.x) {
+            const int r = k + 1 + e / rem, j = k + 1 + e % rem;
+            const double2 l = cmul(m[r * o + k], rp);
+            m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
+        }
         for (int e = tid; e < o * 2 * o; e += blockDim.x) {
             const int r = e / (2 * o), j = e % (2 * o);
             if (r == k) continue;
-            const float2 f = mf[r * o + k];
             float2* X = j < o ? mf : invf;
             const int jj = j < o ? j : j - o;
             if (j < o && jj <= k) continue;
+            const float2 f0 = mf[r * o + k];
+            const float2 f = make_float2(f0.x * rpf.x - f0.y * rpf.y, f0.x * rpf.y + f0.y * rpf.x);
             const float2 v = X[k * o + jj], x = X[r * o + jj];
             X[r * o + jj] = make_float2(x.x - (f.x * v.x - f.y * v.y), x.y - (f.x * v.y + f.y * v.x));
         }
         __syncthreads();
     }
+    if (tid == 0 && ovlp_out) ovlp_out[w] = cmul(s_det, s_det);
 
     // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
     __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;

@@ -118,10 +118,10 @@ def _r64(x):
 
 def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
     """(work per launch, pipe) of each timed phase.  FP64 form: algorithmic
-    real flops.  Mixed forms: the tensor-core phases count the flops the
-    tensor cores execute on the bf16 split operands (2 M N K with K the split
-    row length), the exchange reduction the bytes of F it must read, the
-    others algorithmic flops on their pipe."""
+    real flops.  Mixed forms: the tensor-core phases count the flops of the
+    bf16 split operands (2 M N K with K the split row length; the energy GEMM
+    without the padding of its exchange-fused layout), the exchange step the
+    bytes it must read, the others algorithmic flops on their pipe."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
     work = {
         "vbuild_gemm": (4.0 * G * n * n * W, "fp64"),
@@ -138,7 +138,10 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
         work["fb_gemm"] = (2.0 * (2 * W) * G * _r64(ks * o * n), "tensor")
         del work["energy"]  # composite phase: e_green_rows + e_gemm + e_exchange
         work["e_gemm"] = (2.0 * (G * o) * (2 * o * W) * _r64(ks * n), "tensor")
-        work["e_exchange"] = (4.0 * (2 * o * W) * (G * o), "hbm")
+        if 24 < o <= 32:  # exchange contracted in the GEMM's epilogue: the finish reads its fp32 sums
+            work["e_exchange"] = (4.0 * W * (2 * 2 * ((32 * G + 127) // 128) + 2 * G), "hbm")
+        else:  # the reduction reads F (G o x 2 o W fp32)
+            work["e_exchange"] = (4.0 * (2 * o * W) * (G * o), "hbm")
         work["trotter"] = ((48.0 + 8.0) * n * n * o * W, "fp32")
     return work
 
