@@ -902,6 +902,8 @@ int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, doubl
     if (o > 64) return fail(AFQ_E_UNSUPPORTED, "qr: nocc=%d > 64", o);
     const size_t smem = (size_t)o * o * (sizeof(double2) + sizeof(float4)) + (size_t)((o + 1) & ~1) * sizeof(float2) +
                         2 * (size_t)(n | 1) * o * sizeof(float2);
+    // walkers whose double-float copy does not fit in shared memory: the binary64 Householder QR
+    if (smem > 220 * 1024) return launch_qr(W, n, o, win, wout, det_r, s);
     AFQ_TRY(smem_attr(k_cholqr2, smem));
     k_cholqr2<<<W, 256, smem, s>>>(n, o, win, wout, det_r);
     AFQ_LAUNCHED("k_cholqr2");

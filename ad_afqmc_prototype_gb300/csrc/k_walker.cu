@@ -610,25 +610,33 @@ int launch_energy_finish(int W, int n, int o, int nchunk, double h0, const doubl
 // shared memory, column-major with odd leading dimension.  Q is formed in
 // place by backward accumulation of the reflectors H_k = I - 2 u u^H.
 // =====================================================================
+// GLOBAL: the walker is factorised in place in wout (element (i, j) at
+// A[i o + j], wout already holding the input), for walkers too large for
+// shared memory; otherwise A[j ld + i] in shared memory.
+template <bool GLOBAL>
 __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restrict__ win,
                                             double2* __restrict__ wout, double2* __restrict__ det_out) {
-    extern __shared__ double2 A[];  // A[j * ld + i]
+    extern __shared__ double2 Asm[];
     __shared__ double2 s_alpha[64];
     __shared__ double s_red[8];
     __shared__ double s_sigma;
-    const int ld = n | 1;
+    const int ld = GLOBAL ? 1 : (n | 1);  // column stride
+    const int rs = GLOBAL ? o : 1;        // row stride
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nw = blockDim.x >> 5;
-    const double2* Wp = win + (size_t)w * n * o;
-    for (int e = tid; e < n * o; e += blockDim.x) {
-        int i = e / o, j = e % o;
-        A[j * ld + i] = Wp[e];
+    double2* A = GLOBAL ? wout + (size_t)w * n * o : Asm;
+    if (!GLOBAL) {
+        const double2* Wp = win + (size_t)w * n * o;
+        for (int e = tid; e < n * o; e += blockDim.x) {
+            int i = e / o, j = e % o;
+            A[j * ld + i] = Wp[e];
+        }
     }
     __syncthreads();
     for (int k = 0; k < o; ++k) {
         double2* x = A + k * ld;
         double sg = 0.0;
-        for (int i = k + 1 + tid; i < n; i += blockDim.x) sg += cabs2(x[i]);
+        for (int i = k + 1 + tid; i < n; i += blockDim.x) sg += cabs2(x[i * rs]);
         sg = warp_sum(sg);
         if (lane == 0) s_red[wid] = sg;
         __syncthreads();
@@ -639,7 +647,7 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
         }
         __syncthreads();
         const double sigma = s_sigma;
-        const double2 x0 = x[k];
+        const double2 x0 = x[k * rs];
         const double ax0 = sqrt(cabs2(x0));
         const double nx = sqrt(ax0 * ax0 + sigma);
         const double2 ph = ax0 == 0.0 ? make_double2(1.0, 0.0) : make_double2(x0.x / ax0, x0.y / ax0);
@@ -648,7 +656,7 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
         const double vn2 = cabs2(v0) + sigma;
         const double sc = vn2 > 0.0 ? 1.0 / sqrt(vn2) : 0.0;
         __syncthreads();
-        for (int i = k + tid; i < n; i += blockDim.x) x[i] = (i == k) ? cscale(v0, sc) : cscale(x[i], sc);
+        for (int i = k + tid; i < n; i += blockDim.x) x[i * rs] = (i == k) ? cscale(v0, sc) : cscale(x[i * rs], sc);
         if (tid == 0) s_alpha[k] = alpha;
         __syncthreads();
         // columns j > k: A[k:, j] -= 2 u (u^H A[k:, j]); one warp per column
@@ -656,12 +664,12 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
             double2* y = A + j * ld;
             double dr = 0.0, di = 0.0;
             for (int i = k + lane; i < n; i += 32) {
-                double2 p = cmulc(x[i], y[i]);
+                double2 p = cmulc(x[i * rs], y[i * rs]);
                 dr += p.x; di += p.y;
             }
             dr = warp_sum(dr); di = warp_sum(di);
             const double2 d2 = make_double2(2.0 * dr, 2.0 * di);
-            for (int i = k + lane; i < n; i += 32) y[i] = csub(y[i], cmul(x[i], d2));
+            for (int i = k + lane; i < n; i += 32) y[i * rs] = csub(y[i * rs], cmul(x[i * rs], d2));
         }
         __syncthreads();
     }
@@ -672,22 +680,22 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
             double2* y = A + j * ld;
             double dr = 0.0, di = 0.0;
             for (int i = k + lane; i < n; i += 32) {
-                double2 p = cmulc(u[i], y[i]);
+                double2 p = cmulc(u[i * rs], y[i * rs]);
                 dr += p.x; di += p.y;
             }
             dr = warp_sum(dr); di = warp_sum(di);
             const double2 d2 = make_double2(2.0 * dr, 2.0 * di);
-            for (int i = k + lane; i < n; i += 32) y[i] = csub(y[i], cmul(u[i], d2));
+            for (int i = k + lane; i < n; i += 32) y[i * rs] = csub(y[i * rs], cmul(u[i * rs], d2));
         }
         __syncthreads();
-        const double2 uk = u[k];
+        const double2 uk = u[k * rs];
         __syncthreads();
         for (int i = tid; i < n; i += blockDim.x) {
-            if (i < k) u[i] = make_double2(0.0, 0.0);
-            else if (i == k) u[i] = make_double2(1.0 - 2.0 * cabs2(uk), 0.0);
+            if (i < k) u[i * rs] = make_double2(0.0, 0.0);
+            else if (i == k) u[i * rs] = make_double2(1.0 - 2.0 * cabs2(uk), 0.0);
             else {
-                double2 t = cmulc(uk, u[i]);  // u_i conj(u_k)
-                u[i] = make_double2(-2.0 * t.x, -2.0 * t.y);
+                double2 t = cmulc(uk, u[i * rs]);  // u_i conj(u_k)
+                u[i * rs] = make_double2(-2.0 * t.x, -2.0 * t.y);
             }
         }
         __syncthreads();
@@ -701,7 +709,7 @@ __global__ void __launch_bounds__(256) k_qr(int n, int o, const double2* __restr
         double2 a = s_alpha[j];
         double aa = sqrt(cabs2(a));
         double2 cph = aa == 0.0 ? make_double2(1.0, 0.0) : make_double2(a.x / aa, a.y / aa);
-        Wo[e] = cmul(A[j * ld + i], cph);
+        Wo[e] = cmul(A[j * ld + i * rs], cph);
     }
     if (det_out && tid == 0) {
         double d = 1.0;
@@ -714,9 +722,17 @@ int launch_qr(int W, int n, int o, const double2* win, double2* wout, double2* d
     if (W <= 0) return AFQ_OK;
     if (o > 64) return fail(AFQ_E_UNSUPPORTED, "qr: nocc=%d > 64", o);
     size_t smem = (size_t)(n | 1) * o * sizeof(double2);
-    AFQ_TRY(set_smem(k_qr, smem));
-    k_qr<<<W, 256, smem, s>>>(n, o, win, wout, det_r);
-    AFQ_LAUNCHED("k_qr");
+    if (smem <= 200 * 1024) {
+        AFQ_TRY(set_smem(k_qr<false>, smem));
+        k_qr<false><<<W, 256, smem, s>>>(n, o, win, wout, det_r);
+        AFQ_LAUNCHED("k_qr");
+        return AFQ_OK;
+    }
+    // too large for shared memory: in place in wout
+    if (wout != win)
+        AFQ_CUDA(cudaMemcpyAsync(wout, win, sizeof(double2) * (size_t)W * n * o, cudaMemcpyDeviceToDevice, s));
+    k_qr<true><<<W, 256, 0, s>>>(n, o, wout, wout, det_r);
+    AFQ_LAUNCHED("k_qr(global)");
     return AFQ_OK;
 }
 

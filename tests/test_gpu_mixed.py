@@ -130,3 +130,36 @@ def test_mixed_overlap_matches_binary64(cuda):
     assert engine.workspace_status() == 0
     rel = float(((x.overlaps - y.overlaps).abs() / x.overlaps.abs()).max().item())
     assert rel < 1e-10, rel
+
+
+def test_large_walker_qr_matches_numpy(cuda):
+    """400 x 50 walkers do not fit in shared memory: the Householder QR runs
+    in place in global memory; Q equals numpy's phase-fixed Q."""
+    from ad_afqmc_prototype_gb300 import engine
+    from oracle import afqmc_oracle as O
+    rng = np.random.default_rng(4)
+    w = rng.normal(size=(3, 400, 50)) + 1j * rng.normal(size=(3, 400, 50))
+    q, det = engine.orthogonalize(torch.as_tensor(w, device="cuda"))
+    qo, deto = O.qr_phase(w)
+    np.testing.assert_allclose(q.cpu().numpy(), qo, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(det.cpu().numpy().real, np.abs(deto), rtol=1e-11)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_c5_block_matches_fp64(cuda, prec):
+    """nbasis 400, nocc 50, nchol 2000: one 10-step block (QR after step 5)
+    of the mixed form against the binary64 form on the same fields, within
+    0.1 mHa; the QRs take the global-memory path at this size."""
+    from ad_afqmc_prototype_gb300 import engine
+    W = 64
+    pa, pra, st = _setup("c5_n400_o50_g2000_w1024", W, "fp64", n_prop_steps=10, qr_every=5)
+    pb, prb, _ = _setup("c5_n400_o50_g2000_w1024", W, prec, n_prop_steps=10, qr_every=5)
+    ref = _dstate(st)
+    b = engine.DeviceState(*[t.clone() for t in (ref.walkers, ref.weights, ref.overlaps, ref.pop_shift,
+                                                  ref.e_estimate)])
+    f = engine.fill_normal((10, W, pa.nchol), 9, 0)
+    ea, wa = engine.block(pa, pra, ref, 0, 0, fields=f, zeta=0.25)
+    eb, wb = engine.block(pb, prb, b, 0, 0, fields=f, zeta=0.25)
+    assert engine.workspace_status() == 0
+    print(f"C5 {prec}: E_fp64 {float(ea):.8f}  |dE| {abs(float(ea) - float(eb)):.2e}")
+    assert abs(float(ea) - float(eb)) < 1e-4
