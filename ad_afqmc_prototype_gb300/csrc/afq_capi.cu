@@ -979,6 +979,9 @@ int run_block_taped(const afq_problem* pb, const afq_params* p, const afq_state*
     for (int st_i = 0; st_i < p->n_prop_steps; ++st_i) {
         AFQ_TRY(snap_state(d, st, snap, op++, s));
         AFQ_TRY(step_impl(pb, p, st, nullptr, seed, counter + st_i, ws.step, s));
+        if (snap && snap->V && chunk_size(W, p->n_chunks) == W)
+            AFQ_CUDA(cudaMemcpyAsync(snap->V + (size_t)st_i * W * n * n, ws.step.V, sizeof(double2) * (size_t)W * n * n,
+                                     cudaMemcpyDeviceToDevice, s));
         if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps) {
             AFQ_TRY(snap_state(d, st, snap, op++, s));
             AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));

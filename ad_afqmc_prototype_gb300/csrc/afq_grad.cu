@@ -63,7 +63,9 @@ struct GradWS {
     // replay state
     double2* walkers; double* weights; double2* overlaps; double* pop; double* e_est;
     double* be; double* bw;
-    BlockSnap snap;  // ck blocks, n_ops slots each (energy: ck x W)
+    BlockSnap snap;  // ck blocks, n_ops slots each (energy: ck x W; V: ck x n_prop_steps when kept)
+    bool keep_v;     // the replay keeps each step's V for the adjoint (no V-build recomputation)
+    double2* zpart;  // split-K layers of the adjoint's FP64 GEMMs
     // adjoint state (two copies for the comb's scatter)
     double2 *wk, *wk2, *ob, *ob2;
     double *wb, *wb2, *pb, *wsum;
@@ -106,6 +108,15 @@ GradWS layout_grad(Arena& a, const afq_dims* d, const afq_params* p, int ck) {
     g.snap.overlaps = a.take<double2>(ck * nops * W);
     g.snap.pop = a.take<double>(ck * nops);
     g.snap.energy = a.take<double2>(ck * W);
+    const size_t vbytes = (size_t)ck * p->n_prop_steps * W * n * n * sizeof(double2);
+    const int wc1 = p->n_chunks <= 1 ? (int)W : (int)((W + p->n_chunks - 1) / p->n_chunks);
+    g.keep_v = wc1 == (int)W && vbytes <= ((size_t)8 << 30);
+    g.snap.V = g.keep_v ? a.take<double2>(vbytes / sizeof(double2)) : nullptr;
+    {
+        const size_t z1 = (size_t)zgemm_splits((int)W, (int)G, (int)(n * n)) * W * G;
+        const size_t z2 = (size_t)zgemm_splits((int)W, (int)no, (int)G) * W * no;
+        g.zpart = a.take<double2>(z1 > z2 ? z1 : z2);
+    }
     g.wk = a.take<double2>(W * no);
     g.wk2 = a.take<double2>(W * no);
     g.ob = a.take<double2>(W);
@@ -172,8 +183,8 @@ struct Ctx {
 template <class T>
 T* slot(T* base, size_t per, int k) { return base + (size_t)k * per; }
 
-// Adjoint of step s of a block, whose input state is snapshot slot op.
-int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, uint64_t counter) {
+// Adjoint of step st_i of a block, whose input state is snapshot slot op.
+int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, int st_i, uint64_t counter) {
     const afq_problem* pb = c.pb;
     const afq_dims* d = &pb->dims;
     const GradWS& g = *c.g;
@@ -191,13 +202,14 @@ int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, uint64_t counter) {
         AFQ_TRY(launch_field_shift(W, G, pb->sqrt_dt, g.fields, g.fb, (const double2*)pb->mf_shifts, g.xs,
                                    g.shift_term, g.fb_term, s));
     }
-    {
+    const double2* V = sn.V ? sn.V + (size_t)st_i * W * n * n : g.V;
+    if (!sn.V) {
         AFQ_PHASE("adj_vbuild_gemm", s);
         AFQ_TRY(launch_zgemm(W, n * n, G, 1.0, g.xs, G, pb->chol, (int64_t)n * n, false, false, g.V,
                              (int64_t)n * n, s));
     }
     { AFQ_PHASE("adj_taylor_tape", s);
-      AFQ_TRY(launch_taylor_tape(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, Wpre, g.terms, g.w2, s)); }
+      AFQ_TRY(launch_taylor_tape(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, V, Wpre, g.terms, g.w2, s)); }
     AFQ_PHASE("adj_step_rest", s);
     // weights, population shift and overlap ratio
     AFQ_TRY(launch_weight_adj(W, c.p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
@@ -210,18 +222,18 @@ int step_adjoint(const Ctx& c, const BlockSnap& sn, int op, uint64_t counter) {
     // W' = E W2: dL/dE += Re W'b W2^H; Taylor reverse; W1 = E W: dL/dE += Re W1b W^H
     { AFQ_PHASE("adj_ebar", s); AFQ_TRY(launch_ebar(W, n, o, g.wk, no, g.w2, no, g.ebar_part, s)); }
     { AFQ_PHASE("adj_taylor", s);
-      AFQ_TRY(launch_taylor_adj(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, g.V, g.wk, g.tbar, g.wk, s)); }
+      AFQ_TRY(launch_taylor_adj(W, n, o, K, pb->sqrt_dt, pb->exp_h1_half, V, g.wk, g.tbar, g.wk, s)); }
     { AFQ_PHASE("adj_ebar", s);
       AFQ_TRY(launch_ebar(W, n, o, g.tbar, (long long)(K + 1) * no, Wpre, no, g.ebar_part, s)); }
     // V = sum_g x~_g L_g: x~b = Vb . L^T
     { AFQ_PHASE("adj_vbar", s); AFQ_TRY(launch_vbar(W, n, o, K, pb->sqrt_dt, g.tbar, g.terms, g.V, s)); }
     { AFQ_PHASE("adj_xbar_gemm", s);
-      AFQ_TRY(launch_zgemm(W, G, n * n, 1.0, g.V, (int64_t)n * n, pb->chol, (int64_t)n * n, false, true, g.xtb, G,
-                           s)); }
+      AFQ_TRY(launch_zgemm_splitk(W, G, n * n, 1.0, g.V, (int64_t)n * n, pb->chol, (int64_t)n * n, false, true,
+                                  g.xtb, g.zpart, s)); }
     // field shifts, then the force bias fb = 2 L~ vec(G_half)
     AFQ_TRY(launch_fs_adj(W, G, pb->sqrt_dt, g.fields, g.fb, (const double2*)pb->mf_shifts, g.fbt_bar, g.shift_bar,
                           g.xtb, s));
-    AFQ_TRY(launch_zgemm(W, no, G, 2.0, g.xtb, G, pb->rot_chol, no, false, false, g.gbar, no, s));
+    AFQ_TRY(launch_zgemm_splitk(W, no, G, 2.0, g.xtb, G, pb->rot_chol, no, false, false, g.gbar, g.zpart, s));
     return launch_green_adj(W, n, o, mo, Wpre, g.gbar, nullptr, nullptr, g.wk, g.status, s);
 }
 
@@ -279,7 +291,7 @@ int block_adjoint(const Ctx& c, const BlockSnap& sn, const TapeLayout& t, int b,
             AFQ_TRY(launch_qr_adj(W, n, o, slot(sn.walkers, (size_t)W * no, op), post, g.wk, g.wk, g.status, s));
             --op;
         }
-        AFQ_TRY(step_adjoint(c, sn, op, counter + st_i));
+        AFQ_TRY(step_adjoint(c, sn, op, st_i, counter + st_i));
         --op;
     }
     if (op != -1) return fail(AFQ_E_INVALID_ARGUMENT, "internal: block operations out of step (%d)", op);
@@ -395,6 +407,7 @@ int afq_grad_backward(const afq_problem* pb, const afq_params* p, const double* 
             x.overlaps = g.snap.overlaps + k * W;
             x.pop = g.snap.pop + k;
             x.energy = g.snap.energy + (size_t)(b - b0) * W;
+            x.V = g.keep_v ? g.snap.V + (size_t)(b - b0) * p->n_prop_steps * W * n * n : nullptr;
             return x;
         };
         for (int b = b0; b < b1; ++b) {

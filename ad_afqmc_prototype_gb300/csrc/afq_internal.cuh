@@ -210,6 +210,12 @@ int launch_sum_spin_blocks(int n, const double2* rdm1, double2* dm, cudaStream_t
 int launch_zgemm(int M, int N, int K, double alpha, const double2* A, int64_t lda,
                  const void* B, int64_t ldb, bool b_complex, bool b_trans, double2* C,
                  int64_t ldc, cudaStream_t s);
+// Same product with K split over CTA layers when the M x N tiles alone would
+// not fill the GPU; C dense (ldc = N); part: zgemm_splits(M, N, K) x M x N
+// scratch; the layers are added in a fixed order (deterministic).
+int zgemm_splits(int M, int N, int K);
+int launch_zgemm_splitk(int M, int N, int K, double alpha, const double2* A, int64_t lda, const void* B,
+                        int64_t ldb, bool b_complex, bool b_trans, double2* C, double2* part, cudaStream_t s);
 
 // k_walker.cu
 int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
@@ -370,6 +376,7 @@ struct BlockSnap {
     double2* overlaps = nullptr;  // n_ops x W
     double* pop = nullptr;        // n_ops
     double2* energy = nullptr;    // W local energies of the measurement
+    double2* V = nullptr;         // optional, n_prop_steps x W n n: each step's V (one walker chunk only)
 };
 int block_op_count(const afq_params* p);
 size_t block_ws_bytes(const afq_dims* d, int n_chunks);

@@ -26,13 +26,18 @@ __device__ __forceinline__ void mac(double2& acc, double2 a, double b) { rfma(ac
 __device__ __forceinline__ void mac(double2& acc, double2 a, double2 b) { cfma(acc, a, b); }
 }  // namespace
 
+// grid.z > 1 (split K): CTA layer z sums k in [z kc, min(K, (z + 1) kc)) into
+// C + z cs (the caller adds the layers in a fixed order).
 template <bool BC, bool BT>
 __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double alpha,
                                                const double2* __restrict__ A, int64_t lda,
                                                const void* __restrict__ Bv, int64_t ldb,
-                                               double2* __restrict__ C, int64_t ldc) {
+                                               double2* __restrict__ C, int64_t ldc, int kc, int64_t cs) {
     using TB = typename BElem<BC>::T;
     const TB* B = (const TB*)Bv;
+    const int kbeg = blockIdx.z * kc;
+    const int kend = min(K, kbeg + kc);
+    C += (int64_t)blockIdx.z * cs;
     __shared__ double2 As[BK][BM + 1];
     __shared__ TB Bs[BK][BN + 1];
     const int tid = threadIdx.x;
@@ -45,13 +50,13 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double alpha
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = zero2();
 
-    for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
         // A tile: 64 rows x 16 k, k fastest for coalescing
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             int mm = (tid >> 4) + 16 * r, kk = tid & 15;
             int gm = m0 + mm, gk = k0 + kk;
-            As[kk][mm] = (gm < M && gk < K) ? A[(int64_t)gm * lda + gk] : zero2();
+            As[kk][mm] = (gm < M && gk < kend) ? A[(int64_t)gm * lda + gk] : zero2();
         }
         if (!BT) {
             // B(k, n) = B[k*ldb + n], n fastest
@@ -59,7 +64,7 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double alpha
             for (int r = 0; r < 4; ++r) {
                 int kk = (tid >> 6) + 4 * r, nn = tid & 63;
                 int gk = k0 + kk, gn = n0 + nn;
-                bool ok = gk < K && gn < N;
+                bool ok = gk < kend && gn < N;
                 load_b(Bs[kk][nn], B + (ok ? (int64_t)gk * ldb + gn : 0), ok);
             }
         } else {
@@ -68,7 +73,7 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double alpha
             for (int r = 0; r < 4; ++r) {
                 int nn = (tid >> 4) + 16 * r, kk = tid & 15;
                 int gk = k0 + kk, gn = n0 + nn;
-                bool ok = gk < K && gn < N;
+                bool ok = gk < kend && gn < N;
                 load_b(Bs[kk][nn], B + (ok ? (int64_t)gn * ldb + gk : 0), ok);
             }
         }
@@ -107,13 +112,55 @@ int launch_zgemm(int M, int N, int K, double alpha, const double2* A, int64_t ld
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
     if (grid.y > 65535u) return fail(AFQ_E_UNSUPPORTED, "zgemm: M=%d too large", M);
     if (b_complex) {
-        if (b_trans) k_zgemm<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc);
-        else k_zgemm<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc);
+        if (b_trans) k_zgemm<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, K, 0);
+        else k_zgemm<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, K, 0);
     } else {
-        if (b_trans) k_zgemm<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc);
-        else k_zgemm<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc);
+        if (b_trans) k_zgemm<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, K, 0);
+        else k_zgemm<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, K, 0);
     }
     AFQ_LAUNCHED("k_zgemm");
+    return AFQ_OK;
+}
+
+// C (M x N, ldc = N) = sum_z part[z] in order z = 0 .. splits-1
+__global__ void k_zsum_layers(long long count, int splits, const double2* __restrict__ part,
+                              double2* __restrict__ C) {
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+         e += (long long)gridDim.x * blockDim.x) {
+        double2 a = part[e];
+        for (int z = 1; z < splits; ++z) a = cadd(a, part[(long long)z * count + e]);
+        C[e] = a;
+    }
+}
+
+int zgemm_splits(int M, int N, int K) {
+    const long long ctas = (long long)((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+    int z = 1;
+    while (ctas * z < 2 * 152 && K / (z * 2) >= 4 * BK && z < 8) z *= 2;
+    return z;
+}
+
+int launch_zgemm_splitk(int M, int N, int K, double alpha, const double2* A, int64_t lda, const void* B,
+                        int64_t ldb, bool b_complex, bool b_trans, double2* C, double2* part, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return AFQ_OK;
+    const int z = zgemm_splits(M, N, K);
+    if (z == 1) return launch_zgemm(M, N, K, alpha, A, lda, B, ldb, b_complex, b_trans, C, N, s);
+    const int kc = (K / z + BK - 1) / BK * BK;
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, z);
+    if (grid.y > 65535u) return fail(AFQ_E_UNSUPPORTED, "zgemm: M=%d too large", M);
+    const int64_t cs = (int64_t)M * N;
+    if (b_complex) {
+        if (b_trans) k_zgemm<true, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, part, N, kc, cs);
+        else k_zgemm<true, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, part, N, kc, cs);
+    } else {
+        if (b_trans) k_zgemm<false, true><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, part, N, kc, cs);
+        else k_zgemm<false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, part, N, kc, cs);
+    }
+    AFQ_LAUNCHED("k_zgemm(split k)");
+    long long blocks = (cs + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_zsum_layers<<<(unsigned)blocks, 256, 0, s>>>(cs, z, part, C);
+    AFQ_LAUNCHED("k_zsum_layers");
     return AFQ_OK;
 }
 
