@@ -65,6 +65,7 @@ struct LowpDims {
     long long ldv;   // row stride of V (fp32)
     bool xf;         // exchange contracted in the energy GEMM's epilogue (24 < nocc <= 32)
     int Pe;          // rows per (walker, part) block and per Cholesky vector in the energy GEMM
+    int kd;          // 64-wide K blocks per tensor-core partial of the drained GEMMs
 };
 
 static LowpDims lowp_dims(const afq_dims* d) {
@@ -82,6 +83,9 @@ static LowpDims lowp_dims(const afq_dims* d) {
     // reading F (G o x 2 o fp32 per walker): worth it for o close to 32
     L.xf = o > 24 && o <= 32;
     L.Pe = L.xf ? 32 : o;
+    // the tensor cores' truncating fp32 sum over 128 products (bias ~2^-22 relative) stays below the
+    // three-section split's 2^-17; the six-section form drains every 64 (bias < 2^-23)
+    L.kd = d->precision == AFQ_PREC_MIXED_FAST ? 2 : 1;
     return L;
 }
 
@@ -298,7 +302,8 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
         AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, nullptr, fb_split(d, ws), s, nullptr, ws.csplit));
     }
     { AFQ_PHASE("fb_gemm", s);
-      AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s)); }
+      AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s,
+                                      L.kd)); }
     const int Wc = chunk_size(W, p->n_chunks);
     { AFQ_PHASE("field_shift", s);
       AFQ_TRY(launch_field_shift_mixed(W, G, Wc, pb->sqrt_dt, fields, ws.fbm, G, (const double2*)pb->mf_shifts, ws.Av,
@@ -314,7 +319,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
             __nv_bfloat16* vmid = vh + (size_t)2 * wc * L.ldv;
             { AFQ_PHASE("vbuild_gemm", s);
               AFQ_TRY(launch_tc_gemm_tn_drain_split(2 * wc, n * n, L.Kt_V, ws.Av + (size_t)2 * w0 * L.Kt_V, L.Kt_V,
-                                                    lb.Bv, L.Kt_V, vh, vmid, L.ldv, ws.status, s)); }
+                                                    lb.Bv, L.Kt_V, vh, vmid, L.ldv, ws.status, s, L.kd)); }
             { AFQ_PHASE("trotter", s);
               AFQ_TRY(launch_trotter_tc(wc, n, o, p->n_exp_terms, pb->sqrt_dt, ws.esplit, ws.esplit + (size_t)n * n, vh,
                                         vmid, walk + (size_t)w0 * n * o, walk + (size_t)w0 * n * o, ws.status, s)); }
@@ -368,7 +373,7 @@ static int energy_impl(const afq_problem* pb, const afq_state* st, const BlockWS
         if (L.xf) {
             { AFQ_PHASE("e_gemm", s);
               AFQ_TRY(launch_tc_gemm_exchange(wc, G, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.xsum, ws.ctr,
-                                              ws.step.status, s)); }
+                                              ws.step.status, s, L.kd)); }
             { AFQ_PHASE("e_exchange", s);
               AFQ_TRY(launch_exchange_finish(wc, G, ws.xsum, ws.ctr, partial + (size_t)w0 * nch * 2, s)); }
             continue;
@@ -903,7 +908,7 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
                                              L.Kt_E, L.sec, s));
                 if (L.xf) {
                     AFQ_TRY(launch_tc_gemm_exchange(sc, G, L.Kt_E, ws.Bg, L.Kt_E, lb.Le, L.Kt_E, ws.xsum, ws.ctr,
-                                                    ws.step.status, s));
+                                                    ws.step.status, s, L.kd));
                     AFQ_TRY(launch_exchange_finish(sc, G, ws.xsum, ws.ctr,
                                                    (double2*)ws.partial + (size_t)s0 * nch * 2, s));
                     continue;

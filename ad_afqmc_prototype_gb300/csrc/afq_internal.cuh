@@ -326,7 +326,7 @@ int launch_green_rows(int wc, int n, int o, int P, const double2* green, __nv_bf
 // walkers (2 x 32 rows each), B = L~ rows (32 per Cholesky vector); writes
 // x (nw x exchange_halves(G) x 2) and c (nw x G x 2) fp32 instead of F.
 int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
-                            float* x, float* c, int* err, cudaStream_t s);
+                            float* x, float* c, int* err, cudaStream_t s, int kd = 1);
 int exchange_halves(int G);
 int launch_exchange_finish(int nw, int G, const float* x, const float* c, double2* partial, cudaStream_t s);
 

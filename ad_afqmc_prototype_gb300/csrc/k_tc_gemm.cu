@@ -573,9 +573,9 @@ int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long 
 }
 
 int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
-                            float* x, float* c, int* err, cudaStream_t s) {
+                            float* x, float* c, int* err, cudaStream_t s, int kd) {
     if (nw <= 0 || G <= 0) return AFQ_OK;
-    AFQ_TRY(drain_prologue(K, 1));
+    AFQ_TRY(drain_prologue(K, kd));
     const int M = 64 * nw, N = 32 * G;
     tc::ExchOut xo;
     xo.x = x;
@@ -583,7 +583,7 @@ int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, 
     xo.G = G;
     xo.nw = nw;
     xo.nhalf = 2 * ((N + 127) / 128);
-    return launch_drain<128, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, 1, err, s, xo);
+    return launch_drain<128, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, kd, err, s, xo);
 }
 
 int exchange_halves(int G) { return 2 * ((32 * G + 127) / 128); }
