@@ -427,7 +427,6 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
     float2* wl = wf + (size_t)OS_CH * o;           // DF: lo part of a chunk of OS_CH rows
     __shared__ int s_piv;
     __shared__ double2 s_rp;
-    __shared__ float2 s_rpf;
     __shared__ double2 s_det;
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
