@@ -340,7 +340,8 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
     params = afqmc_params(dt=0.005, n_walkers=wl.n_walkers, seed=wl.seed, n_prop_steps=STEPS_PER_BLOCK,
                           qr_every=QR_EVERY)
     st0 = init_prop_state(sys=sys_, n_walkers=wl.n_walkers, seed=wl.seed, ham_data=ham,
-                          trial_ops_=make_rhf_trial_ops(sys_), trial_data=trial, meas_ops=make_rhf_meas_ops(sys_))
+                          trial_ops_=make_rhf_trial_ops(sys_), trial_data=trial, meas_ops=make_rhf_meas_ops(sys_),
+                          initial_walkers=synth.trial_walkers(H["mo_coeff"], wl.n_walkers))
     D = torch.as_tensor(H["D"], device="cuda")
     kw = dict(ham_data=ham, trial_data=trial, params=params, state=st0, n_blocks=n_blocks, seed=17, counter=0,
               checkpoint_every=checkpoint_every)
@@ -359,6 +360,7 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
     ev[2].record(stream)
     torch.cuda.synchronize()
     fwd_ms, bwd_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    e_val = float(E.detach())
     adj = float((h1.grad * D).sum())
     idx = runs[0].sr_idx
 
@@ -376,7 +378,7 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
     free, moved = central(None)
     return {"workload": workload, "n_blocks": n_blocks, "steps": n_blocks * STEPS_PER_BLOCK,
             "checkpoint_every_steps": checkpoint_every, "precision": "fp64",
-            "energy": round(float(E), 10), "dE_dlambda_adjoint": adj, "dE_dlambda_fd_fixed_comb": fd,
+            "energy": round(e_val, 10), "dE_dlambda_adjoint": adj, "dE_dlambda_fd_fixed_comb": fd,
             "rel_diff": abs(adj - fd) / abs(fd), "fd_eps": eps,
             "dE_dlambda_fd_free_comb": free, "free_comb_indices_moved": moved,
             "forward_ms": round(fwd_ms, 2), "backward_ms": round(bwd_ms, 2),
