@@ -33,6 +33,10 @@ STEPS_PER_BLOCK = 10
 QR_EVERY = 5
 # bf16 sections of a split tensor-core operand row, per precision (split_sections in the CUDA sources)
 SPLIT_SECTIONS = {"mixed": 6, "mixed_fast": 3}
+# DRAM bytes (read + write) per launch of a kernel, from one ncu capture of this bench's own command
+# (profiles/launches_block_c4_n200_o30_g1000_w4096_mixed_fast.md), keyed by (workload, precision,
+# walkers, phase); the roofline reports them beside the algorithmic bytes
+MEASURED_TRAFFIC = {("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "vbuild_gemm"): 894594048 + 1319975936}
 
 
 def parse():
@@ -277,6 +281,16 @@ def run_ours(args, rank, world):
     # dominant kernel and its roofline
     work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=args.precision)
     roof = roofline_for(phases, work, lib, args.steps)
+    if roof is not None:
+        t = MEASURED_TRAFFIC.get((args.workload, args.precision, W, roof["kernel"]))
+        if t is not None:
+            roof["traffic"] = t
+            roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full-size launch"
+            if roof["kernel"] == "vbuild_gemm" and args.precision in SPLIT_SECTIONS:
+                ks = SPLIT_SECTIONS[args.precision]
+                # split x~ and chol^T rows (bf16) read, V written (bf16 hi + mid, or fp32): 8 W n^2 bytes
+                roof["traffic_algorithmic"] = int(2 * (2 * W) * _r64(ks * G) + 2 * n * n * _r64(ks * G)
+                                                  + 8 * W * n * n)
     tc = {k: roofline_for(phases, work, lib, args.steps, name=k) for k in phases
           if k in work and work[k][1] in ("tensor", "hbm")}
 
