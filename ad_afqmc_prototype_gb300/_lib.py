@@ -120,6 +120,10 @@ _SIGS = {
                              P, c_size_t, P]),
     "afq_block_u": (c_int32, [POINTER(afq_problem), POINTER(afq_params), POINTER(afq_state), P, c_double,
                               c_uint64, c_uint64, P, P, P, P, c_size_t, P]),
+    "afq_g_workspace": (c_size_t, [POINTER(afq_dims), c_int32]),
+    "afq_overlap_g": (c_int32, [POINTER(afq_dims), P, P, P, P, c_size_t, P]),
+    "afq_force_bias_g": (c_int32, [POINTER(afq_dims), P, P, P, P, P, c_size_t, P]),
+    "afq_apply_trotter_g": (c_int32, [POINTER(afq_dims), c_int32, c_double, c_int32, P, P, P, P, P, P, c_size_t, P]),
     "afq_modified_cholesky_workspace": (c_size_t, [c_int32, c_int32]),
     "afq_modified_cholesky": (c_int32, [c_int32, P, c_double, c_int32, P, POINTER(c_int32), P, c_size_t, P]),
     "afq_mlp_param_count": (c_size_t, [c_int32, c_int32]),

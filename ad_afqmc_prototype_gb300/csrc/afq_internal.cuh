@@ -220,8 +220,9 @@ int launch_zgemm_splitk(int M, int N, int K, double alpha, const double2* A, int
 // k_walker.cu
 int launch_green(int W, int n, int o, const double2* mo, int trial_real, const double2* walkers,
                  double2* ovlp_out, double2* green_out, cudaStream_t s);
+// vdiv walkers share each V (2: the top and bottom halves of generalized walkers)
 int launch_trotter(int W, int n, int o, int n_terms, double sqrt_dt, const double* E,
-                   const double2* V, const double2* win, double2* wout, cudaStream_t s);
+                   const double2* V, const double2* win, double2* wout, cudaStream_t s, int vdiv = 1);
 int launch_field_shift(int W, int G, double sqrt_dt, const double* x, const double2* fb,
                        const double2* mf, double2* xs, double2* shift_term, double2* fb_term,
                        cudaStream_t s);

@@ -1,5 +1,7 @@
-// Unrestricted walkers with the RHF trial (walker_kind "unrestricted"):
-// kernels and extern "C" entry points of the binary64 step and block.
+// Unrestricted and generalized walkers with the RHF trial: kernels and
+// extern "C" entry points of the binary64 step and block (unrestricted) and
+// of the overlap, force bias and Trotter step (generalized; the reference has
+// no generalized energy kernel, so no block either).
 //
 // A walker is a pair (W_up, W_dn), each n x o (the RHF trial gives both
 // spins nocc columns).  The engine stores the W pairs as one (2, W, n, o)
@@ -237,10 +239,142 @@ int check_state_u(const afq_state* st) {
     return AFQ_OK;
 }
 
+// ---------------------------------------------------- generalized walkers
+// A generalized walker is (2n x 2o): the up block of rows over the down
+// block (meas/rhf.py:103-130).  With the block-diagonal trial
+// C_g = [[C, 0], [0, C]], m = C_g^H W is the reference's vstack(C^H W_top,
+// C^H W_bot), so the restricted Green's-function kernel at (2n, 2o) gives
+// det(m) and G_half (2o x 2n).
+
+__global__ void k_blockdiag_c(int n, int o, const double2* __restrict__ mo, double2* __restrict__ cg) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 4 * n * o) return;
+    const int r = e / (2 * o), c = e % (2 * o);
+    const bool top = r < n, left = c < o;
+    cg[e] = top == left ? mo[(size_t)(top ? r : r - n) * o + (left ? c : c - o)] : make_double2(0.0, 0.0);
+}
+
+// g[w, a, j] = G[w, a, j] + G[w, o + a, n + j]  (the up-up plus down-down blocks of G_half)
+__global__ void k_fold_g(int W, int n, int o, const double2* __restrict__ G, double2* __restrict__ g) {
+    const long long total = (long long)W * o * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(e / ((long long)o * n));
+        const int r = (int)(e % ((long long)o * n));
+        const int a = r / n, j = r % n;
+        const double2* Gw = G + (size_t)w * 4 * o * n;  // (2o x 2n)
+        g[e] = cadd(Gw[(size_t)a * 2 * n + j], Gw[(size_t)(o + a) * 2 * n + n + j]);
+    }
+}
+
+struct GWS {
+    int* status;
+    double2* cg;     // 2n x 2o
+    double2* green;  // W x 2o x 2n
+    double2* gsum;   // W x o x n
+    double2* V;      // Wc x n x n
+};
+
+GWS layout_g(Arena& a, const afq_dims* d, int n_chunks) {
+    const size_t W = d->n_walkers, n = d->norb, o = d->nocc;
+    GWS g = {};
+    g.status = a.take<int>(64);
+    g.cg = a.take<double2>(4 * n * o);
+    g.green = a.take<double2>(W * 4 * o * n);
+    g.gsum = a.take<double2>(W * o * n);
+    g.V = a.take<double2>((size_t)chunk_of(d->n_walkers, n_chunks) * n * n);
+    return g;
+}
+
+int check_g(const afq_dims* d) {
+    if (!d) return fail(AFQ_E_INVALID_ARGUMENT, "dims is NULL");
+    if (d->n_walkers < 1 || d->norb < 1 || d->nocc < 1 || d->nocc > d->norb || d->nchol < 1)
+        return fail(AFQ_E_INVALID_ARGUMENT, "bad dims W=%d n=%d o=%d G=%d", d->n_walkers, d->norb, d->nocc,
+                    d->nchol);
+    if (d->precision != AFQ_PREC_FP64) return fail(AFQ_E_UNSUPPORTED, "generalized walkers run the binary64 form");
+    if (2 * d->nocc > 64) return fail(AFQ_E_UNSUPPORTED, "generalized walkers: 2 nocc = %d > 64", 2 * d->nocc);
+    if (2 * d->n_walkers > 65535) return fail(AFQ_E_UNSUPPORTED, "generalized walkers: W=%d > 32767", d->n_walkers);
+    return AFQ_OK;
+}
+
+int build_cg(const afq_dims* d, const double2* mo, const GWS& g, cudaStream_t s) {
+    const int count = 4 * d->norb * d->nocc;
+    k_blockdiag_c<<<(count + 255) / 256, 256, 0, s>>>(d->norb, d->nocc, mo, g.cg);
+    AFQ_LAUNCHED("k_blockdiag_c");
+    return AFQ_OK;
+}
+
 }  // namespace
 }  // namespace afq
 
 using namespace afq;
+
+size_t afq_g_workspace(const afq_dims* d, int32_t n_chunks) {
+    if (check_g(d) != AFQ_OK) return 0;
+    Arena a;
+    layout_g(a, d, n_chunks);
+    return a.used;
+}
+
+int afq_overlap_g(const afq_dims* d, const double* mo_coeff, const double* walkers, double* overlaps,
+                  void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_g(d));
+    if (!mo_coeff || !walkers || !overlaps || !workspace) return fail(AFQ_E_INVALID_ARGUMENT, "NULL argument");
+    Arena a(workspace, workspace_bytes);
+    const GWS g = layout_g(a, d, 1);
+    if (!a.ok()) return fail(AFQ_E_WORKSPACE, "workspace: %zu bytes < %zu", workspace_bytes, a.used);
+    cudaStream_t s = as_stream(stream);
+    AFQ_TRY(build_cg(d, (const double2*)mo_coeff, g, s));
+    return launch_green_det(d->n_walkers, 2 * d->norb, 2 * d->nocc, g.cg, d->trial_is_real, (const double2*)walkers,
+                            (double2*)overlaps, nullptr, s);
+}
+
+int afq_force_bias_g(const afq_dims* d, const double* mo_coeff, const double* rot_chol, const double* walkers,
+                     double* force_bias, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_g(d));
+    if (!mo_coeff || !rot_chol || !walkers || !force_bias || !workspace)
+        return fail(AFQ_E_INVALID_ARGUMENT, "NULL argument");
+    Arena a(workspace, workspace_bytes);
+    const GWS g = layout_g(a, d, 1);
+    if (!a.ok()) return fail(AFQ_E_WORKSPACE, "workspace: %zu bytes < %zu", workspace_bytes, a.used);
+    cudaStream_t s = as_stream(stream);
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, on = n * o;
+    AFQ_TRY(build_cg(d, (const double2*)mo_coeff, g, s));
+    AFQ_TRY(launch_green(W, 2 * n, 2 * o, g.cg, d->trial_is_real, (const double2*)walkers, nullptr, g.green, s));
+    const long long total = (long long)W * on;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_fold_g<<<(unsigned)blocks, 256, 0, s>>>(W, n, o, g.green, g.gsum);
+    AFQ_LAUNCHED("k_fold_g");
+    return launch_zgemm(W, d->nchol, on, 1.0, g.gsum, on, rot_chol, on, !d->trial_is_real, true,
+                        (double2*)force_bias, d->nchol, s);
+}
+
+int afq_apply_trotter_g(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_t n_chunks, const double* chol,
+                        const double* exp_h1_half, const double* walkers, const double* shifted_fields,
+                        double* walkers_out, void* workspace, size_t workspace_bytes, void* stream) {
+    AFQ_TRY(check_g(d));
+    if (!chol || !exp_h1_half || !walkers || !shifted_fields || !walkers_out || !workspace)
+        return fail(AFQ_E_INVALID_ARGUMENT, "NULL argument");
+    if (n_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_terms=%d < 0", n_terms);
+    Arena a(workspace, workspace_bytes);
+    const GWS g = layout_g(a, d, n_chunks);
+    if (!a.ok()) return fail(AFQ_E_WORKSPACE, "workspace: %zu bytes < %zu", workspace_bytes, a.used);
+    cudaStream_t s = as_stream(stream);
+    const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
+    const int Wc = chunk_of(W, n_chunks);
+    const double2* xs = (const double2*)shifted_fields;
+    for (int w0 = 0; w0 < W; w0 += Wc) {
+        const int wc = W - w0 < Wc ? W - w0 : Wc;
+        AFQ_TRY(launch_zgemm(wc, n * n, G, 1.0, xs + (size_t)w0 * G, G, chol, (int64_t)n * n, false, false, g.V,
+                             (int64_t)n * n, s));
+        // the top and bottom n x 2o halves of each walker, both with the walker's V
+        AFQ_TRY(launch_trotter(2 * wc, n, 2 * o, n_terms, sqrt_dt, exp_h1_half, g.V,
+                               (const double2*)walkers + (size_t)w0 * 4 * n * o,
+                               (double2*)walkers_out + (size_t)w0 * 4 * n * o, s, 2));
+    }
+    return AFQ_OK;
+}
 
 size_t afq_u_workspace(const afq_dims* d, int32_t n_chunks) {
     if (check_u(d) != AFQ_OK) return 0;

@@ -269,14 +269,14 @@ template <int NR>
 __global__ void __launch_bounds__(TR_THREADS) k_trotter(int n, int o, int n_terms, double sqrt_dt,
                                                         const double* __restrict__ E,
                                                         const double2* __restrict__ V,
-                                                        const double2* win, double2* wout) {
+                                                        const double2* win, double2* wout, int vdiv) {
     extern __shared__ double2 sm[];
     double2* T = sm;                    // n x OC
     double2* Ms = sm + (size_t)n * TR_OC;  // n x BJ
     const int w = blockIdx.y, c0 = blockIdx.x * TR_OC;
     const int tid = threadIdx.x, c = tid % TR_OC, rg = tid / TR_OC;
     const double2* Wp = win + (size_t)w * n * o;
-    const double2* Vw = V + (size_t)w * n * n;
+    const double2* Vw = V + (size_t)(w / vdiv) * n * n;
 
     for (int e = tid; e < n * TR_OC; e += TR_THREADS) {
         int i = e / TR_OC, cc = e % TR_OC;
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(TR_THREADS) k_trotter(int n, int o, int n_term
 }
 
 int launch_trotter(int W, int n, int o, int n_terms, double sqrt_dt, const double* E, const double2* V,
-                   const double2* win, double2* wout, cudaStream_t s) {
+                   const double2* win, double2* wout, cudaStream_t s, int vdiv) {
     if (W <= 0) return AFQ_OK;
     const int nr = (n + TR_NRG - 1) / TR_NRG;
     size_t smem = (size_t)n * (TR_OC + TR_BJ) * sizeof(double2);
@@ -329,7 +329,7 @@ int launch_trotter(int W, int n, int o, int n_terms, double sqrt_dt, const doubl
 #define AFQ_TR(NRV)                                                                   \
     do {                                                                              \
         AFQ_TRY(set_smem(k_trotter<NRV>, smem));                                      \
-        k_trotter<NRV><<<grid, TR_THREADS, smem, s>>>(n, o, n_terms, sqrt_dt, E, V, win, wout); \
+        k_trotter<NRV><<<grid, TR_THREADS, smem, s>>>(n, o, n_terms, sqrt_dt, E, V, win, wout, vdiv); \
     } while (0)
     if (nr <= 1) AFQ_TR(1);
     else if (nr <= 2) AFQ_TR(2);

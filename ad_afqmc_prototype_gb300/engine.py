@@ -576,6 +576,55 @@ def block_u(prob: Problem, params, st: DeviceState, seed: int, counter: int, fie
     return e, wsum
 
 
+# ------------------------------------------------- generalized walkers
+def _g_dims(w: torch.Tensor, mo: torch.Tensor, nchol: int, trial_is_real: bool):
+    n, o = mo.shape
+    if w.dim() != 3 or w.shape[1] != 2 * n or w.shape[2] != 2 * o:
+        raise ValueError(f"generalized walkers must be (W, {2 * n}, {2 * o}); got {tuple(w.shape)}")
+    return make_dims(w.shape[0], n, o, nchol, trial_is_real)
+
+
+def _g_ws(d, n_chunks: int = 1):
+    return workspace(_lib.load().afq_g_workspace(ctypes.byref(d), int(n_chunks)))
+
+
+def overlap_g(walkers, mo: torch.Tensor, trial_is_real: bool) -> torch.Tensor:
+    """det(vstack(C^H W_top, C^H W_bot)) per walker (meas/rhf.py:103-109)."""
+    w = as_device(walkers, C128)
+    d = _g_dims(w, mo, 1, trial_is_real)
+    out = torch.empty((w.shape[0],), dtype=C128, device=w.device)
+    wsp, wsn = _g_ws(d)
+    _lib.call("afq_overlap_g", ctypes.byref(d), ptr(mo), ptr(w), ptr(out), wsp, wsn, stream_ptr())
+    return out
+
+
+def force_bias_g(walkers, mo, rot_chol, trial_is_real: bool) -> torch.Tensor:
+    """L~_flat vec(G_uu + G_dd) per walker (meas/rhf.py:112-130)."""
+    w = as_device(walkers, C128)
+    d = _g_dims(w, mo, rot_chol.shape[0], trial_is_real)
+    out = torch.empty((w.shape[0], rot_chol.shape[0]), dtype=C128, device=w.device)
+    wsp, wsn = _g_ws(d)
+    _lib.call("afq_force_bias_g", ctypes.byref(d), ptr(mo), ptr(rot_chol), ptr(w), ptr(out), wsp, wsn,
+              stream_ptr())
+    return out
+
+
+def apply_trotter_g(walkers, shifted_fields, chol, exp_h1_half, sqrt_dt: float, n_terms: int,
+                    n_chunks: int = 1) -> torch.Tensor:
+    """Both halves of each (2n, 2o) walker with its V (prop/chol_afqmc_ops.py:141-197)."""
+    w = as_device(walkers, C128)
+    xs = as_device(shifted_fields, C128)
+    n = int(chol.shape[1])
+    if w.dim() != 3 or w.shape[1] != 2 * n or w.shape[2] % 2:
+        raise ValueError(f"generalized walkers must be (W, {2 * n}, 2 nocc); got {tuple(w.shape)}")
+    d = make_dims(w.shape[0], n, w.shape[2] // 2, chol.shape[0], True)
+    out = torch.empty_like(w)
+    wsp, wsn = _g_ws(d, n_chunks)
+    _lib.call("afq_apply_trotter_g", ctypes.byref(d), int(n_terms), float(sqrt_dt), int(n_chunks), ptr(chol),
+              ptr(exp_h1_half), ptr(w), ptr(xs), ptr(out), wsp, wsn, stream_ptr())
+    return out
+
+
 # ------------------------------------------------- differentiated energy
 def grad_forward(prob: Problem, params, st: DeviceState, n_blocks: int, seed: int, counter: int,
                  checkpoint_blocks: int, sr_fixed: Optional[torch.Tensor] = None):

@@ -13,7 +13,7 @@ from .. import engine
 from ..core.ops import k_energy, k_force_bias, meas_ops
 from ..core.system import system
 from ..ham.chol import ham_chol
-from ..trial.rhf import overlap_r, overlap_u, rhf_trial
+from ..trial.rhf import overlap_g, overlap_r, overlap_u, rhf_trial
 
 
 @dataclass(frozen=True)
@@ -94,9 +94,21 @@ def energy_kernel_u(walker, ham_data: ham_chol, meas_ctx: rhf_meas_ctx, trial_da
 energy_kernel_u.batched = _energy_u_batched
 
 
+def _fb_g_batched(walkers, _ham, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    return engine.force_bias_g(walkers, trial_data.mo_coeff, meas_ctx.rot_chol, trial_data.is_real)
+
+
+def force_bias_kernel_g(walker, _ham: Any, meas_ctx: rhf_meas_ctx, trial_data: rhf_trial):
+    """L~_flat vec(G_uu + G_dd) for one (2n, 2o) walker (meas/rhf.py:112-130)."""
+    return _fb_g_batched(torch.as_tensor(walker)[None], _ham, meas_ctx, trial_data)[0]
+
+
+force_bias_kernel_g.batched = _fb_g_batched
+
+
 def make_rhf_meas_ops(sys: system) -> meas_ops:
-    """meas/rhf.py:153-176; restricted and unrestricted walkers run on the
-    CUDA engine (generalized walkers are not built)."""
+    """meas/rhf.py:153-176.  Generalized walkers have a force bias but, as in
+    the reference, no energy kernel."""
     wk = sys.walker_kind.lower()
     if wk == "restricted":
         return meas_ops(overlap=overlap_r, build_meas_ctx=build_meas_ctx,
@@ -105,5 +117,5 @@ def make_rhf_meas_ops(sys: system) -> meas_ops:
         return meas_ops(overlap=overlap_u, build_meas_ctx=build_meas_ctx,
                         kernels={k_force_bias: force_bias_kernel_u, k_energy: energy_kernel_u})
     if wk == "generalized":
-        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
+        return meas_ops(overlap=overlap_g, build_meas_ctx=build_meas_ctx, kernels={k_force_bias: force_bias_kernel_g})
     raise ValueError(f"unknown walker_kind: {sys.walker_kind}")

@@ -52,9 +52,22 @@ def make_chol_afqmc_ops(ham_data: ham_chol, walker_kind: str) -> chol_afqmc_ops:
         raise ValueError("ham_data.basis='generalized' requires walker_kind='generalized'")
     if walker_kind not in ("restricted", "unrestricted", "generalized"):
         raise ValueError(f"unknown walker_kind: {walker_kind}")
-    if ham_data.basis != "restricted" or walker_kind == "generalized":
-        raise ValueError("the CUDA engine propagates restricted and unrestricted walkers with a restricted-basis "
-                         "Hamiltonian only")
+    if ham_data.basis != "restricted":
+        raise ValueError("the CUDA engine propagates walkers with a restricted-basis Hamiltonian only")
+
+    if walker_kind == "generalized":
+        def apply_trotter_g_batched(walkers, fields, ctx: chol_afqmc_ctx, n_terms: int, n_chunks: int = 1):
+            """Top and bottom halves with the walker's V (:141-197)."""
+            return engine.apply_trotter_g(walkers, fields, ham_data.chol, ctx.exp_h1_half, float(ctx.sqrt_dt),
+                                          int(n_terms), n_chunks=n_chunks)
+
+        def apply_trotter_g(w, field, ctx: chol_afqmc_ctx, n_terms: int):
+            f = torch.as_tensor(field)[None].to(torch.complex128)
+            return apply_trotter_g_batched(torch.as_tensor(w)[None], f, ctx, n_terms)[0]
+
+        apply_trotter_g.batched = apply_trotter_g_batched
+        apply_trotter_g.ham_data = ham_data
+        return chol_afqmc_ops(n_fields_, build_prop_ctx, apply_trotter_g)
 
     if walker_kind == "unrestricted":
         def apply_trotter_u_batched(walkers, fields, ctx: chol_afqmc_ctx, n_terms: int, n_chunks: int = 1):

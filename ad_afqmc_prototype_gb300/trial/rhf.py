@@ -68,9 +68,20 @@ def overlap_u(walker, trial_data: rhf_trial):
 overlap_u.batched = _overlap_u_batched
 
 
+def _overlap_g_batched(walkers, trial_data: rhf_trial):
+    return engine.overlap_g(walkers, trial_data.mo_coeff, trial_data.is_real)
+
+
+def overlap_g(walker, trial_data: rhf_trial):
+    """det(vstack(C^H W_top, C^H W_bot)) for one (2n, 2o) walker (trial/rhf.py:47-53)."""
+    return _overlap_g_batched(torch.as_tensor(walker)[None], trial_data)[0]
+
+
+overlap_g.batched = _overlap_g_batched
+
+
 def make_rhf_trial_ops(sys: system) -> trial_ops:
-    """trial/rhf.py:56-71; restricted and unrestricted walkers run on the
-    CUDA engine (generalized walkers are not built)."""
+    """trial/rhf.py:56-71."""
     if sys.nup != sys.ndn:
         raise ValueError("RHF requires nelec[0] == nelec[1].")
     wk = sys.walker_kind.lower()
@@ -79,5 +90,5 @@ def make_rhf_trial_ops(sys: system) -> trial_ops:
     if wk == "unrestricted":
         return trial_ops(overlap=overlap_u, get_rdm1=get_rdm1)
     if wk == "generalized":
-        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
+        return trial_ops(overlap=overlap_g, get_rdm1=get_rdm1)
     raise ValueError(f"unknown walker_kind: {sys.walker_kind}")

@@ -1,5 +1,6 @@
 """Walker batches and population operations (walkers.py:1-265 of the
-reference), restricted and unrestricted walkers on the CUDA engine.
+reference), restricted, unrestricted and generalized walkers on the CUDA
+engine.
 
 Unrestricted walkers are the reference's pair (w_up, w_dn); this package
 returns the pair as the two halves of one (2, W, n, o) device tensor
@@ -48,7 +49,22 @@ def init_walkers(sys: system, rdm1, n_walkers: int):
                             wd.unsqueeze(0).expand(n_walkers, *wd.shape)]).contiguous()
         return engine.pair_views(pair)
     if wk == "generalized":
-        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
+        ne = sys.nup + sys.ndn
+        n = sys.norb
+        if rdm1.dim() == 2:
+            if rdm1.shape[0] != 2 * n or rdm1.shape[1] != 2 * n:
+                raise ValueError("For generalized walkers, a 2D rdm1 must have shape (2*norb, 2*norb).")
+            w0 = _natorbs(engine.as_device(rdm1, engine.C128), ne).to(engine.C128)
+        else:
+            if rdm1.dim() != 3 or rdm1.shape[0] != 2:
+                raise ValueError("Expected rdm1 with shape (2, norb, norb) for generalized init from spin blocks.")
+            dm = engine.as_device(rdm1, engine.C128)
+            up = _natorbs(dm[0], sys.nup).to(engine.C128)
+            dn = _natorbs(dm[1], sys.ndn).to(engine.C128)
+            w0 = torch.zeros((2 * n, ne), dtype=engine.C128, device=up.device)
+            w0[:n, :sys.nup] = up
+            w0[n:, sys.nup:] = dn
+        return w0.unsqueeze(0).expand(n_walkers, *w0.shape).contiguous()
     raise ValueError(f"unknown walker_kind: {wk}")
 
 
@@ -107,7 +123,7 @@ def apply_chunked_prop(w, fields, prop_fn: Callable, n_chunks: int, *args, **kwa
 def orthogonalize(w, walker_kind: str):
     """QR with diag(R) >= 0 (walkers.py:183-203); returns (Q, det(R)^2) for
     restricted walkers, ((Q_up, Q_dn), det(R_up) det(R_dn)) for
-    unrestricted ones."""
+    unrestricted ones, (Q, det(R)) for generalized ones."""
     wk = walker_kind.lower()
     if wk == "restricted":
         q, det_r = engine.orthogonalize(w)
@@ -118,7 +134,7 @@ def orthogonalize(w, walker_kind: str):
         q, det_r = engine.orthogonalize(p.reshape(2 * W, *p.shape[2:]))
         return engine.pair_views(q.reshape(p.shape)), det_r[:W] * det_r[W:]
     if wk == "generalized":
-        raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
+        return engine.orthogonalize(w)
     raise ValueError(f"unknown walker_kind: {walker_kind}")
 
 
@@ -153,9 +169,7 @@ def stochastic_reconfiguration(w, weights, zeta: float, walker_kind: str):
     if wk == "unrestricted":
         p, weights_new, _ = engine.stochastic_reconfiguration_u(w, weights, float(zeta))
         return engine.pair_views(p), weights_new
-    if wk != "restricted":
-        if wk == "generalized":
-            raise ValueError("walker_kind 'generalized' is not supported by the CUDA engine")
+    if wk not in ("restricted", "generalized"):
         raise ValueError(f"unknown walker_kind: {walker_kind}")
     w_new, weights_new, _ = engine.stochastic_reconfiguration(w, weights, float(zeta))
     return w_new, weights_new

@@ -425,6 +425,27 @@ int afq_block_u(const afq_problem* pb, const afq_params* p, const afq_state* st,
                 double zeta, uint64_t seed, uint64_t counter, double* block_energy, double* block_weight,
                 int32_t* sr_idx, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- generalized walkers (walker_kind "generalized" with the RHF trial:
+ * meas/rhf.py:103-130, prop/chol_afqmc_ops.py:141-197) ----------------------
+ *
+ * Walkers (W, 2n, 2o) complex128: the up block of rows over the down block;
+ * d->norb = n, d->nocc = o (per spin), mo_coeff the RHF trial (n x o).
+ * Overlap det(m), m = vstack(C^H W_top, C^H W_bot); force bias
+ * L~ vec(G_uu + G_dd) of G_half = solve(m^T, W^T) (2o x 2n); Trotter: both
+ * halves with the walker's V.  afq_orthogonalize and afq_stochastic_-
+ * reconfiguration with dims (W, 2n, 2o) orthonormalise and reconfigure
+ * them.  The reference has no generalized energy kernel.  Binary64 form.
+ * workspace: afq_g_workspace bytes. */
+size_t afq_g_workspace(const afq_dims* d, int32_t n_chunks);
+int afq_overlap_g(const afq_dims* d, const double* mo_coeff, const double* walkers, double* overlaps,
+                  void* workspace, size_t workspace_bytes, void* stream);
+int afq_force_bias_g(const afq_dims* d, const double* mo_coeff, const double* rot_chol, const double* walkers,
+                     double* force_bias, void* workspace, size_t workspace_bytes, void* stream);
+int afq_apply_trotter_g(const afq_dims* d, int32_t n_terms, double sqrt_dt, int32_t n_chunks,
+                        const double* chol, const double* exp_h1_half, const double* walkers,
+                        const double* shifted_fields, double* walkers_out, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* ---- integrals (integrals.py:3-46) ---------------------------------------
  *
  * modified_cholesky: pivoted Cholesky vectors of the 4-fold symmetric ERI

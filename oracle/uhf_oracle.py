@@ -1,6 +1,6 @@
-"""CPU FP64 oracle for unrestricted walkers with the RHF trial (walker_kind
-"unrestricted").  TEST INFRASTRUCTURE ONLY: the checker for the engine's
-afq_*_u entry points.
+"""CPU FP64 oracle for unrestricted and generalized walkers with the RHF
+trial (walker_kind "unrestricted", "generalized").  TEST INFRASTRUCTURE
+ONLY: the checker for the engine's afq_*_u and afq_*_g entry points.
 
 Restates meas/rhf.py:53-100 (overlap_u, force_bias_kernel_u,
 energy_kernel_u), prop/chol_afqmc_ops.py:118-183 (the unrestricted Trotter
@@ -120,3 +120,47 @@ def block_u(prob: O.Problem, params: O.Params, st: StateU, fields_steps, zeta):
     st = replace(st, wu=st.wu[idx], wd=st.wd[idx], weights=np.full(st.weights.shape, cw[-1] / st.weights.shape[0]),
                  overlaps=st.overlaps[idx])
     return st, {"energy": float(e_block), "weight": float(wsum)}, idx
+
+
+# --------------------------------------------------------------------------
+# generalized walkers (W, 2n, 2o) with the RHF trial: meas/rhf.py:103-130,
+# prop/chol_afqmc_ops.py:141-197 (the reference has no generalized energy)
+# --------------------------------------------------------------------------
+
+
+def _m_g(w, mo):
+    n = mo.shape[0]
+    cH = mo.conj().T
+    return np.concatenate([cH[None] @ w[:, :n, :], cH[None] @ w[:, n:, :]], axis=1)
+
+
+def overlap_g(w, mo):
+    """det(vstack(C^H W_top, C^H W_bot)).  meas/rhf.py:103-109."""
+    return np.linalg.det(_m_g(w, mo))
+
+
+def force_bias_g(w, meas_ctx: O.MeasCtx, mo):
+    """L~_flat vec(G_up + G_dn) of G_half = solve(m^T, W^T).  meas/rhf.py:112-130."""
+    n, o = mo.shape
+    g = np.linalg.solve(np.swapaxes(_m_g(w, mo), 1, 2), np.swapaxes(w, 1, 2))  # (W, 2o, 2n)
+    gs = g[:, :o, :n] + g[:, o:, n:]
+    return gs.reshape(gs.shape[0], -1) @ meas_ctx.rot_chol_flat.T
+
+
+def apply_trotter_g(w, shifted, ctx: O.PropCtx, chol_flat, n_terms):
+    """Both halves with the walker's V (prop/chol_afqmc_ops.py:141-197)."""
+    n = ctx.exp_h1_half.shape[0]
+    top = O.apply_trotter_r(w[:, :n, :], shifted, ctx, chol_flat, n_terms)
+    bot = O.apply_trotter_r(w[:, n:, :], shifted, ctx, chol_flat, n_terms)
+    return np.concatenate([top, bot], axis=1)
+
+
+def step_g(prob: O.Problem, params: O.Params, st: O.State, fields) -> O.State:
+    """prop/afqmc.py:74-147 with generalized walkers in st.walkers."""
+    fb = force_bias_g(st.walkers, prob.meas_ctx, prob.mo_coeff)
+    ctx = prob.prop_ctx
+    fs = -ctx.sqrt_dt * (1.0j * fb - ctx.mf_shifts)
+    w = apply_trotter_g(st.walkers, fields - fs, ctx, prob.chol_flat, params.n_exp_terms)
+    ov_new = overlap_g(w, prob.mo_coeff)
+    _, w_new, pop = O.step_weights(prob, params, st, fields, fb, ov_new)
+    return O.State(walkers=w, weights=w_new, overlaps=ov_new, pop_control_ene_shift=pop, e_estimate=st.e_estimate)

@@ -216,9 +216,10 @@ def test_generic_block_path_equals_fused(api):
 
 
 def test_api_errors(api):
-    sys_g = api["system"](norb=4, nelec=(2, 2), walker_kind="generalized")
+    sys_x = api["system"](norb=4, nelec=(2, 2), walker_kind="generalized")
+    object.__setattr__(sys_x, "walker_kind", "bogus")
     with pytest.raises(ValueError):
-        api["make_rhf_meas_ops"](sys_g)
+        api["make_rhf_meas_ops"](sys_x)
     with pytest.raises(ValueError):
         api["make_rhf_trial_ops"](api["system"](norb=4, nelec=(2, 1), walker_kind="restricted"))
     with pytest.raises(ValueError):

@@ -135,3 +135,91 @@ def test_driver_runs_unrestricted(cuda, capsys):
                                             trial_data=kw["trial_data"], meas_ops=kw["meas_ops"],
                                             trial_ops=t_ops, block_fn=afqmc_block)
     assert np.isfinite(mu) and err >= 0 and e_all.shape[0] >= 90
+
+
+# ---- generalized walkers (W, 2n, 2o) ------------------------------------------
+
+def _gwalkers(H, W, seed=0):
+    rng = np.random.default_rng(seed)
+    mo = H["mo_coeff"]
+    n, o = mo.shape
+    base = np.zeros((2 * n, 2 * o), complex)
+    base[:n, :o] = mo
+    base[n:, o:] = mo
+    return base[None] + 0.3 * (rng.normal(size=(W, 2 * n, 2 * o)) + 1j * rng.normal(size=(W, 2 * n, 2 * o)))
+
+
+def test_generalized_kernels_match_oracle(cuda):
+    from ad_afqmc_prototype_gb300 import engine
+    from oracle import afqmc_oracle as O
+    from oracle import uhf_oracle as U
+    H = _ham()
+    W = 8
+    w = _gwalkers(H, W)
+    prob = O.make_problem(H["h0"], H["h1"], H["chol"], H["mo_coeff"], 0.01)
+    sys_, t_ops, kw = _objects(H, W, "generalized")
+    mc, trial = kw["meas_ctx"], kw["trial_data"]
+    wt = torch.as_tensor(w, device="cuda")
+    np.testing.assert_allclose(engine.overlap_g(wt, trial.mo_coeff, True).cpu().numpy(),
+                               U.overlap_g(w, H["mo_coeff"]), rtol=1e-11)
+    fb = engine.force_bias_g(wt, trial.mo_coeff, mc.rot_chol, True).cpu().numpy()
+    ref = U.force_bias_g(w, prob.meas_ctx, H["mo_coeff"])
+    np.testing.assert_allclose(fb, ref, rtol=1e-11, atol=1e-11 * np.abs(ref).max())
+    rng = np.random.default_rng(1)
+    xs = rng.normal(size=(W, H["chol"].shape[0])) + 0.1j * rng.normal(size=(W, H["chol"].shape[0]))
+    out = kw["prop_ops"].apply_trotter.batched(wt, torch.as_tensor(xs, device="cuda"), kw["prop_ctx"], 6)
+    np.testing.assert_allclose(out.cpu().numpy(), U.apply_trotter_g(w, xs, prob.prop_ctx, prob.chol_flat, 6),
+                               rtol=1e-12, atol=1e-12)
+
+
+def test_generalized_step_matches_oracle_and_restricted(cuda):
+    """A generalized step against the oracle; block-diagonal walkers
+    [[W, 0], [0, W]] follow the restricted walkers W (same weights)."""
+    from ad_afqmc_prototype_gb300.prop.afqmc import afqmc_step, init_prop_state
+    from oracle import afqmc_oracle as O
+    from oracle import uhf_oracle as U
+    H = _ham(n=10, o=3, G=24, seed=8)
+    W = 16
+    n, o = H["mo_coeff"].shape
+    sys_r, t_r, kw_r = _objects(H, W, "restricted")
+    sys_g, t_g, kw_g = _objects(H, W, "generalized")
+    sr = init_prop_state(sys=sys_r, n_walkers=W, seed=5, ham_data=kw_r["ham_data"], trial_ops_=t_r,
+                         trial_data=kw_r["trial_data"], meas_ops=kw_r["meas_ops"])
+    wr = sr.walkers.cpu().numpy()
+    wg = np.zeros((W, 2 * n, 2 * o), complex)
+    wg[:, :n, :o] = wr
+    wg[:, n:, o:] = wr
+    sg = init_prop_state(sys=sys_g, n_walkers=W, seed=5, ham_data=kw_g["ham_data"], trial_ops_=t_g,
+                         trial_data=kw_g["trial_data"], meas_ops=kw_g["meas_ops"], initial_walkers=wg,
+                         initial_e_estimate=sr.e_estimate)
+    np.testing.assert_allclose(sg.overlaps.cpu().numpy(), sr.overlaps.cpu().numpy(), rtol=1e-11)
+    step_kw = {k: v for k, v in kw_g.items() if k != "sys"}
+    step_kw_r = {k: v for k, v in kw_r.items() if k != "sys"}
+    prob = O.make_problem(H["h0"], H["h1"], H["chol"], H["mo_coeff"], 0.01)
+    op = O.Params(dt=0.01)
+    ost = O.State(walkers=wg, weights=np.ones(W), overlaps=sg.overlaps.cpu().numpy(),
+                  pop_control_ene_shift=float(sg.pop_control_ene_shift), e_estimate=float(sg.e_estimate))
+    rng = np.random.default_rng(3)
+    for k in range(3):
+        f = rng.normal(size=(W, H["chol"].shape[0]))
+        sg = afqmc_step(sg, fields=f, **step_kw)
+        sr = afqmc_step(sr, fields=f, **step_kw_r)
+        ost = U.step_g(prob, op, ost, f)
+        np.testing.assert_allclose(sg.walkers.cpu().numpy(), ost.walkers, rtol=0, atol=1e-11)
+        np.testing.assert_allclose(sg.weights.cpu().numpy(), ost.weights, rtol=1e-11, atol=1e-14)
+        np.testing.assert_allclose(sg.weights.cpu().numpy(), sr.weights.cpu().numpy(), rtol=1e-11, atol=1e-14)
+        np.testing.assert_allclose(sg.walkers[:, :n, :o].cpu().numpy(), sr.walkers.cpu().numpy(), rtol=0, atol=1e-11)
+
+
+def test_generalized_block_has_no_energy_kernel(cuda):
+    """As in the reference, generalized meas ops have no energy kernel: the
+    block's measurement raises KeyError naming the available kernels."""
+    from ad_afqmc_prototype_gb300.prop.afqmc import init_prop_state
+    from ad_afqmc_prototype_gb300.prop.blocks import afqmc_block
+    H = _ham(n=8, o=2, G=12, seed=9)
+    sys_g, t_g, kw_g = _objects(H, 8, "generalized", n_prop_steps=2)
+    st = init_prop_state(sys=sys_g, n_walkers=8, seed=5, ham_data=kw_g["ham_data"], trial_ops_=t_g,
+                         trial_data=kw_g["trial_data"], meas_ops=kw_g["meas_ops"], initial_e_estimate=0.0)
+    assert tuple(st.walkers.shape) == (8, 16, 4)
+    with pytest.raises(KeyError, match="available"):
+        afqmc_block(st, **kw_g)
