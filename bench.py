@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--grad-only", action="store_true",
                     help="print only the differentiated-energy measurement (60-orbital workload)")
     ap.add_argument("--grad-blocks", type=int, default=20, help="blocks of the differentiated run")
+    ap.add_argument("--no-large", action="store_true", help="skip the 400-orbital workload line")
     return ap.parse_args()
 
 
@@ -323,6 +324,8 @@ def run_ours(args, rank, world):
         out["control_variate"] = cvline
     if rank == 0 and not args.no_grad:
         out["differentiation"] = run_grad(n_blocks=args.grad_blocks)
+    if rank == 0 and not args.no_large and args.workload != "c5_n400_o50_g2000_w1024":
+        out["large_workload"] = run_large(args.precision)
     if compare:
         out["plain_fp64"] = compare
         out["ratio_vs_plain_fp64"] = round(value / compare["value"], 2)
@@ -401,6 +404,36 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
             "backward_over_forward": round(bwd_ms / fwd_ms, 2),
             "walker_steps_per_s_forward_backward": round(wl.n_walkers * n_blocks * STEPS_PER_BLOCK
                                                         / ((fwd_ms + bwd_ms) / 1000.0), 1)}
+
+
+def run_large(precision, workload="c5_n400_o50_g2000_w1024", blocks=2):
+    """The 400-orbital workload (nocc 50, nchol 2000, 1024 walkers) in the
+    chosen form: one warm-up and `blocks` timed blocks, then one block of the
+    binary64 form from the same state and fields for the ratio and |dE|."""
+    import torch
+    from ad_afqmc_prototype_gb300 import engine, synth
+    from ad_afqmc_prototype_gb300.prop.afqmc import device_state
+    wl = synth.WORKLOADS[workload]
+    W = wl.n_walkers
+    env = make_engine_state(wl, W, precision)
+    st = device_state(env["state"], inplace=True)
+    ctr = 0
+    engine.block(env["prob"], env["params"], st, 11, ctr)
+    ctr += STEPS_PER_BLOCK + 1
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(blocks):
+        engine.block(env["prob"], env["params"], st, 11, ctr)
+        ctr += STEPS_PER_BLOCK + 1
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / blocks
+    value = W * STEPS_PER_BLOCK / (ms / 1000.0)
+    cmp = compare_with_fp64(env, st, W)
+    return {"workload": workload, "precision": precision, "value": round(value, 3), "unit": UNIT,
+            "ms_per_step": round(ms, 2), "plain_fp64": cmp, "ratio_vs_plain_fp64": round(value / cmp["value"], 2),
+            "note": "norb 400 > 256: the Taylor series runs on the fp32 SIMT kernel; the QRs in global memory"}
 
 
 def run_cv(args, env, st, W, world, seed, ctr):

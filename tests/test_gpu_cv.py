@@ -157,3 +157,29 @@ def test_cv_unbiased_and_network_reduces_variance(cuda):
     print("variance with network %.3e, sample alone %.3e" % (with_net.var(ddof=1), without.var(ddof=1)))
     assert with_net.var(ddof=1) < 0.25 * without.var(ddof=1)
     assert engine.workspace_status() == 0
+
+
+def test_cv_full_sample_equals_exact_at_nocc_50(cuda):
+    """400 orbitals, nocc 50 (the unfused exchange path): with every walker
+    sampled the control-variate energy equals the exact measurement."""
+    from ad_afqmc_prototype_gb300 import engine
+    from ad_afqmc_prototype_gb300.prop.cv import ExchangeControlVariate
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_gpu_mixed import _setup, _dstate
+    W = 64
+    pb, prb, st = _setup("c5_n400_o50_g2000_w1024", W, "mixed_fast", n_prop_steps=2, qr_every=0)
+    s0 = _dstate(st)
+    engine.block(pb, prb, s0, 7, 0)
+    z = prb.__class__(**{**prb.__dict__, "n_prop_steps": 0})
+    e_exact, _ = engine.block(pb, z, _clone(s0), 7, 50, zeta=0.5)
+    cv = ExchangeControlVariate(hidden=H, sample_fraction=1.0, seed=4)
+    cv.mode = "record"
+    engine.block(pb, z, _clone(s0), 7, 50, zeta=0.5, cv=cv.block_args(W))
+    cv.after_block()
+    cv.fit(epochs=2, batch=32)
+    cv.mode = "estimate"
+    e_cv, _ = engine.block(pb, z, _clone(s0), 7, 50, zeta=0.5, cv=cv.block_args(W))
+    cv.after_block()
+    assert abs(float(e_cv) - float(e_exact)) < 1e-5, (float(e_cv), float(e_exact))
+    assert engine.workspace_status() == 0
