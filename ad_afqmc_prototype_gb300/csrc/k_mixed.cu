@@ -384,8 +384,9 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 // ------------------------------------------- overlap + force-bias operand
 // Mixed-form replacement of k_green for the overlap (meas/rhf.py:22-24) and
 // the next step's force-bias operand (meas/rhf.py:15-19, 27-33):
-//   m = C^H W in binary64; LU with partial pivoting in binary64 gives
-//   det(m) and the overlap det(m)^2 -- the only binary64 work;
+//   m = C^H W; LU with partial pivoting gives det(m) and the overlap
+//   det(m)^2 (binary64, or with DF in double-float with the determinant's
+//   product of pivots in binary64);
 //   m^-1 by fp32 Gauss-Jordan on a float copy of m, and
 //   G_half^T = W m^-1 in fp32, written as the bf16 split operand (which
 //   resolves at most ~2^-24, so fp32 here costs no accuracy downstream)
@@ -413,6 +414,55 @@ __device__ __forceinline__ void df_acc(float& s, float& e, float ch, float cl, f
     e = __fadd_rn(e, __fadd_rn(__fadd_rn(r, pe), __fmaf_rn(ch, wl, __fmul_rn(cl, wh))));
 }
 
+// Double-float (fp32 pair, ~2^-44) complex arithmetic for the overlap's LU,
+// after the QD library's algorithms (Hida, Li and Bailey): Knuth's two-sum,
+// the fma two-product, the "sloppy" pair addition, and the reciprocal by one
+// Newton-Raphson step from the fp32 reciprocal.  A complex value is a float4
+// (re hi, re lo, im hi, im lo).
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 df_quick(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float2 s = df_two_sum(a.x, b.x);
+    return df_quick(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e));
+    return df_quick(p, e);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float4 zdf_mul(float4 a, float4 b) {
+    const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+    const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
+    const float2 re = df_add(df_mul(ar, br), df_neg(df_mul(ai, bi)));
+    const float2 im = df_add(df_mul(ar, bi), df_mul(ai, br));
+    return make_float4(re.x, re.y, im.x, im.y);
+}
+__device__ __forceinline__ float4 zdf_sub(float4 a, float4 b) {
+    const float2 re = df_add(make_float2(a.x, a.y), make_float2(-b.x, -b.y));
+    const float2 im = df_add(make_float2(a.z, a.w), make_float2(-b.z, -b.w));
+    return make_float4(re.x, re.y, im.x, im.y);
+}
+__device__ __forceinline__ float2 df_rcp(float2 d) {
+    const float2 r0 = make_float2(1.0f / d.x, 0.f);
+    const float2 e = df_add(make_float2(1.f, 0.f), df_neg(df_mul(d, r0)));  // 1 - d r0
+    return df_add(r0, df_mul(r0, e));
+}
+__device__ __forceinline__ float4 zdf_rcp(float4 p) {  // 1 / (a + i b) = (a - i b) / (a^2 + b^2)
+    const float2 a = make_float2(p.x, p.y), b = make_float2(p.z, p.w);
+    const float2 inv = df_rcp(df_add(df_mul(a, a), df_mul(b, b)));
+    const float2 re = df_mul(a, inv), im = df_neg(df_mul(b, inv));
+    return make_float4(re.x, re.y, im.x, im.y);
+}
+
 template <int MA, bool STAGE_W, bool DF>
 __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
@@ -421,12 +471,14 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
                                                        const float2* __restrict__ cs) {
     extern __shared__ double2 smd[];
     double2* m = smd;                              // o x o binary64 (LU in place)
+    float4* md = (float4*)smd;                     // DF: the same storage as double-float pairs
     float2* mf = (float2*)(m + o * o);             // o x o fp32 copy -> Gauss-Jordan
     float2* invf = mf + o * o;                     // o x o fp32 inverse
     float2* wf = invf + o * o;                     // n x o fp32 copy of W (its hi part)
     float2* wl = wf + (size_t)OS_CH * o;           // DF: lo part of a chunk of OS_CH rows
     __shared__ int s_piv;
     __shared__ double2 s_rp;
+    __shared__ float4 s_rpd;
     __shared__ double2 s_det;
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
@@ -467,9 +519,9 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             for (int k = 0; k < MA; ++k) {
                 const int a = ag + AG * k;
                 if (a < o) {
-                    const double2 v = make_double2((double)sr[k] + (double)er[k], (double)si[k] + (double)ei[k]);
-                    m[a * o + b] = v;
-                    mf[a * o + b] = make_float2((float)v.x, (float)v.y);
+                    const float2 re = df_quick(sr[k], er[k]), im = df_quick(si[k], ei[k]);
+                    md[a * o + b] = make_float4(re.x, re.y, im.x, im.y);
+                    mf[a * o + b] = make_float2(re.x, im.x);
                 }
             }
         }
@@ -518,7 +570,13 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             double best = -1.0;
             int bi = k;
             for (int r = k + lane; r < o; r += 32) {
-                const double v = cabs2(m[r * o + k]);
+                double v;
+                if (DF) {
+                    const float4 x = md[r * o + k];
+                    v = (double)x.x * x.x + (double)x.z * x.z;
+                } else {
+                    v = cabs2(m[r * o + k]);
+                }
                 if (v > best) { best = v; bi = r; }
             }
 #pragma unroll
@@ -529,10 +587,17 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             }
             if (lane == 0) {
                 s_piv = bi;
-                const double2 piv = m[bi * o + k];
+                double2 piv;
+                if (DF) {
+                    const float4 p = md[bi * o + k];
+                    piv = make_double2((double)p.x + (double)p.y, (double)p.z + (double)p.w);
+                    s_rpd = zdf_rcp(p);
+                } else {
+                    piv = m[bi * o + k];
+                    s_rp = cdiv(make_double2(1.0, 0.0), piv);
+                }
                 const double2 d = cmul(s_det, piv);
                 s_det = (bi != k) ? make_double2(-d.x, -d.y) : d;
-                s_rp = cdiv(make_double2(1.0, 0.0), piv);
             }
         } else if (k < o && wid == 1) {
             float best = -1.f;
@@ -570,7 +635,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
         const int p = s_piv, p2 = s_piv2;
         for (int j = tid; j < 3 * o; j += blockDim.x) {
             if (j < o) {
-                if (p != k) {
+                if (p != k) {  // 16-byte entries: binary64 complex, or double-float
                     const double2 t = m[k * o + j];
                     m[k * o + j] = m[p * o + j];
                     m[p * o + j] = t;
@@ -584,13 +649,22 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             }
         }
         __syncthreads();
-        const double2 rp = s_rp;
         const float2 rpf = s_rpf2[k & 1];
         const int rem = o - k - 1;
-        for (int e = tid; e < rem * rem; e += blockDim.x) {
-            const int r = k + 1 + e / rem, j = k + 1 + e % rem;
-            const double2 l = cmul(m[r * o + k], rp);
-            m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
+        if (DF) {
+            const float4 rpd = s_rpd;
+            for (int e = tid; e < rem * rem; e += blockDim.x) {
+                const int r = k + 1 + e / rem, j = k + 1 + e % rem;
+                const float4 l = zdf_mul(md[r * o + k], rpd);
+                md[r * o + j] = zdf_sub(md[r * o + j], zdf_mul(l, md[k * o + j]));
+            }
+        } else {
+            const double2 rp = s_rp;
+            for (int e = tid; e < rem * rem; e += blockDim.x) {
+                const int r = k + 1 + e / rem, j = k + 1 + e % rem;
+                const double2 l = cmul(m[r * o + k], rp);
+                m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
+            }
         }
         for (int e = tid; e < o * 2 * o; e += blockDim.x) {
             const int r = e / (2 * o), j = e % (2 * o);
