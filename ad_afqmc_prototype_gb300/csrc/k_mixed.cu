@@ -845,18 +845,27 @@ __device__ __forceinline__ void cq_gram(int n, int o, int ld, const float2* Ah, 
 // R[k][j] at Gm[k o + j]); thread 0 multiplies the pivots into *det.
 // Returns (uniformly) whether a pivot was not above rel_tol times the
 // column's diagonal entry before elimination (d0, o entries of scratch); such
-// a pivot becomes 1 with a zero row.
-__device__ __forceinline__ bool cq_chol(int o, double2* Gm, double* det, double rel_tol, double* d0) {
+// a pivot becomes 1 with a zero row.  Thread 0 takes each pivot's square
+// root and reciprocal and hands them to the block through piv[2] (a
+// negative reciprocal marks a rejected pivot).
+__device__ __forceinline__ bool cq_chol(int o, double2* Gm, double* det, double rel_tol, double* d0,
+                                        double* piv) {
     for (int k = threadIdx.x; k < o; k += blockDim.x) d0[k] = Gm[k * o + k].x;
     __syncthreads();
     bool bad = false;
     for (int k = 0; k < o; ++k) {
-        const double gkk = Gm[k * o + k].x;
-        const bool b = !(gkk > rel_tol * d0[k]) || !(gkk > 0.0);
-        bad |= b;
-        const double rkk = b ? 1.0 : sqrt(gkk), ir = 1.0 / rkk;
-        if (threadIdx.x == 0) *det *= rkk;
+        if (threadIdx.x == 0) {
+            const double gkk = Gm[k * o + k].x;
+            const bool b = !(gkk > rel_tol * d0[k]) || !(gkk > 0.0);
+            const double r = b ? 1.0 : sqrt(gkk);
+            *det *= r;
+            piv[0] = r;
+            piv[1] = b ? -1.0 : 1.0 / r;
+        }
         __syncthreads();
+        const double rkk = piv[0], ir = piv[1];
+        const bool b = ir < 0.0;
+        bad |= b;
         for (int j = k + threadIdx.x; j < o; j += blockDim.x) {
             const double2 g = Gm[k * o + j];
             Gm[k * o + j] = j == k ? make_double2(rkk, 0.0) : (b ? make_double2(0.0, 0.0) : cscale(g, ir));
@@ -872,18 +881,19 @@ __device__ __forceinline__ bool cq_chol(int o, double2* Gm, double* det, double 
     return bad;
 }
 
-// R (upper triangle of Gm, binary64) as double-float pairs for the solve:
+// R (upper triangle of Gm, binary64) as double-float pairs for the solve, in
+// place (Rd aliases Gm; each entry is read and rewritten by one thread):
 // Rd[j o + k] = (re hi, re lo, im hi, im lo); rinv[k] = (hi, lo) of 1 / R_kk.
-__device__ __forceinline__ void cq_rsplit(int o, const double2* Gm, float4* Rd, float2* rinv) {
+__device__ __forceinline__ void cq_rsplit(int o, double2* Gm, float4* Rd, float2* rinv) {
     for (int e = threadIdx.x; e < o * o; e += blockDim.x) {
         const double2 r = Gm[e];
+        if (e % (o + 1) == 0) {
+            const double v = 1.0 / r.x;
+            const float h = (float)v;
+            rinv[e / (o + 1)] = make_float2(h, (float)(v - (double)h));
+        }
         const float rh = (float)r.x, ih = (float)r.y;
         Rd[e] = make_float4(rh, (float)(r.x - (double)rh), ih, (float)(r.y - (double)ih));
-    }
-    for (int k = threadIdx.x; k < o; k += blockDim.x) {
-        const double v = 1.0 / Gm[k * o + k].x;
-        const float h = (float)v;
-        rinv[k] = make_float2(h, (float)(v - (double)h));
     }
     __syncthreads();
 }
@@ -924,41 +934,54 @@ __device__ __forceinline__ void cq_solve(int n, int o, int ld, float2* Ah, float
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) k_cholqr2(int n, int o, const double2* __restrict__ win,
-                                                 double2* __restrict__ wout, double2* __restrict__ det_out) {
+__global__ void __launch_bounds__(256, 2) k_cholqr2(int n, int o, const double2* __restrict__ win,
+                                                    double2* __restrict__ wout, double2* __restrict__ det_out) {
     extern __shared__ double2 csm[];
     __shared__ double s_det;  // prod diag(R1) prod diag(R2) = prod diag(R)
     __shared__ double s_d0[64];
+    __shared__ double s_piv[2];
     const int ld = n | 1;
-    double2* Gm = csm;                                // o x o binary64
-    float4* Rd = (float4*)(Gm + o * o);               // o x o double-float R
-    float2* rinv = (float2*)(Rd + o * o);             // o
+    double2* Gm = csm;                                // o x o binary64 Gram matrix, then R
+    float4* Rd = (float4*)Gm;                         // o x o double-float R, in place of Gm
+    float2* rinv = (float2*)(Gm + o * o);             // o
     float2* Ah = rinv + ((o + 1) & ~1);               // ld x o: A[j ld + i] = W[i, j], hi
     float2* Al = Ah + (size_t)ld * o;                 // lo
     const int w = blockIdx.x;
     const double2* Wp = win + (size_t)w * n * o;
-    for (int e = threadIdx.x; e < n * o; e += blockDim.x) {
-        const double2 x = Wp[e];
-        const float2 h = make_float2((float)x.x, (float)x.y);
-        const size_t d = (size_t)(e % o) * ld + e / o;
-        Ah[d] = h;
-        Al[d] = make_float2((float)(x.x - (double)h.x), (float)(x.y - (double)h.y));
+    constexpr int LU = 8;  // loads in flight per thread
+    for (int e0 = 0; e0 < n * o; e0 += LU * blockDim.x) {
+        double2 x[LU];
+#pragma unroll
+        for (int u = 0; u < LU; ++u) {
+            const int e = e0 + u * blockDim.x + threadIdx.x;
+            if (e < n * o) x[u] = Wp[e];
+        }
+#pragma unroll
+        for (int u = 0; u < LU; ++u) {
+            const int e = e0 + u * blockDim.x + threadIdx.x;
+            if (e < n * o) {
+                const float2 h = make_float2((float)x[u].x, (float)x[u].y);
+                const size_t d = (size_t)(e % o) * ld + e / o;
+                Ah[d] = h;
+                Al[d] = make_float2((float)(x[u].x - (double)h.x), (float)(x[u].y - (double)h.y));
+            }
+        }
     }
     if (threadIdx.x == 0) s_det = 1.0;
     __syncthreads();
     cq_gram<false>(n, o, ld, Ah, Al, Gm);
     __syncthreads();
-    if (cq_chol(o, Gm, &s_det, 1e-5, s_d0)) {  // fp32 cannot resolve W's conditioning: double-float G1
+    if (cq_chol(o, Gm, &s_det, 1e-5, s_d0, s_piv)) {  // fp32 cannot resolve W's conditioning: double-float G1
         if (threadIdx.x == 0) s_det = 1.0;
         cq_gram<true>(n, o, ld, Ah, Al, Gm);
         __syncthreads();
-        cq_chol(o, Gm, &s_det, 0.0, s_d0);
+        cq_chol(o, Gm, &s_det, 0.0, s_d0, s_piv);
     }
     cq_rsplit(o, Gm, Rd, rinv);
     cq_solve(n, o, ld, Ah, Al, Rd, rinv);
     cq_gram<true>(n, o, ld, Ah, Al, Gm);
     __syncthreads();
-    cq_chol(o, Gm, &s_det, 0.0, s_d0);
+    cq_chol(o, Gm, &s_det, 0.0, s_d0, s_piv);
     cq_rsplit(o, Gm, Rd, rinv);
     cq_solve(n, o, ld, Ah, Al, Rd, rinv);
     double2* Wo = wout + (size_t)w * n * o;
@@ -973,7 +996,7 @@ __global__ void __launch_bounds__(256) k_cholqr2(int n, int o, const double2* __
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     if (o > 64) return fail(AFQ_E_UNSUPPORTED, "qr: nocc=%d > 64", o);
-    const size_t smem = (size_t)o * o * (sizeof(double2) + sizeof(float4)) + (size_t)((o + 1) & ~1) * sizeof(float2) +
+    const size_t smem = (size_t)o * o * sizeof(double2) + (size_t)((o + 1) & ~1) * sizeof(float2) +
                         2 * (size_t)(n | 1) * o * sizeof(float2);
     // walkers whose double-float copy does not fit in shared memory: the binary64 Householder QR
     if (smem > 220 * 1024) return launch_qr(W, n, o, win, wout, det_r, s);
