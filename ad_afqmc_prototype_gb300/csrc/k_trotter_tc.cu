@@ -213,10 +213,9 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                 if (e) {
                                     tma_load_2d(dh, &mEh, kb * 64, mt * 128, full);
                                     tma_load_2d(dm, &mEm, kb * 64, mt * 128, full);
-                                } else {
-                                    const int y = (hf * wc + w) * n + mt * 128;
-                                    tma_load_2d(dh, &mVh, kb * 64, y, full);
-                                    tma_load_2d(dm, &mVm, kb * 64, y, full);
+                                } else {  // rows past n of the last tile read as zero
+                                    tma_load_3d(dh, &mVh, kb * 64, mt * 128, hf * wc + w, full);
+                                    tma_load_3d(dm, &mVm, kb * 64, mt * 128, hf * wc + w, full);
                                 }
                                 issued[stage] = 1;
                                 issued_par[stage] = phase;
@@ -292,22 +291,29 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             const uint32_t ta = tmem + mt * TT_TCOLS + lq;            // accumulator
             const uint32_t ts = tmem + TT_SCOL + mt * TT_N + lq;      // running update
             const uint32_t tf = tmem + TT_FCOL + mt * TT_N + lq;      // fp32 copy of the row
+            // the row's loads go out 16 at a time ahead of the shared-memory
+            // writes (which the compiler may not move loads across)
 #pragma unroll
-            for (int cb = 0; cb < 32; cb += 8) {
-                uint32_t fv[16];
+            for (int hb = 0; hb < 32; hb += 16) {
+                float2 f[16];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int c = cb + u;
-                    float2 f = make_float2(0.f, 0.f);
-                    if (row && c < o) {
-                        const double2 v = Wi[c];
-                        f = make_float2((float)v.x, (float)v.y);
-                        tt_write_b(sB, i, kb0, c, f);
-                    }
-                    fv[u] = __float_as_uint(f.x);
-                    fv[8 + u] = __float_as_uint(f.y);
+                for (int u = 0; u < 16; ++u) {
+                    const int c = hb + u;
+                    const double2 v = (row && c < o) ? Wi[c] : make_double2(0.0, 0.0);
+                    f[u] = make_float2((float)v.x, (float)v.y);
                 }
-                tmem_st8x2(tf + cb, tf + 32 + cb, fv);
+#pragma unroll
+                for (int cb = 0; cb < 16; cb += 8) {
+                    uint32_t fv[16];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int c = hb + cb + u;
+                        if (row && c < o) tt_write_b(sB, i, kb0, c, f[cb + u]);
+                        fv[u] = __float_as_uint(f[cb + u].x);
+                        fv[8 + u] = __float_as_uint(f[cb + u].y);
+                    }
+                    tmem_st8x2(tf + hb + cb, tf + 32 + hb + cb, fv);
+                }
             }
             tc_fence_before();
             fence_proxy_async();
@@ -327,6 +333,30 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                 }
                 tc_fence_after();
                 const float sk = sqrt_dt / (float)(r > 0 ? r : 1);
+                if (r == R - 1) {  // W' = W + (S + (E - I) out): the one binary64 update
+#pragma unroll
+                    for (int cb = 0; cb < 32; cb += 8) {
+                        double2 wv[8];  // loaded ahead of the stores (Wi and Wr alias)
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            wv[u] = (row && cb + u < o) ? Wi[cb + u] : make_double2(0.0, 0.0);
+                        uint32_t y[32], sv[16];
+                        tmem_ld8x4(ta + cb, ta + TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb, y);
+                        tmem_ld8x2(ts + cb, ts + 32 + cb, sv);
+                        if (row) {
+#pragma unroll
+                            for (int u = 0; u < 8; ++u) {
+                                const int c = cb + u;
+                                const float yr = __uint_as_float(y[u]) + __uint_as_float(y[8 + u]);
+                                const float yi = __uint_as_float(y[16 + u]) + __uint_as_float(y[24 + u]);
+                                const float sr = __uint_as_float(sv[u]), si = __uint_as_float(sv[8 + u]);
+                                if (c < o) Wr[c] = make_double2(wv[u].x + (double)(sr + yr), wv[u].y + (double)(si + yi));
+                            }
+                        }
+                    }
+                    tc_fence_before();
+                    continue;
+                }
 #pragma unroll
                 for (int cb = 0; cb < 32; cb += 8) {
                     // Y columns cb..cb+7 of Yr and Yi (hi.hi + corrections); S and the row copy
@@ -347,28 +377,23 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                     sr = yr;
                                     si = yi;
                                     tt_write_b(sB, i, kb0, c, make_float2(fr + yr, fi + yi));
-                                } else if (r < R - 1) {  // T_r = (i sqrt_dt / r) Y
+                                } else {  // T_r = (i sqrt_dt / r) Y
                                     const float2 t = make_float2(-sk * yi, sk * yr);
                                     sr += t.x;
                                     si += t.y;
                                     if (r < n_terms) tt_write_b(sB, i, kb0, c, t);
                                     else tt_write_b(sB, i, kb0, c, make_float2(fr + sr, fi + si));  // out = W1 + sum T_k
-                                } else {  // W' = W + (S + (E - I) out): the one binary64 update
-                                    const double2 v = Wi[c];
-                                    Wr[c] = make_double2(v.x + (double)(sr + yr), v.y + (double)(si + yi));
                                 }
                             }
                             sv[u] = __float_as_uint(sr);
                             sv[8 + u] = __float_as_uint(si);
                         }
                     }
-                    if (r < R - 1) tmem_st8x2(ts + cb, ts + 32 + cb, sv);
+                    tmem_st8x2(ts + cb, ts + 32 + cb, sv);
                 }
                 tc_fence_before();
-                if (r < R - 1) {
-                    fence_proxy_async();
-                    mbar_arrive(bready);
-                }
+                fence_proxy_async();
+                mbar_arrive(bready);
             }
         }
     }
@@ -404,8 +429,8 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
         attr = true;
     }
     CUtensorMap mvh, mvm, meh, mem;
-    AFQ_TRY(make_map(&mvh, vh, 2LL * wc * n, n, n, 128));
-    AFQ_TRY(make_map(&mvm, vm, 2LL * wc * n, n, n, 128));
+    AFQ_TRY(make_map3(&mvh, vh, 2LL * wc, n, n, n, 128));
+    AFQ_TRY(make_map3(&mvm, vm, 2LL * wc, n, n, n, 128));
     AFQ_TRY(make_map(&meh, eh, n, n, n, 128));
     AFQ_TRY(make_map(&mem, em, n, n, n, 128));
     const int grid = wc < nsm ? wc : nsm;
