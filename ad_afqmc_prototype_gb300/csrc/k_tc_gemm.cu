@@ -214,7 +214,7 @@ struct Drain {
     static constexpr int THREADS = 320;
     static constexpr int EW0 = 2;  // first epilogue warp
     static constexpr int SLOTS = DTMEM_COLS / BNT;
-    static constexpr int STG = 6;
+    static constexpr int STG = BNT == 128 ? 6 : 4;
     static constexpr int B_BYTES = BNT * BK * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
     static constexpr int SMEM = STG * STAGE + 1024 + 256;
@@ -222,7 +222,8 @@ struct Drain {
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BNT >> 3) << 17) |
                                       ((uint32_t)(BM >> 4) << 24);
 };
-static_assert(Drain<128>::STG * Drain<128>::STAGE + 1024 + 256 <= 227 * 1024, "drained GEMM shared memory");
+static_assert(Drain<128>::SMEM <= 227 * 1024, "drained GEMM shared memory");
+static_assert(Drain<256>::SMEM <= 227 * 1024, "drained GEMM shared memory (256-wide tiles)");
 
 // Epilogue of the exchange-fused energy GEMM (MODE 2): a 32 x 33 fp32
 // transpose buffer per epilogue warp after the barriers.
@@ -569,7 +570,7 @@ int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long 
                                   int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<128, 1>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
+    return launch_drain<256, 1>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
 }
 
 int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
