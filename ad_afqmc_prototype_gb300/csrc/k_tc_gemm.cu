@@ -228,13 +228,14 @@ static_assert(Drain<256>::SMEM <= 227 * 1024, "drained GEMM shared memory (256-w
 // Epilogue of the exchange-fused energy GEMM (MODE 2): a 32 x 33 fp32
 // transpose buffer per epilogue warp after the barriers.
 constexpr int XT_BYTES = 8 * 32 * 33 * 4;
-static_assert(Drain<128>::SMEM + XT_BYTES <= 227 * 1024, "exchange-fused GEMM shared memory");
+constexpr int EXCH_BNT = 256;  // tile width of the exchange-fused GEMM
+static_assert(Drain<EXCH_BNT>::SMEM + XT_BYTES <= 227 * 1024, "exchange-fused GEMM shared memory");
 
 // Outputs of MODE 2 (the local energy's exchange, meas/rhf.py:36-50).  Rows
 // of the product are (walker, part, k) with 32 rows per part (k >= nocc zero)
-// and columns (g, i) with 32 per Cholesky vector, so a 128 x 128 tile holds
-// the Re and Im planes of f_g[i, k] for two walkers and four vectors.
-//   x[(w nhalf + h) 2 + part] = sum over the 64-column half h of
+// and columns (g, i) with 32 per Cholesky vector, so a 128 x 256 tile holds
+// the Re and Im planes of f_g[i, k] for two walkers and eight vectors.
+//   x[(w nhalf + h) 2 + part] = sum over the 128-column half h of
 //                               sum_{i,k} F_part[k, i] F_part[i, k]
 //   c[(w G + g) 2 + part]     = sum_k F_part[k, k]   (the trace of f_g)
 struct ExchOut {
@@ -242,7 +243,7 @@ struct ExchOut {
     float* c = nullptr;
     int G = 0;       // Cholesky vectors
     int nw = 0;      // walkers in this product
-    int nhalf = 0;   // 64-column halves per row = 2 x column tiles
+    int nhalf = 0;   // column halves per row = 2 x column tiles
 };
 
 // MODE 0: fp32 C.  MODE 1 (split): the two-piece bf16 split of each sum to
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
                     int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
     using D = Drain<BNT>;
     constexpr bool SPLIT = MODE == 1;
-    static_assert(MODE != 2 || BNT == 128, "the exchange epilogue takes 128-column tiles");
+    static_assert(MODE != 2 || BNT % 64 == 0, "the exchange epilogue takes whole 32 x 32 blocks per warp");
     constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -408,13 +409,13 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
             }
             if (!ok) break;
             if constexpr (MODE == 2) {
-                // this warp's 32 rows are (walker wl, part) rows k = lane of four 32 x 32 blocks;
-                // the thread's 64 columns are the blocks of two Cholesky vectors
+                // this warp's 32 rows are (walker wl, part) rows k = lane of 32 x 32 blocks;
+                // the thread's CW columns are the blocks of CW / 32 Cholesky vectors
                 float* tr = (float*)(smem + STG * D::STAGE + 256) + (warp - D::EW0) * 32 * 33;
                 const int wl = mb * 2 + (q >> 1), part = q & 1;
                 float ex = 0.f;
 #pragma unroll
-                for (int jj = 0; jj < 2; ++jj) {
+                for (int jj = 0; jj < CW / 32; ++jj) {
                     const int g = (nb * BNT + cb) / 32 + jj;
 #pragma unroll
                     for (int i = 0; i < 32; i += 2) {
@@ -562,7 +563,7 @@ int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, c
                             long long ldc, int* err, cudaStream_t s, int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<128, 0>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
+    return launch_drain<256, 0>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
 }
 
 int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb,
@@ -583,10 +584,10 @@ int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, 
     xo.c = c;
     xo.G = G;
     xo.nw = nw;
-    xo.nhalf = 2 * ((N + 127) / 128);
-    return launch_drain<128, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, kd, err, s, xo);
+    xo.nhalf = exchange_halves(G);
+    return launch_drain<tc::EXCH_BNT, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, kd, err, s, xo);
 }
 
-int exchange_halves(int G) { return 2 * ((32 * G + 127) / 128); }
+int exchange_halves(int G) { return 2 * ((32 * G + tc::EXCH_BNT - 1) / tc::EXCH_BNT); }
 
 }  // namespace afq
