@@ -66,6 +66,26 @@ __device__ __forceinline__ void rfma(double2& acc, double r, double2 b) {
     acc.y = fma(r, b.y, acc.y);
 }
 __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+// x = hi + lo as an fp32 pair from the binary64 fields with integer
+// operations (binary64 conversions run at the binary64 rate): hi is x cut
+// to 24 significant bits, lo the remaining 29 bits rounded to 24, so
+// |x - hi - lo| <= 2^-48 |x|.  Exponents outside [2^-74, 2^128) (zero,
+// tiny, huge, inf, nan) take the binary64 conversions.
+__device__ __forceinline__ float2 split_d2f(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
+    const unsigned e = (h >> 20) & 0x7ffu;
+    if (e < 949u || e > 1150u) {
+        const float hi = (float)x;
+        return make_float2(hi, (float)(x - (double)hi));
+    }
+    const unsigned sign = h & 0x80000000u;
+    const float hi = __uint_as_float(sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29)));
+    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075), the weight of bit 0 of l
+    const float lo = __uint_as_float(sign | __float_as_uint(__uint2float_rn(l & 0x1fffffffu) * scale));
+    return make_float2(hi, lo);
+}
 // complex division a / b (Smith's method)
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
     if (fabs(b.x) >= fabs(b.y)) {

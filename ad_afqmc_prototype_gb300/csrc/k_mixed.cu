@@ -494,9 +494,9 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             __syncthreads();
             for (int e = tid; e < rows * o; e += blockDim.x) {
                 const double2 x = Wp[(size_t)i0 * o + e];
-                const float2 h = make_float2((float)x.x, (float)x.y);
-                wf[e] = h;
-                wl[e] = make_float2((float)(x.x - (double)h.x), (float)(x.y - (double)h.y));
+                const float2 re = split_d2f(x.x), im = split_d2f(x.y);
+                wf[e] = make_float2(re.x, im.x);
+                wl[e] = make_float2(re.y, im.y);
             }
             __syncthreads();
             if (ag < AG) {
@@ -960,10 +960,10 @@ __global__ void __launch_bounds__(256, 2) k_cholqr2(int n, int o, const double2*
         for (int u = 0; u < LU; ++u) {
             const int e = e0 + u * blockDim.x + threadIdx.x;
             if (e < n * o) {
-                const float2 h = make_float2((float)x[u].x, (float)x[u].y);
+                const float2 re = split_d2f(x[u].x), im = split_d2f(x[u].y);
                 const size_t d = (size_t)(e % o) * ld + e / o;
-                Ah[d] = h;
-                Al[d] = make_float2((float)(x[u].x - (double)h.x), (float)(x[u].y - (double)h.y));
+                Ah[d] = make_float2(re.x, im.x);
+                Al[d] = make_float2(re.y, im.y);
             }
         }
     }
