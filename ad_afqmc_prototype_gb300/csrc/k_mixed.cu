@@ -414,6 +414,23 @@ __device__ __forceinline__ void df_acc(float& s, float& e, float ch, float cl, f
     e = __fadd_rn(e, __fadd_rn(__fadd_rn(r, pe), __fmaf_rn(ch, wl, __fmul_rn(cl, wh))));
 }
 
+// df_acc on two lanes at once with the paired fp32 instructions (f32x2):
+// (s, e) += c (wr, wi) for one double-float c and a pair w = (wr, wi), hi and
+// lo parts in wh and wl.  The same roundings as two df_acc calls: a
+// subtraction y - x is fma(x, -1, y), and -p comes from (-c) w exactly.
+__device__ __forceinline__ void df_acc2(float2& s, float2& e, float ch, float cl, float2 wh, float2 wl) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 c2 = make_float2(ch, ch);
+    const float2 np = __fmul2_rn(make_float2(-ch, -ch), wh);  // -p
+    const float2 pe = __ffma2_rn(c2, wh, np);                 // exact: c wh = p + pe
+    const float2 t = __ffma2_rn(np, m1, s);                   // s + p
+    const float2 v = __ffma2_rn(s, m1, t);                    // t - s
+    const float2 a2 = __ffma2_rn(__ffma2_rn(v, m1, t), m1, s);  // s - (t - v)
+    const float2 r = __ffma2_rn(__fadd2_rn(np, v), m1, a2);   // exact: s + p = t + r
+    s = t;
+    e = __fadd2_rn(e, __fadd2_rn(__fadd2_rn(r, pe), __ffma2_rn(c2, wl, __fmul2_rn(make_float2(cl, cl), wh))));
+}
+
 // Double-float (fp32 pair, ~2^-44) complex arithmetic for the overlap's LU,
 // after the QD library's algorithms (Hida, Li and Bailey): Knuth's two-sum,
 // the fma two-product, the "sloppy" pair addition, and the reciprocal by one
@@ -464,7 +481,7 @@ __device__ __forceinline__ float4 zdf_rcp(float4 p) {  // 1 / (a + i b) = (a - i
 }
 
 template <int MA, bool STAGE_W, bool DF>
-__global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const double2* __restrict__ mo,
+__global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
                                                        double2* __restrict__ ovlp_out, SplitOut split,
                                                        double2* __restrict__ green_out,
@@ -486,9 +503,9 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
     if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
         const int AG = blockDim.x / o;
         const int b = tid % o, ag = tid / o;
-        float sr[MA], er[MA], si[MA], ei[MA];
+        float2 s2[MA], e2[MA];  // (Re, Im) sums and their error terms
 #pragma unroll
-        for (int k = 0; k < MA; ++k) sr[k] = er[k] = si[k] = ei[k] = 0.f;
+        for (int k = 0; k < MA; ++k) s2[k] = e2[k] = make_float2(0.f, 0.f);
         for (int i0 = 0; i0 < n; i0 += OS_CH) {
             const int rows = min(OS_CH, n - i0);
             __syncthreads();
@@ -507,8 +524,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
                         const int a = ag + AG * k;
                         if (a < o) {
                             const float2 c = cs[(i0 + i) * o + a];  // (hi, lo) of C[i, a]
-                            df_acc(sr[k], er[k], c.x, c.y, xh.x, xl.x);
-                            df_acc(si[k], ei[k], c.x, c.y, xh.y, xl.y);
+                            df_acc2(s2[k], e2[k], c.x, c.y, xh, xl);
                         }
                     }
                 }
@@ -519,7 +535,7 @@ __global__ void __launch_bounds__(256) k_overlap_split(int n, int o, const doubl
             for (int k = 0; k < MA; ++k) {
                 const int a = ag + AG * k;
                 if (a < o) {
-                    const float2 re = df_quick(sr[k], er[k]), im = df_quick(si[k], ei[k]);
+                    const float2 re = df_quick(s2[k].x, e2[k].x), im = df_quick(s2[k].y, e2[k].y);
                     md[a * o + b] = make_float4(re.x, re.y, im.x, im.y);
                     mf[a * o + b] = make_float2(re.x, im.x);
                 }
@@ -818,18 +834,17 @@ __device__ __forceinline__ void cq_gram(int n, int o, int ld, const float2* Ah, 
         cq_entry(o, e, j, k);
         const float2* ah = Ah + (size_t)j * ld;
         const float2* bh = Ah + (size_t)k * ld;
-        float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+        float sr = 0.f, si = 0.f;
         if (DF) {
             const float2* al = Al + (size_t)j * ld;
             const float2* bl = Al + (size_t)k * ld;
-            for (int i = 0; i < n; ++i) {  // conj(a) b
+            float2 s2 = make_float2(0.f, 0.f), e2 = make_float2(0.f, 0.f);
+            for (int i = 0; i < n; ++i) {  // conj(a) b: (Re, Im) += a_r (b_r, b_i) + a_i (b_i, -b_r)
                 const float2 xh = ah[i], xl = al[i], yh = bh[i], yl = bl[i];
-                df_acc(sr, er, xh.x, xl.x, yh.x, yl.x);
-                df_acc(sr, er, xh.y, xl.y, yh.y, yl.y);
-                df_acc(si, ei, xh.x, xl.x, yh.y, yl.y);
-                df_acc(si, ei, -xh.y, -xl.y, yh.x, yl.x);
+                df_acc2(s2, e2, xh.x, xl.x, yh, yl);
+                df_acc2(s2, e2, xh.y, xl.y, make_float2(yh.y, -yh.x), make_float2(yl.y, -yl.x));
             }
-            Gm[j * o + k] = make_double2((double)sr + (double)er, (double)si + (double)ei);
+            Gm[j * o + k] = make_double2((double)s2.x + (double)e2.x, (double)s2.y + (double)e2.y);
         } else {
             for (int i = 0; i < n; ++i) {
                 const float2 x = ah[i], y = bh[i];
@@ -904,15 +919,14 @@ __device__ __forceinline__ void cq_solve(int n, int o, int ld, float2* Ah, float
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         for (int k = 0; k < o; ++k) {
             const float2 ah = Ah[(size_t)k * ld + i], al = Al[(size_t)k * ld + i];
-            float sr = ah.x, er = al.x, si = ah.y, ei = al.y;
-            for (int j = 0; j < k; ++j) {  // a -= x r
+            float2 s2 = ah, e2 = al;  // (Re, Im) and their error terms
+            for (int j = 0; j < k; ++j) {  // a -= x r: (Re, Im) += -x_r (r_r, r_i) + x_i (r_i, -r_r)
                 const float2 xh = Ah[(size_t)j * ld + i], xl = Al[(size_t)j * ld + i];
                 const float4 r = Rd[j * o + k];
-                df_acc(sr, er, -xh.x, -xl.x, r.x, r.y);
-                df_acc(sr, er, xh.y, xl.y, r.z, r.w);
-                df_acc(si, ei, -xh.x, -xl.x, r.z, r.w);
-                df_acc(si, ei, -xh.y, -xl.y, r.x, r.y);
+                df_acc2(s2, e2, -xh.x, -xl.x, make_float2(r.x, r.z), make_float2(r.y, r.w));
+                df_acc2(s2, e2, xh.y, xl.y, make_float2(r.z, -r.x), make_float2(r.w, -r.y));
             }
+            const float sr = s2.x, er = e2.x, si = s2.y, ei = e2.y;
             const float2 q = rinv[k];  // x = (s + e) q, renormalised to a pair
             float2 h, l;
             {
