@@ -71,20 +71,44 @@ __device__ __forceinline__ uint32_t tt_boff(int r, int k) {
                       ((k & 7) << 1));
 }
 
-__device__ __forceinline__ void tt_put(uint8_t* b, int r, int k, float v) {
-    const __nv_bfloat16 h = __float2bfloat16(v);
-    const __nv_bfloat16 m = __float2bfloat16(v - __bfloat162float(h));
-    *(__nv_bfloat16*)(b + tt_boff(r, k)) = h;
-    *(__nv_bfloat16*)(b + tt_boff(TT_N + r, k)) = m;
+// tt_boff(r, k) = kb(k) + rb(r) + (kx(k) ^ ((r & 7) << 4)) with the K parts
+// kb(k) = (k >> 6) TT_BBLK + 2 (k & 7), kx(k) = ((k & 63) >> 3) << 4 fixed
+// per thread (its rows k = i and k = kb0 + i) and rb(r) = (r >> 3) 1024 +
+// (r & 7) 128 a constant once the column loops are unrolled.
+struct TTRow {
+    uint32_t kb0, kx0;  // k = i: the top half of B's K range
+    uint32_t kb1, kx1;  // k = kb0 + i: the bottom half
+};
+__device__ __forceinline__ TTRow tt_row(int i, int kbot) {
+    const int k1 = kbot + i;
+    return TTRow{(uint32_t)((i >> 6) * TT_BBLK + ((i & 7) << 1)), (uint32_t)(((i & 63) >> 3) << 4),
+                 (uint32_t)((k1 >> 6) * TT_BBLK + ((k1 & 7) << 1)), (uint32_t)(((k1 & 63) >> 3) << 4)};
 }
+__device__ __forceinline__ void tt_st16(uint8_t* p, uint32_t v) { *(uint16_t*)p = (uint16_t)v; }
 
-// B <- the embedding of T(i, c) = t, c < o, for this thread's row i.
-__device__ __forceinline__ void tt_write_b(uint8_t* b, int i, int kb0, int c, float2 t) {
-    tt_put(b, c, i, t.x);
-    tt_put(b, c, kb0 + i, -t.y);
-    tt_put(b, 32 + c, i, t.y);
-    tt_put(b, 32 + c, kb0 + i, t.x);
+// B <- the embedding of T(i, c) = t, c < o, for this thread's row: rows c
+// and 32 + c of the hi piece (64 + ... of the mid piece) get [Tr; -Ti] and
+// [Ti; Tr] over the two K halves.  Re and Im are rounded together; -Ti's
+// pieces are Ti's with the sign bit flipped (round-to-nearest is odd).
+__device__ __forceinline__ void tt_write_b(uint8_t* b, const TTRow& q, int c, float2 t) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(t.x, t.y);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 m = __floats2bfloat162_rn(t.x - hf.x, t.y - hf.y);
+    const uint32_t hv = *(const uint32_t*)&h, mv = *(const uint32_t*)&m;
+    const uint32_t sw = (uint32_t)((c & 7) << 4);
+    uint8_t* p0 = b + q.kb0 + (q.kx0 ^ sw);
+    uint8_t* p1 = b + q.kb1 + (q.kx1 ^ sw);
+    const int rc = (c >> 3) * 1024 + (c & 7) * 128;  // rb(c); rb(32 + c) = rc + 4096, +8192 for the mid piece
+    tt_st16(p0 + rc, hv);                            // (c, i) = Tr
+    tt_st16(p0 + rc + 8192, mv);
+    tt_st16(p1 + rc, (hv >> 16) ^ 0x8000u);          // (c, kb0 + i) = -Ti
+    tt_st16(p1 + rc + 8192, (mv >> 16) ^ 0x8000u);
+    tt_st16(p0 + rc + 4096, hv >> 16);               // (32 + c, i) = Ti
+    tt_st16(p0 + rc + 4096 + 8192, mv >> 16);
+    tt_st16(p1 + rc + 4096, hv);                     // (32 + c, kb0 + i) = Tr
+    tt_st16(p1 + rc + 4096 + 8192, mv);
 }
+static_assert(TT_N == 64, "tt_write_b: row offsets of 32 + c (4096) and of the mid piece (8192)");
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
@@ -278,6 +302,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         const int i = mt * 128 + q * 32 + lane;
         const bool row = i < n;
         const int kb0 = 16 * S;  // K index of the bottom half
+        const TTRow trow = tt_row(i, kb0);
         // B starts (and its padding stays) zero
         for (int e = threadIdx.x - 64; e < KBB * TT_BBLK / 16; e += TT_THREADS - 64)
             ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
@@ -308,7 +333,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         const int c = hb + cb + u;
-                        if (row && c < o) tt_write_b(sB, i, kb0, c, f[cb + u]);
+                        if (row && c < o) tt_write_b(sB, trow, c, f[cb + u]);
                         fv[u] = __float_as_uint(f[cb + u].x);
                         fv[8 + u] = __float_as_uint(f[cb + u].y);
                     }
@@ -376,13 +401,13 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                 if (r == 0) {  // W1 = W + (E - I) W
                                     sr = yr;
                                     si = yi;
-                                    tt_write_b(sB, i, kb0, c, make_float2(fr + yr, fi + yi));
+                                    tt_write_b(sB, trow, c, make_float2(fr + yr, fi + yi));
                                 } else {  // T_r = (i sqrt_dt / r) Y
                                     const float2 t = make_float2(-sk * yi, sk * yr);
                                     sr += t.x;
                                     si += t.y;
-                                    if (r < n_terms) tt_write_b(sB, i, kb0, c, t);
-                                    else tt_write_b(sB, i, kb0, c, make_float2(fr + sr, fi + si));  // out = W1 + sum T_k
+                                    if (r < n_terms) tt_write_b(sB, trow, c, t);
+                                    else tt_write_b(sB, trow, c, make_float2(fr + sr, fi + si));  // out = W1 + sum T_k
                                 }
                             }
                             sv[u] = __float_as_uint(sr);
