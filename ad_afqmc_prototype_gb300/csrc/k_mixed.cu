@@ -64,6 +64,11 @@ int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s) {
 // tensor-core output fbm (rows w: Re, rows W + w: Im, fb = 2 fbm) and the
 // shifted fields written as the split left operand of the V-build GEMM:
 // per walker chunk [w0, w0 + wc) the Re rows come first, then the Im rows.
+// F32 (the three-section form, whose operands carry bf16 x 3 = 24 bits): the
+// shifted field is formed and split in fp32 (the force bias is fp32 already)
+// and only the four sums for the weight accumulate in binary64; otherwise
+// all of it is binary64.
+template <bool F32>
 __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* __restrict__ x,
                                     const float* __restrict__ fbm, long long ldf, const double2* __restrict__ mf,
                                     __nv_bfloat16* __restrict__ av, int S, int Kt, int sec,
@@ -76,8 +81,21 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
     __nv_bfloat16* re_row = av + (long long)(2 * w0 + (w - w0)) * Kt;
     __nv_bfloat16* im_row = av + (long long)(2 * w0 + wc + (w - w0)) * Kt;
     double sr = 0.0, si = 0.0, br = 0.0, bi = 0.0;
+    const float sdt = (float)sqrt_dt;
     for (int g = lane; g < S; g += 32) {
-        if (g < G) {
+        if (F32 && g < G) {
+            const float fr = 2.f * fbm[(long long)w * ldf + g], fi = 2.f * fbm[(long long)(W + w) * ldf + g];
+            const double2 md = mf[g];
+            const float mx = (float)md.x, my = (float)md.y, xv = (float)x[(size_t)w * G + g];
+            const float fsx = -sdt * (-fi - mx), fsy = -sdt * (fr - my);
+            const float xr = xv - fsx, xi = -fsy;
+            split_storef(re_row, S, g, xr, true, sec);
+            split_storef(im_row, S, g, xi, true, sec);
+            sr += (double)(xr * mx - xi * my);
+            si += (double)(xr * my + xi * mx);
+            br += (double)(xv * fsx - 0.5f * (fsx * fsx - fsy * fsy));
+            bi += (double)(xv * fsy - fsx * fsy);
+        } else if (g < G) {
             const double2 f = make_double2(2.0 * (double)fbm[(long long)w * ldf + g],
                                            2.0 * (double)fbm[(long long)(W + w) * ldf + g]);
             const double2 m = mf[g];
@@ -109,8 +127,12 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
 int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
                              const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
                              double2* fb_term, cudaStream_t s) {
-    k_field_shift_mixed<<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec, shift_term,
-                                                    fb_term);
+    if (sec == 3)
+        k_field_shift_mixed<true><<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
+                                                              shift_term, fb_term);
+    else
+        k_field_shift_mixed<false><<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
+                                                               shift_term, fb_term);
     AFQ_LAUNCHED("k_field_shift_mixed");
     return AFQ_OK;
 }

@@ -924,7 +924,10 @@ int launch_block_measure(int W, double dt, double shift_ema, const double* weigh
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) counter-based RNG.
 // Call e uses counter (lo(e), hi(e), lo(counter), hi(counter)) and key
 // (lo(seed), hi(seed)); its four words give two 53-bit uniforms u, v.
-// Normals: Box-Muller, r = sqrt(-2 log(1-u)), (r cos 2 pi v, r sin 2 pi v).
+// Normals: Box-Muller, r = sqrt(-2 log(1-u)), (r cos 2 pi v, r sin 2 pi v),
+// evaluated in fp32 from x = fp32(1 - u) and fp32(v) (the binary64
+// transcendentals cost ~80 binary64 operations a pair at 1/64 of the fp32
+// rate); each normal carries fp32 rounding, ~1e-7 relative.
 // =====================================================================
 __device__ __forceinline__ uint4 philox10(uint4 c, uint2 k) {
     const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
@@ -953,11 +956,11 @@ __global__ void k_philox(int64_t count, uint64_t seed, uint64_t counter0, int no
     const double u = u53(r.x, r.y), v = u53(r.z, r.w);
     double a = u, b = v;
     if (normal) {
-        const double rad = sqrt(-2.0 * log(1.0 - u));
-        double sn, cs;
-        sincospi(2.0 * v, &sn, &cs);
-        a = rad * cs;
-        b = rad * sn;
+        const float rad = sqrtf(-2.0f * logf((float)(1.0 - u)));
+        float sn, cs;
+        sincospif(2.0f * (float)v, &sn, &cs);
+        a = (double)(rad * cs);
+        b = (double)(rad * sn);
     }
     out[2 * e] = a;
     if (2 * e + 1 < count) out[2 * e + 1] = b;

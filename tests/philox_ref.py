@@ -43,8 +43,12 @@ def uniform(count, seed, counter):
 
 
 def normal(count, seed, counter):
+    """Box-Muller of the fp32-rounded inputs fp32(1 - u) and fp32(v), here in
+    float64; the device evaluates the same formula in fp32 (~1e-7 apart)."""
     r = raw(count, seed, counter)
     u, v = _u53(r[:, 0], r[:, 1]), _u53(r[:, 2], r[:, 3])
-    rad = np.sqrt(-2.0 * np.log(1.0 - u))
-    out = np.stack([rad * np.cos(2 * np.pi * v), rad * np.sin(2 * np.pi * v)], axis=1).reshape(-1)
+    x = (1.0 - u).astype(np.float32).astype(np.float64)
+    t = 2.0 * v.astype(np.float32).astype(np.float64)
+    rad = np.sqrt(-2.0 * np.log(x))
+    out = np.stack([rad * np.cos(np.pi * t), rad * np.sin(np.pi * t)], axis=1).reshape(-1)
     return out[:count]

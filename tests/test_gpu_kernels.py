@@ -171,7 +171,8 @@ def test_philox_matches_cpu_mirror(E):
         u = cpu(E.fill_uniform((count,), seed, ctr))
         np.testing.assert_array_equal(u, philox_ref.uniform(count, seed, ctr))
         x = cpu(E.fill_normal((count,), seed, ctr))
-        np.testing.assert_allclose(x, philox_ref.normal(count, seed, ctr), rtol=1e-13, atol=1e-13)
+        # the device's fp32 log / sqrt / sincospi against float64 of the same inputs
+        np.testing.assert_allclose(x, philox_ref.normal(count, seed, ctr), rtol=2e-6, atol=2e-6)
 
 
 def test_field_shift_and_weight_update_match_oracle(E):
