@@ -384,28 +384,36 @@ int launch_field_shift(int W, int G, double sqrt_dt, const double* x, const doub
 }
 
 // =====================================================================
-// Importance weights with the phaseless cut (prop/afqmc.py:116-138).  One
-// CTA: the mean weight feeding the population-control shift is reduced
-// deterministically in the same launch.
+// Importance weights with the phaseless cut (prop/afqmc.py:116-138): one
+// thread a walker over W / 256 CTAs (the binary64 exp / sincos / atan2 of a
+// walker are a few hundred binary64 operations), then one CTA reduces the
+// mean weight feeding the population-control shift in a fixed order
+// (thread t sums walkers t, t + 1024, ...; then the warps and the CTA).
 // =====================================================================
-__global__ void __launch_bounds__(1024) k_weight_update(
-    int W, double dt, double sqrt_dt, double damping, double w_floor, double w_cap, double2 h0_prop,
+__global__ void __launch_bounds__(256) k_weight_update(
+    int W, double dt, double sqrt_dt, double w_floor, double w_cap, double2 h0_prop,
     const double2* __restrict__ shift_term, const double2* __restrict__ fb_term,
     const double2* __restrict__ ovlp_new, double* __restrict__ weights, double2* __restrict__ overlaps,
-    double* __restrict__ pop_shift, const double* __restrict__ e_est) {
+    const double* __restrict__ pop_shift) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
     const double ps = pop_shift[0];
+    const double2 on = ovlp_new[w];
+    double imp_ph = weight_factor(dt, sqrt_dt, ps, h0_prop, shift_term[w], fb_term[w], on, overlaps[w]).imp_ph;
+    if (imp_ph < w_floor) imp_ph = 0.0;
+    if (imp_ph > w_cap) imp_ph = 0.0;
+    double wn = weights[w] * imp_ph;
+    if (wn > w_cap) wn = 0.0;
+    weights[w] = wn;
+    overlaps[w] = on;
+}
+
+__global__ void __launch_bounds__(1024) k_weight_mean(int W, double dt, double damping,
+                                                      const double* __restrict__ weights,
+                                                      double* __restrict__ pop_shift,
+                                                      const double* __restrict__ e_est) {
     double local = 0.0;
-    for (int w = threadIdx.x; w < W; w += blockDim.x) {
-        const double2 on = ovlp_new[w];
-        double imp_ph = weight_factor(dt, sqrt_dt, ps, h0_prop, shift_term[w], fb_term[w], on, overlaps[w]).imp_ph;
-        if (imp_ph < w_floor) imp_ph = 0.0;
-        if (imp_ph > w_cap) imp_ph = 0.0;
-        double wn = weights[w] * imp_ph;
-        if (wn > w_cap) wn = 0.0;
-        weights[w] = wn;
-        overlaps[w] = on;
-        local += wn;
-    }
+    for (int w = threadIdx.x; w < W; w += blockDim.x) local += weights[w];
     __shared__ double red[32];
     local = warp_sum(local);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
@@ -426,10 +434,11 @@ int launch_weight_update(int W, const afq_params* p, double sqrt_dt, double dt, 
                          double* weights, double2* overlaps, double* pop_shift, const double* e_est,
                          cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
-    k_weight_update<<<1, 1024, 0, s>>>(W, dt, sqrt_dt, p->pop_control_damping, p->weight_floor,
-                                       p->weight_cap, h0_prop, shift_term, fb_term, ovlp_new, weights,
-                                       overlaps, pop_shift, e_est);
+    k_weight_update<<<(W + 255) / 256, 256, 0, s>>>(W, dt, sqrt_dt, p->weight_floor, p->weight_cap, h0_prop,
+                                                    shift_term, fb_term, ovlp_new, weights, overlaps, pop_shift);
     AFQ_LAUNCHED("k_weight_update");
+    k_weight_mean<<<1, 1024, 0, s>>>(W, dt, p->pop_control_damping, weights, pop_shift, e_est);
+    AFQ_LAUNCHED("k_weight_mean");
     return AFQ_OK;
 }
 
