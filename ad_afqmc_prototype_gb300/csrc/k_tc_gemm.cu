@@ -249,12 +249,27 @@ struct ExchOut {
 // MODE 0: fp32 C.  MODE 1 (split): the two-piece bf16 split of each sum to
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
 // exchange contraction of each 32 x 32 block (ExchOut) instead of C.
-template <int BNT, int MODE>
+//
+// CM > 1: launched in clusters of CM CTAs that take CM consecutive M tiles of
+// one N tile.  Each CTA loads its A tile and rows [r BNT / CM, (r + 1) BNT /
+// CM) of the B tile (r its rank) into the same stage offset of every CTA in
+// the cluster (TMA multicast), so the cluster reads each B tile from L2 once
+// instead of CM times.  A stage is refilled only after every CTA's MMAs have
+// consumed it: each MMA thread's commit arrives on the empty barrier of
+// every CTA (count CM).
+template <int BNT, int MODE, int CM>
 __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
                     int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
     using D = Drain<BNT>;
+    static_assert(CM == 1 || CM == 2 || CM == 4, "cluster of 1, 2 or 4 CTAs along M");
+    if (CM > 1 && cluster_nctarank() != (uint32_t)CM) {  // launched without the cluster shape: nothing runs
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+    const int rank = CM > 1 ? (int)cluster_ctarank() : 0;
+    const uint16_t cmask = (uint16_t)((1u << CM) - 1);
     constexpr bool SPLIT = MODE == 1;
     static_assert(MODE != 2 || BNT % 64 == 0, "the exchange epilogue takes whole 32 x 32 blocks per warp");
     constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
@@ -271,12 +286,14 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mt = (M + BM - 1) / BM, nt = (N + BNT - 1) / BNT, kt = K / BK;
-    const int ntiles = mt * nt, np = (kt + kd - 1) / kd;  // partials per tile
+    // cluster tiles: CM consecutive M tiles of one N tile; this CTA's is mg CM + rank
+    const int mtc = (mt + CM - 1) / CM, ntiles = mtc * nt, np = (kt + kd - 1) / kd;  // partials per tile
+    const int cid = blockIdx.x / CM, ncl = gridDim.x / CM;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STG; ++s) {
             mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, CM);
         }
         for (int a = 0; a < SLOTS; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
@@ -294,6 +311,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     }
     tc_fence_before();
     __syncthreads();
+    if (CM > 1) cluster_sync();  // every CTA's barriers are initialised before any multicast lands
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -307,14 +325,18 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
             uint32_t issued_par[STG];
             for (int s = 0; s < STG; ++s) issued[s] = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-                const int mb = t % mt, nb = t / mt;
+            for (int t = cid; ok && t < ntiles; t += ncl) {
+                const int mb = (t % mtc) * CM + rank, nb = t / mtc;
                 for (int kb = 0; kb < kt; ++kb) {
                     if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
                     mbar_expect_tx(full0 + 8 * stage, D::STAGE);
                     tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
-                    tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
+                    if (CM == 1)
+                        tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
+                    else
+                        tma_load_2d_mc(smem_u32(sB + stage * D::B_BYTES + rank * (D::B_BYTES / CM)), &tmB, kb * BK,
+                                       nb * BNT + rank * (BNT / CM), full0 + 8 * stage, cmask);
                     issued[stage] = 1;
                     issued_par[stage] = phase;
                     if (++stage == STG) { stage = 0; phase ^= 1; }
@@ -332,7 +354,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
             int stage = 0, slot = 0;
             uint32_t phase = 0, slot_phase = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            for (int t = cid; ok && t < ntiles; t += ncl) {
                 for (int kb = 0; kb < kt; ++kb) {
                     const int g = kb % kd;  // position inside the current partial
                     if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
@@ -343,7 +365,8 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
                     for (int k = 0; k < BK / 16; ++k)
                         umma_bf16_i(tmem + slot * BNT, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), D::IDESC,
                                     (k != 0) || (g != 0));
-                    umma_commit(empty0 + 8 * stage);
+                    if (CM == 1) umma_commit(empty0 + 8 * stage);
+                    else umma_commit_mc(empty0 + 8 * stage, cmask);
                     if (g == kd - 1 || kb == kt - 1) {
                         umma_commit(tfull0 + 8 * slot);
                         if (++slot == SLOTS) { slot = 0; slot_phase ^= 1; }
@@ -365,8 +388,8 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
         const bool vec = SPLIT ? (ldc % 8) == 0 && ((((uintptr_t)Ch) | ((uintptr_t)Cm)) & 15) == 0
                                : (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
-        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-            const int mb = t % mt, nb = t / mt;
+        for (int t = cid; ok && t < ntiles; t += ncl) {
+            const int mb = (t % mtc) * CM + rank, nb = t / mtc;
             float2 acc[CW / 2];
 #pragma unroll
             for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
@@ -491,6 +514,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
     }
     tc_fence_before();
     __syncthreads();
+    if (CM > 1) cluster_sync();  // no CTA leaves while a peer may still write its shared memory
     if (warp == 1) {
         __syncwarp();
         tc_fence_after();
@@ -524,23 +548,43 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     return AFQ_OK;
 }
 
+// Clusters of DRAIN_CM CTAs along M share each B tile by TMA multicast
+// (k_gemm_tn_drain); the grid is as many clusters as are resident at once.
+constexpr int DRAIN_CM = 2;
+
 template <int BNT, int MODE>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                         __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
                         tc::ExchOut xo = tc::ExchOut{}) {
     using namespace tc;
-    static bool attr = false;
+    constexpr int CM = DRAIN_CM;
+    static int max_clusters = 0;
     constexpr int SMEM = Drain<BNT>::SMEM + (MODE == 2 ? XT_BYTES : 0);
+    auto kern = k_gemm_tn_drain<BNT, MODE, CM>;
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
-    AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT));
-    if (!attr) {
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn_drain<BNT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        attr = true;
+    AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT / CM));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CM;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(Drain<BNT>::THREADS);
+    cfg.dynamicSmemBytes = SMEM;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (!max_clusters) {
+        AFQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        cfg.gridDim = dim3(CM * (g_num_sms / CM));
+        AFQ_CUDA(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
+        if (max_clusters < 1) return fail(AFQ_E_CUDA, "drained GEMM: no cluster of %d CTAs fits", CM);
     }
-    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
-    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    k_gemm_tn_drain<BNT, MODE><<<grid, Drain<BNT>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo);
+    const long long ctiles = (long long)((M + BM * CM - 1) / (BM * CM)) * ((N + BNT - 1) / BNT);
+    const int ncl = (int)(ctiles < max_clusters ? ctiles : max_clusters);
+    cfg.gridDim = dim3(CM * ncl);
+    AFQ_CUDA(cudaLaunchKernelEx(&cfg, kern, ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo));
     AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }
