@@ -207,18 +207,22 @@ __global__ void __launch_bounds__(THREADS, 1)
 // warps 2-5 and 6-9 each cover all 128 rows, one column half each.
 constexpr int DTMEM_COLS = 512;
 
-// 320 threads (warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9 epilogue);
-// each epilogue thread sums BNT/2 = 64 columns of one row.
-template <int BNT>
+// 64 + 32 EWN threads (warp 0 TMA, warp 1 MMA + TMEM owner, EWN epilogue
+// warps, EWN / 4 of them on each 32-lane quarter of the accumulator); each
+// epilogue thread sums CW = 4 BNT / EWN columns of one row.  Sixteen
+// epilogue warps drain a 128 x 256 partial in about half the time of eight
+// (the drain has to keep up with the MMAs of the next partial).
+template <int BNT, int EWN = 8>
 struct Drain {
-    static constexpr int THREADS = 320;
+    static_assert(EWN == 8 || EWN == 16, "eight or sixteen epilogue warps");
+    static constexpr int THREADS = 64 + 32 * EWN;
     static constexpr int EW0 = 2;  // first epilogue warp
     static constexpr int SLOTS = DTMEM_COLS / BNT;
     static constexpr int STG = BNT == 128 ? 6 : 4;
     static constexpr int B_BYTES = BNT * BK * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
     static constexpr int SMEM = STG * STAGE + 1024 + 256;
-    static constexpr int CW = BNT / 2;  // columns per epilogue warp
+    static constexpr int CW = 4 * BNT / EWN;  // columns per epilogue warp
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BNT >> 3) << 17) |
                                       ((uint32_t)(BM >> 4) << 24);
 };
@@ -257,12 +261,13 @@ struct ExchOut {
 // instead of CM times.  A stage is refilled only after every CTA's MMAs have
 // consumed it: each MMA thread's commit arrives on the empty barrier of
 // every CTA (count CM).
-template <int BNT, int MODE, int CM>
-__global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
+template <int BNT, int MODE, int CM, int EWN>
+__global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
                     int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
-    using D = Drain<BNT>;
+    using D = Drain<BNT, EWN>;
+    static_assert(MODE != 2 || EWN == 8, "the exchange epilogue's transpose buffers are sized for eight warps");
     static_assert(CM == 1 || CM == 2 || CM == 4, "cluster of 1, 2 or 4 CTAs along M");
     if (CM > 1 && cluster_nctarank() != (uint32_t)CM) {  // launched without the cluster shape: nothing runs
         if (threadIdx.x == 0) atomicExch(err, 1);
@@ -297,7 +302,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
         }
         for (int a = 0; a < SLOTS; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, 256);  // eight epilogue warps
+            mbar_init(tempty0 + 8 * a, 32 * EWN);  // every epilogue thread
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -403,13 +408,14 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
                 tc_fence_after();
                 // chunks of LC columns; the sums of a chunk are complete before the
                 // next load, so at most LC staged values are live
-                constexpr int LC = BNT == 128 ? 64 : 32;
+                constexpr int LC = EWN == 16 ? 16 : BNT == 128 ? 64 : 32;
 #pragma unroll
                 for (int c = 0; c < CW; c += LC) {
                     uint32_t r[LC];
                     const uint32_t ta = tmem + slot * BNT + cb + c + ((uint32_t)(q * 32) << 16);
                     if constexpr (LC == 64) tmem_ld64(ta, r);
-                    else tmem_ld32(ta, r);
+                    else if constexpr (LC == 32) tmem_ld32(ta, r);
+                    else tmem_ld16(ta, r);
 #pragma unroll
                     for (int j = 0; j < LC / 2; ++j) {
                         if constexpr (BNT == 128) {
@@ -462,7 +468,7 @@ __global__ void __launch_bounds__(Drain<BNT>::THREADS, 1)
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) ex += __shfl_xor_sync(0xffffffffu, ex, off);
                 if (lane == 0 && wl < xo.nw)
-                    xo.x[((size_t)wl * xo.nhalf + nb * 2 + cb / CW) * 2 + part] = ex;
+                    xo.x[((size_t)wl * xo.nhalf + nb * (BNT / CW) + cb / CW) * 2 + part] = ex;
                 continue;
             }
             const int row = mb * BM + q * 32 + lane;
@@ -552,15 +558,15 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
 // (k_gemm_tn_drain); the grid is as many clusters as are resident at once.
 constexpr int DRAIN_CM = 2;
 
-template <int BNT, int MODE>
+template <int BNT, int MODE, int EWN>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                         __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
                         tc::ExchOut xo = tc::ExchOut{}) {
     using namespace tc;
     constexpr int CM = DRAIN_CM;
     static int max_clusters = 0;
-    constexpr int SMEM = Drain<BNT>::SMEM + (MODE == 2 ? XT_BYTES : 0);
-    auto kern = k_gemm_tn_drain<BNT, MODE, CM>;
+    constexpr int SMEM = Drain<BNT, EWN>::SMEM + (MODE == 2 ? XT_BYTES : 0);
+    auto kern = k_gemm_tn_drain<BNT, MODE, CM, EWN>;
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
     AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT / CM));
@@ -570,7 +576,7 @@ static int launch_drain(int M, int N, int K, const void* A, long long lda, const
     at[0].val.clusterDim.x = CM;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(Drain<BNT>::THREADS);
+    cfg.blockDim = dim3(Drain<BNT, EWN>::THREADS);
     cfg.dynamicSmemBytes = SMEM;
     cfg.stream = s;
     cfg.attrs = at;
@@ -607,7 +613,7 @@ int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, c
                             long long ldc, int* err, cudaStream_t s, int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<256, 0>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
+    return launch_drain<256, 0, 16>(M, N, K, A, lda, B, ldb, C, nullptr, nullptr, ldc, kd, err, s);
 }
 
 int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb,
@@ -615,7 +621,7 @@ int launch_tc_gemm_tn_drain_split(int M, int N, int K, const void* A, long long 
                                   int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;
     AFQ_TRY(drain_prologue(K, kd));
-    return launch_drain<256, 1>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
+    return launch_drain<256, 1, 16>(M, N, K, A, lda, B, ldb, nullptr, Ch, Cm, ldc, kd, err, s);
 }
 
 int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, const void* B, long long ldb,
@@ -629,7 +635,7 @@ int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, 
     xo.G = G;
     xo.nw = nw;
     xo.nhalf = exchange_halves(G);
-    return launch_drain<tc::EXCH_BNT, 2>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, kd, err, s, xo);
+    return launch_drain<tc::EXCH_BNT, 2, 8>(M, N, K, A, lda, B, ldb, nullptr, nullptr, nullptr, 0, kd, err, s, xo);
 }
 
 int exchange_halves(int G) { return 2 * ((32 * G + tc::EXCH_BNT - 1) / tc::EXCH_BNT); }
