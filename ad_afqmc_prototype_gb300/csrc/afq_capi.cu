@@ -83,9 +83,9 @@ static LowpDims lowp_dims(const afq_dims* d) {
     // reading F (G o x 2 o fp32 per walker): worth it for o close to 32
     L.xf = o > 24 && o <= 32;
     L.Pe = L.xf ? 32 : o;
-    // the tensor cores' truncating fp32 sum over 128 products (bias ~2^-22 relative) stays below the
+    // the tensor cores' truncating fp32 sum over 256 products (bias ~2^-21 relative) stays below the
     // three-section split's 2^-17; the six-section form drains every 64 (bias < 2^-23)
-    L.kd = d->precision == AFQ_PREC_MIXED_FAST ? 2 : 1;
+    L.kd = d->precision == AFQ_PREC_MIXED_FAST ? 4 : 1;
     return L;
 }
 
