@@ -601,8 +601,18 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     //   fp32 Gauss-Jordan inverse of the copy, pivots by warp 1; its pivot
     //   row k is scaled by 1/pivot in the next step's first phase (rows
     //   r != k eliminate with the unscaled row times 1/pivot meanwhile).
+    //   The row multipliers (LU: m[r][k] / pivot for r > k; Gauss-Jordan:
+    //   mf[r][k] / pivot for r != k) are formed once a step, during the row
+    //   swaps, which leave column k alone: the multipliers read it with the
+    //   swap applied (it is not read again).  Element loops advance (row,
+    //   column) incrementally instead of dividing per element.
     __shared__ int s_piv2;
     __shared__ float2 s_rpf2[2];
+    constexpr int OMAX = MA <= 4 ? 32 : 64;   // nocc bound of this instantiation (AG = 256 / o >= o / MA)
+    __shared__ float4 s_lmul[OMAX];           // LU multipliers (double-float, or binary64 as double2)
+    __shared__ float2 s_fmul[OMAX];           // Gauss-Jordan multipliers
+    const int o2 = 2 * o;
+    const int gj_sr = blockDim.x / o2, gj_sj = blockDim.x % o2, gj_r0 = tid / o2, gj_j0 = tid % o2;
     for (int k = 0; k <= o; ++k) {
         if (k < o && wid == 0) {
             double best = -1.0;
@@ -671,14 +681,15 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
         __syncthreads();
         if (k == o) break;
         const int p = s_piv, p2 = s_piv2;
-        for (int j = tid; j < 3 * o; j += blockDim.x) {
+        const float2 rpf = s_rpf2[k & 1];
+        for (int j = tid; j < 3 * o; j += blockDim.x) {  // row swaps outside column k
             if (j < o) {
-                if (p != k) {  // 16-byte entries: binary64 complex, or double-float
+                if (p != k && j != k) {  // 16-byte entries: binary64 complex, or double-float
                     const double2 t = m[k * o + j];
                     m[k * o + j] = m[p * o + j];
                     m[p * o + j] = t;
                 }
-            } else if (p2 != k) {
+            } else if (p2 != k && j != o + k) {
                 float2* X = j < 2 * o ? mf : invf;
                 const int jj = j < 2 * o ? j - o : j - 2 * o;
                 const float2 t = X[k * o + jj];
@@ -686,34 +697,47 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
                 X[p2 * o + jj] = t;
             }
         }
-        __syncthreads();
-        const float2 rpf = s_rpf2[k & 1];
-        const int rem = o - k - 1;
-        if (DF) {
-            const float4 rpd = s_rpd;
-            for (int e = tid; e < rem * rem; e += blockDim.x) {
-                const int r = k + 1 + e / rem, j = k + 1 + e % rem;
-                const float4 l = zdf_mul(md[r * o + k], rpd);
-                md[r * o + j] = zdf_sub(md[r * o + j], zdf_mul(l, md[k * o + j]));
-            }
-        } else {
-            const double2 rp = s_rp;
-            for (int e = tid; e < rem * rem; e += blockDim.x) {
-                const int r = k + 1 + e / rem, j = k + 1 + e % rem;
-                const double2 l = cmul(m[r * o + k], rp);
-                m[r * o + j] = csub(m[r * o + j], cmul(l, m[k * o + j]));
+        for (int r = tid; r < 2 * o; r += blockDim.x) {  // multipliers from column k, rows swapped
+            if (r < o) {
+                if (r > k) {
+                    const int src = r == p ? k : r;
+                    if (DF) s_lmul[r] = zdf_mul(md[src * o + k], s_rpd);
+                    else ((double2*)s_lmul)[r] = cmul(m[src * o + k], s_rp);
+                }
+            } else if (r - o != k) {
+                const int src = r - o == p2 ? k : r - o;
+                const float2 f0 = mf[src * o + k];
+                s_fmul[r - o] = make_float2(f0.x * rpf.x - f0.y * rpf.y, f0.x * rpf.y + f0.y * rpf.x);
             }
         }
-        for (int e = tid; e < o * 2 * o; e += blockDim.x) {
-            const int r = e / (2 * o), j = e % (2 * o);
-            if (r == k) continue;
-            float2* X = j < o ? mf : invf;
-            const int jj = j < o ? j : j - o;
-            if (j < o && jj <= k) continue;
-            const float2 f0 = mf[r * o + k];
-            const float2 f = make_float2(f0.x * rpf.x - f0.y * rpf.y, f0.x * rpf.y + f0.y * rpf.x);
-            const float2 v = X[k * o + jj], x = X[r * o + jj];
-            X[r * o + jj] = make_float2(x.x - (f.x * v.x - f.y * v.y), x.y - (f.x * v.y + f.y * v.x));
+        __syncthreads();
+        const int rem = o - k - 1;
+        if (rem > 0 && tid < rem * rem) {
+            const int sr = blockDim.x / rem, sj = blockDim.x % rem;
+            int rr = tid / rem, jj = tid % rem;
+            for (int e = tid; e < rem * rem; e += blockDim.x) {
+                const int r = k + 1 + rr, j = k + 1 + jj;
+                if (DF) md[r * o + j] = zdf_sub(md[r * o + j], zdf_mul(s_lmul[r], md[k * o + j]));
+                else m[r * o + j] = csub(m[r * o + j], cmul(((const double2*)s_lmul)[r], m[k * o + j]));
+                rr += sr;
+                jj += sj;
+                if (jj >= rem) { jj -= rem; ++rr; }
+            }
+        }
+        {
+            int r = gj_r0, j = gj_j0;
+            for (int e = tid; e < o * o2; e += blockDim.x) {
+                if (r != k && !(j < o && j <= k)) {
+                    float2* X = j < o ? mf : invf;
+                    const int jj = j < o ? j : j - o;
+                    const float2 f = s_fmul[r];
+                    const float2 v = X[k * o + jj], x = X[r * o + jj];
+                    X[r * o + jj] = make_float2(x.x - (f.x * v.x - f.y * v.y), x.y - (f.x * v.y + f.y * v.x));
+                }
+                r += gj_sr;
+                j += gj_sj;
+                if (j >= o2) { j -= o2; ++r; }
+            }
         }
         __syncthreads();
     }

@@ -124,12 +124,15 @@ def _r64(x):
     return (x + 63) // 64 * 64
 
 
-def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
+def phase_work(n, o, G, W, trial_real=True, precision="fp64", n_terms=6):
     """(work per launch, pipe) of each timed phase.  FP64 form: algorithmic
     real flops.  Mixed forms: the tensor-core phases count the flops of the
     bf16 split operands (2 M N K with K the split row length; the energy GEMM
-    without the padding of its exchange-fused layout), the exchange step the
-    bytes it must read, the others algorithmic flops on their pipe."""
+    without the padding of its exchange-fused layout; the three-section Taylor
+    products 3 x 2 n (2 nocc) (2 n) per V product and 3 x 2 n (2 nocc) n per
+    E - I product), the exchange step the bytes it must read.  The overlap,
+    Green's function and QR phases of the mixed forms run double-float
+    arithmetic on the fp32 pipe ("df32"): no algorithmic-flop roofline."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
     work = {
         "vbuild_gemm": (4.0 * G * n * n * W, "fp64"),
@@ -151,6 +154,10 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64"):
         else:  # the reduction reads F (G o x 2 o W fp32)
             work["e_exchange"] = (4.0 * (2 * o * W) * (G * o), "hbm")
         work["trotter"] = ((48.0 + 8.0) * n * n * o * W, "fp32")
+        if precision == "mixed_fast" and n % 8 == 0 and n <= 256 and o <= 32:  # tensor-core Taylor products
+            work["trotter"] = (3.0 * (8.0 * n_terms + 8.0) * n * n * o * W, "tensor")
+        for k in ("overlap", "green", "qr"):
+            work[k] = (work[k][0], "df32")
     return work
 
 
@@ -161,8 +168,11 @@ def roofline_for(phases, work, lib, steps, name=None):
     launch once per walker chunk make several launches per call, so achieved
     = work x calls per block / device time per block."""
     leaf = {k: v for k, v in phases.items() if not (k == "energy" and "e_gemm" in phases)}
-    dname = name or max(leaf.items(), key=lambda kv: kv[1][1])[0]
-    if dname not in work or dname not in phases:
+    cand = {k: v for k, v in leaf.items() if k in work and work[k][1] != "df32"}
+    if not cand:
+        return None
+    dname = name or max(cand.items(), key=lambda kv: kv[1][1])[0]
+    if dname not in work or dname not in phases or work[dname][1] == "df32":
         return None
     dcalls, dms = phases[dname]
     flops, pipe = work[dname]
@@ -282,6 +292,10 @@ def run_ours(args, rank, world):
     # dominant kernel and its roofline
     work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=args.precision)
     roof = roofline_for(phases, work, lib, args.steps)
+    leaf = {k: v for k, v in phases.items() if not (k == "energy" and "e_gemm" in phases)}
+    top = max(leaf.items(), key=lambda kv: kv[1][1])[0]
+    dominant = {"phase": top, "share_of_step": round(leaf[top][1] / sum(v[1] for v in leaf.values()), 4),
+                "pipe": work[top][1] if top in work else None}
     if roof is not None:
         t = MEASURED_TRAFFIC.get((args.workload, args.precision, W, roof["kernel"]))
         if t is not None:
@@ -317,7 +331,7 @@ def run_ours(args, rank, world):
                       "step": "one block: 10 propagation steps, QR after step 5, QR + energy + comb at the end",
                       "l2": "inputs larger than L2 (walkers %d MB, V %d MB per step)"
                             % (W * n * o * 16 >> 20, W * n * n * 16 >> 20)},
-           "roofline": roof, "tensor_kernels": tc,
+           "roofline": roof, "dominant_phase": dominant, "tensor_kernels": tc,
            "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
            "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
     if cvline:
