@@ -453,6 +453,17 @@ __device__ __forceinline__ void df_acc2(float2& s, float2& e, float ch, float cl
     e = __fadd2_rn(e, __fadd2_rn(__fadd2_rn(r, pe), __ffma2_rn(c2, wl, __fmul2_rn(make_float2(cl, cl), wh))));
 }
 
+// (s, e) += (sb, eb) for two double-float pairs on two lanes (Knuth's two-sum
+// of the heads, the tails and the rounding error added to the tail).
+__device__ __forceinline__ void df_add2(float2& s, float2& e, float2 sb, float2 eb) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 t = __fadd2_rn(s, sb);
+    const float2 v = __ffma2_rn(s, m1, t);                                        // t - s
+    const float2 r = __fadd2_rn(__ffma2_rn(__ffma2_rn(v, m1, t), m1, s), __ffma2_rn(v, m1, sb));
+    s = t;
+    e = __fadd2_rn(__fadd2_rn(e, eb), r);
+}
+
 // Double-float (fp32 pair, ~2^-44) complex arithmetic for the overlap's LU,
 // after the QD library's algorithms (Hida, Li and Bailey): Knuth's two-sum,
 // the fma two-product, the "sloppy" pair addition, and the reciprocal by one
@@ -884,12 +895,23 @@ __device__ __forceinline__ void cq_gram(int n, int o, int ld, const float2* Ah, 
         if (DF) {
             const float2* al = Al + (size_t)j * ld;
             const float2* bl = Al + (size_t)k * ld;
-            float2 s2 = make_float2(0.f, 0.f), e2 = make_float2(0.f, 0.f);
-            for (int i = 0; i < n; ++i) {  // conj(a) b: (Re, Im) += a_r (b_r, b_i) + a_i (b_i, -b_r)
+            // conj(a) b: (Re, Im) += a_r (b_r, b_i) + a_i (b_i, -b_r), in two chains (even / odd i)
+            float2 s2 = make_float2(0.f, 0.f), e2 = s2, s3 = s2, e3 = s2;
+            int i = 0;
+            for (; i + 1 < n; i += 2) {
+                const float2 xh = ah[i], xl = al[i], yh = bh[i], yl = bl[i];
+                const float2 xh1 = ah[i + 1], xl1 = al[i + 1], yh1 = bh[i + 1], yl1 = bl[i + 1];
+                df_acc2(s2, e2, xh.x, xl.x, yh, yl);
+                df_acc2(s3, e3, xh1.x, xl1.x, yh1, yl1);
+                df_acc2(s2, e2, xh.y, xl.y, make_float2(yh.y, -yh.x), make_float2(yl.y, -yl.x));
+                df_acc2(s3, e3, xh1.y, xl1.y, make_float2(yh1.y, -yh1.x), make_float2(yl1.y, -yl1.x));
+            }
+            if (i < n) {
                 const float2 xh = ah[i], xl = al[i], yh = bh[i], yl = bl[i];
                 df_acc2(s2, e2, xh.x, xl.x, yh, yl);
                 df_acc2(s2, e2, xh.y, xl.y, make_float2(yh.y, -yh.x), make_float2(yl.y, -yl.x));
             }
+            df_add2(s2, e2, s3, e3);
             Gm[j * o + k] = make_double2((double)s2.x + (double)e2.x, (double)s2.y + (double)e2.y);
         } else {
             for (int i = 0; i < n; ++i) {
@@ -965,13 +987,26 @@ __device__ __forceinline__ void cq_solve(int n, int o, int ld, float2* Ah, float
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         for (int k = 0; k < o; ++k) {
             const float2 ah = Ah[(size_t)k * ld + i], al = Al[(size_t)k * ld + i];
-            float2 s2 = ah, e2 = al;  // (Re, Im) and their error terms
-            for (int j = 0; j < k; ++j) {  // a -= x r: (Re, Im) += -x_r (r_r, r_i) + x_i (r_i, -r_r)
+            float2 s2 = ah, e2 = al;  // (Re, Im) and their error terms: even j here, odd j in (s3, e3)
+            float2 s3 = make_float2(0.f, 0.f), e3 = s3;
+            // a -= x r: (Re, Im) += -x_r (r_r, r_i) + x_i (r_i, -r_r)
+            int j = 0;
+            for (; j + 1 < k; j += 2) {
+                const float2 xh = Ah[(size_t)j * ld + i], xl = Al[(size_t)j * ld + i];
+                const float2 xh1 = Ah[(size_t)(j + 1) * ld + i], xl1 = Al[(size_t)(j + 1) * ld + i];
+                const float4 r = Rd[j * o + k], r1 = Rd[(j + 1) * o + k];
+                df_acc2(s2, e2, -xh.x, -xl.x, make_float2(r.x, r.z), make_float2(r.y, r.w));
+                df_acc2(s3, e3, -xh1.x, -xl1.x, make_float2(r1.x, r1.z), make_float2(r1.y, r1.w));
+                df_acc2(s2, e2, xh.y, xl.y, make_float2(r.z, -r.x), make_float2(r.w, -r.y));
+                df_acc2(s3, e3, xh1.y, xl1.y, make_float2(r1.z, -r1.x), make_float2(r1.w, -r1.y));
+            }
+            if (j < k) {
                 const float2 xh = Ah[(size_t)j * ld + i], xl = Al[(size_t)j * ld + i];
                 const float4 r = Rd[j * o + k];
                 df_acc2(s2, e2, -xh.x, -xl.x, make_float2(r.x, r.z), make_float2(r.y, r.w));
                 df_acc2(s2, e2, xh.y, xl.y, make_float2(r.z, -r.x), make_float2(r.w, -r.y));
             }
+            df_add2(s2, e2, s3, e3);
             const float sr = s2.x, er = e2.x, si = s2.y, ei = e2.y;
             const float2 q = rinv[k];  // x = (s + e) q, renormalised to a pair
             float2 h, l;
