@@ -608,7 +608,8 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     __syncthreads();
 
     // One pivot loop for both factorisations of m, three barriers a step:
-    //   binary64 LU with partial pivoting (det(m) only), pivots by warp 0;
+    //   LU with partial pivoting (det(m) only; double-float with DF, else
+    //   binary64), pivots by warp 0;
     //   fp32 Gauss-Jordan inverse of the copy, pivots by warp 1; its pivot
     //   row k is scaled by 1/pivot in the next step's first phase (rows
     //   r != k eliminate with the unscaled row times 1/pivot meanwhile).

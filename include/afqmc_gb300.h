@@ -225,8 +225,9 @@ int afq_stochastic_reconfiguration(const afq_dims* d, const double* weights, dou
 
 /* ---- the step pieces (prop/afqmc.py:86-138) ----------------------------- */
 
-/* Philox4x32-10 (Salmon et al., SC'11) normals by Box-Muller, and uniforms
- * in [0, 1); element i depends only on (seed, counter, i). */
+/* Philox4x32-10 (Salmon et al., SC'11) uniforms in [0, 1) with 53 random
+ * bits, and normals by Box-Muller evaluated in fp32 from them (~1e-7
+ * relative rounding); element i depends only on (seed, counter, i). */
 int afq_fill_normal(int64_t count, uint64_t seed, uint64_t counter, double* out,
                     void* stream);
 int afq_fill_uniform(int64_t count, uint64_t seed, uint64_t counter, double* out,
