@@ -36,7 +36,8 @@ SPLIT_SECTIONS = {"mixed": 6, "mixed_fast": 3}
 # DRAM bytes (read + write) per launch of a kernel, from one ncu capture of this bench's own command
 # (profiles/launches_block_c4_n200_o30_g1000_w4096_mixed_fast.md), keyed by (workload, precision,
 # walkers, phase); the roofline reports them beside the algorithmic bytes
-MEASURED_TRAFFIC = {("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "vbuild_gemm"): 894594048 + 1319975936}
+MEASURED_TRAFFIC = {("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "vbuild_gemm"): 1319753216 + 1447654912,
+                    ("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "trotter"): 1736507648 + 368667136}
 
 
 def parse():
@@ -306,8 +307,16 @@ def run_ours(args, rank, world):
                 # split x~ and chol^T rows (bf16) read, V written (bf16 hi + mid, or fp32): 8 W n^2 bytes
                 roof["traffic_algorithmic"] = int(2 * (2 * W) * _r64(ks * G) + 2 * n * n * _r64(ks * G)
                                                   + 8 * W * n * n)
+            if roof["kernel"] == "trotter":
+                # V hi + mid of every walker read once (2 planes x n^2 x 2 pieces x 2 bytes), walkers read
+                # and written in binary64 (16 n o bytes each way)
+                roof["traffic_algorithmic"] = int(W * (8 * n * n + 32 * n * o))
     tc = {k: roofline_for(phases, work, lib, args.steps, name=k) for k in phases
           if k in work and work[k][1] in ("tensor", "hbm")}
+    for k, r in tc.items():
+        t = MEASURED_TRAFFIC.get((args.workload, args.precision, W, k))
+        if r is not None and t is not None:
+            r["traffic"] = t
 
     compare = None
     if args.precision in SPLIT_SECTIONS and not args.no_fp64:
