@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
     __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
     double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
-    constexpr int BG = 8;
+    constexpr int BG = 4;  // columns a task: a 32-row chunk at nocc 30 is 256 tasks, one per thread
     const int nbg = (o + BG - 1) / BG;
     // DF: W's fp32 copy is staged again OS_CH rows at a time (fewer bytes of shared memory, more CTAs)
     for (int i0 = 0; i0 < n; i0 += DF ? OS_CH : n) {
