@@ -1,0 +1,50 @@
+"""CPU checks of bench.py's work model and roofline selection (no GPU):
+the tensor-core Taylor products count as tensor work, the mixed forms'
+double-float phases never become the roofline kernel, and the roofline's
+numbers follow from the phase times."""
+import math
+
+import pytest
+
+bench = pytest.importorskip("bench")
+
+
+def test_phase_work_pipes_per_precision():
+    fp64 = bench.phase_work(200, 30, 1000, 4096, precision="fp64")
+    assert {p for _, p in fp64.values()} == {"fp64"}
+    fast = bench.phase_work(200, 30, 1000, 4096, precision="mixed_fast")
+    assert fast["trotter"][1] == "tensor"
+    # three bf16 sections of 6 V products (2n x 2o x 2n) and 2 E - I products (2n x 2o x n) per walker
+    assert fast["trotter"][0] == pytest.approx(3 * (6 * 2 * 200 * 60 * 400 + 2 * 2 * 200 * 60 * 200) * 4096)
+    for k in ("overlap", "green", "qr"):
+        assert fast[k][1] == "df32"
+    for k in ("vbuild_gemm", "fb_gemm", "e_gemm"):
+        assert fast[k][1] == "tensor"
+    # no tensor-core Taylor kernel past norb 256 or nocc 32
+    assert bench.phase_work(400, 50, 2000, 1024, precision="mixed_fast")["trotter"][1] == "fp32"
+    assert bench.phase_work(200, 30, 1000, 4096, precision="mixed")["trotter"][1] == "fp32"
+
+
+def test_roofline_skips_double_float_phases():
+    work = bench.phase_work(200, 30, 1000, 4096, precision="mixed_fast")
+    # (calls, device ms) over 2 blocks; the overlap is the largest phase but has no flop roofline
+    phases = {"overlap": (20, 60.0), "trotter": (20, 49.0), "vbuild_gemm": (20, 44.0), "e_gemm": (2, 20.0),
+              "energy": (2, 22.0), "qr": (4, 17.0)}
+    r = bench.roofline_for(phases, work, None, 2)
+    assert r["kernel"] == "trotter" and r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    flops_block = work["trotter"][0] * bench.STEPS_PER_BLOCK
+    assert r["achieved"] == pytest.approx(flops_block / (49.0 / 2 / 1000.0) / 1e12, rel=1e-4)
+    assert math.isclose(r["frac"], r["achieved"] / r["peak"], rel_tol=1e-3)
+    # the share excludes the composite energy phase that encloses e_gemm
+    assert r["share_of_step"] == pytest.approx(49.0 / (60 + 49 + 44 + 20 + 17), rel=1e-3)
+    assert bench.roofline_for(phases, work, None, 2, name="overlap") is None
+
+
+def test_roofline_binary64_form_keeps_fp64_phases(monkeypatch):
+    monkeypatch.setitem(bench._FMA_PEAK, True, (1.25, "given"))  # the in-process probe needs a GPU
+    work = bench.phase_work(200, 30, 1000, 4096, precision="fp64")
+    phases = {"vbuild_gemm": (20, 100.0), "overlap": (20, 10.0)}
+    r = bench.roofline_for(phases, work, None, 2)
+    assert r["kernel"] == "vbuild_gemm" and r["bound"] == "fp64" and r["peak"] == 1.25
+    r = bench.roofline_for(phases, work, None, 2, name="overlap")
+    assert r["kernel"] == "overlap" and r["bound"] == "fp64"
