@@ -64,11 +64,8 @@ int launch_e_minus_i(int n, const double* E, float* out, cudaStream_t s) {
 // tensor-core output fbm (rows w: Re, rows W + w: Im, fb = 2 fbm) and the
 // shifted fields written as the split left operand of the V-build GEMM:
 // per walker chunk [w0, w0 + wc) the Re rows come first, then the Im rows.
-// F32 (the three-section form, whose operands carry bf16 x 3 = 24 bits): the
-// shifted field is formed and split in fp32 (the force bias is fp32 already)
-// and only the four sums for the weight accumulate in binary64; otherwise
-// all of it is binary64.
-template <bool F32>
+// The six-section form: all of it in binary64 (k_field_shift_f32 below is the
+// three-section form's).
 __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* __restrict__ x,
                                     const float* __restrict__ fbm, long long ldf, const double2* __restrict__ mf,
                                     __nv_bfloat16* __restrict__ av, int S, int Kt, int sec,
@@ -81,21 +78,8 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
     __nv_bfloat16* re_row = av + (long long)(2 * w0 + (w - w0)) * Kt;
     __nv_bfloat16* im_row = av + (long long)(2 * w0 + wc + (w - w0)) * Kt;
     double sr = 0.0, si = 0.0, br = 0.0, bi = 0.0;
-    const float sdt = (float)sqrt_dt;
     for (int g = lane; g < S; g += 32) {
-        if (F32 && g < G) {
-            const float fr = 2.f * fbm[(long long)w * ldf + g], fi = 2.f * fbm[(long long)(W + w) * ldf + g];
-            const double2 md = mf[g];
-            const float mx = (float)md.x, my = (float)md.y, xv = (float)x[(size_t)w * G + g];
-            const float fsx = -sdt * (-fi - mx), fsy = -sdt * (fr - my);
-            const float xr = xv - fsx, xi = -fsy;
-            split_storef(re_row, S, g, xr, true, sec);
-            split_storef(im_row, S, g, xi, true, sec);
-            sr += (double)(xr * mx - xi * my);
-            si += (double)(xr * my + xi * mx);
-            br += (double)(xv * fsx - 0.5f * (fsx * fsx - fsy * fsy));
-            bi += (double)(xv * fsy - fsx * fsy);
-        } else if (g < G) {
+        if (g < G) {
             const double2 f = make_double2(2.0 * (double)fbm[(long long)w * ldf + g],
                                            2.0 * (double)fbm[(long long)(W + w) * ldf + g]);
             const double2 m = mf[g];
@@ -124,15 +108,78 @@ __global__ void k_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const 
     }
 }
 
+// The three-section form (operands of bf16 x 3 = 24 bits): the shifted field
+// is formed and split in fp32 (the force bias is fp32 already).  The CTA's
+// eight walkers share the mean-field shifts, staged once a CTA as fp32 in
+// chunks of FS_CH; each lane sums its ~G/32 terms of the four weight sums in
+// fp32 and the warp adds the lanes' sums in binary64.
+constexpr int FS_CH = 1024;
+__global__ void __launch_bounds__(256) k_field_shift_f32(int W, int G, int Wc, float sdt, const double* __restrict__ x,
+                                                         const float* __restrict__ fbm, long long ldf,
+                                                         const double2* __restrict__ mf,
+                                                         __nv_bfloat16* __restrict__ av, int S, int Kt, int sec,
+                                                         double2* __restrict__ shift_term,
+                                                         double2* __restrict__ fb_term) {
+    __shared__ float2 s_mf[FS_CH];
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const bool active = w < W;  // every thread takes part in the staging barriers
+    const int w0 = (w / Wc) * Wc;
+    const int wc = min(Wc, W - w0);
+    __nv_bfloat16* re_row = av + (long long)(2 * w0 + (w - w0)) * Kt;
+    __nv_bfloat16* im_row = av + (long long)(2 * w0 + wc + (w - w0)) * Kt;
+    float sr = 0.f, si = 0.f, br = 0.f, bi = 0.f;
+    for (int g0 = 0; g0 < S; g0 += FS_CH) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < FS_CH; e += blockDim.x) {
+            const int g = g0 + e;
+            const double2 m = g < G ? mf[g] : make_double2(0.0, 0.0);
+            s_mf[e] = make_float2((float)m.x, (float)m.y);
+        }
+        __syncthreads();
+        if (!active) continue;
+        const int g1 = min(S, g0 + FS_CH);
+        for (int g = g0 + lane; g < g1; g += 32) {
+            if (g < G) {
+                const float fr = 2.f * fbm[(long long)w * ldf + g], fi = 2.f * fbm[(long long)(W + w) * ldf + g];
+                const float2 m = s_mf[g - g0];
+                const float xv = (float)x[(size_t)w * G + g];
+                const float fsx = -sdt * (-fi - m.x), fsy = -sdt * (fr - m.y);
+                const float xr = xv - fsx, xi = -fsy;
+                split_storef(re_row, S, g, xr, true, sec);
+                split_storef(im_row, S, g, xi, true, sec);
+                sr += xr * m.x - xi * m.y;
+                si += xr * m.y + xi * m.x;
+                br += xv * fsx - 0.5f * (fsx * fsx - fsy * fsy);
+                bi += xv * fsy - fsx * fsy;
+            } else {
+                split_storef(re_row, S, g, 0.f, true, sec);
+                split_storef(im_row, S, g, 0.f, true, sec);
+            }
+        }
+    }
+    if (!active) return;
+    for (int k = sec * S + lane; k < Kt; k += 32) {
+        re_row[k] = __float2bfloat16(0.f);
+        im_row[k] = __float2bfloat16(0.f);
+    }
+    const double tr = warp_sum((double)sr), ti = warp_sum((double)si);
+    const double ur = warp_sum((double)br), ui = warp_sum((double)bi);
+    if (lane == 0) {
+        shift_term[w] = make_double2(tr, ti);
+        fb_term[w] = make_double2(ur, ui);
+    }
+}
+
 int launch_field_shift_mixed(int W, int G, int Wc, double sqrt_dt, const double* x, const float* fbm, long long ldf,
                              const double2* mf, __nv_bfloat16* av, int S, int Kt, int sec, double2* shift_term,
                              double2* fb_term, cudaStream_t s) {
     if (sec == 3)
-        k_field_shift_mixed<true><<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
-                                                              shift_term, fb_term);
+        k_field_shift_f32<<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, (float)sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
+                                                      shift_term, fb_term);
     else
-        k_field_shift_mixed<false><<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
-                                                               shift_term, fb_term);
+        k_field_shift_mixed<<<(W + 7) / 8, 256, 0, s>>>(W, G, Wc, sqrt_dt, x, fbm, ldf, mf, av, S, Kt, sec,
+                                                        shift_term, fb_term);
     AFQ_LAUNCHED("k_field_shift_mixed");
     return AFQ_OK;
 }
