@@ -473,20 +473,13 @@ int launch_trotter_mixed(int wc, int n, int o, int n_terms, double sqrt_dt, cons
 // determinant's purposes, from fp32 instructions only.
 constexpr int OS_CH = 32;  // rows of W per staging chunk (double-float m, then G_half)
 
-__device__ __forceinline__ void df_acc(float& s, float& e, float ch, float cl, float wh, float wl) {
-    const float p = __fmul_rn(ch, wh);
-    const float pe = __fmaf_rn(ch, wh, -p);  // exact: ch wh = p + pe
-    const float t = __fadd_rn(s, p);
-    const float v = __fsub_rn(t, s);
-    const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v));  // exact: s + p = t + r
-    s = t;
-    e = __fadd_rn(e, __fadd_rn(__fadd_rn(r, pe), __fmaf_rn(ch, wl, __fmul_rn(cl, wh))));
-}
-
-// df_acc on two lanes at once with the paired fp32 instructions (f32x2):
-// (s, e) += c (wr, wi) for one double-float c and a pair w = (wr, wi), hi and
-// lo parts in wh and wl.  The same roundings as two df_acc calls: a
-// subtraction y - x is fma(x, -1, y), and -p comes from (-c) w exactly.
+// (s, e) += c (wr, wi) on two lanes at once with the paired fp32
+// instructions (f32x2), for one double-float c = (ch, cl) and a pair
+// w = (wr, wi) with hi and lo parts in wh and wl: per lane p = ch wh and
+// pe = fma(ch, wh, -p) (TwoProd, exact), t + r = s + p (Knuth's TwoSum,
+// exact), s <- t and e <- e + ((r + pe) + fma(ch, wl, cl wh)).  A
+// subtraction y - x is fma(x, -1, y) (one rounding, as fsub), and -p comes
+// from (-c) w exactly.
 __device__ __forceinline__ void df_acc2(float2& s, float2& e, float ch, float cl, float2 wh, float2 wl) {
     const float2 m1 = make_float2(-1.f, -1.f);
     const float2 c2 = make_float2(ch, ch);
@@ -906,7 +899,7 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
 // Q with diag(R) real and > 0), by CholeskyQR2 in shared memory, one CTA per
 // walker, with the walker held as fp32 pairs x = x_hi + x_lo (48 significant
 // bits) and its products formed in double-float arithmetic on the fp32 pipe
-// (df_acc: TwoProd + TwoSum), which runs ~64x the binary64 rate here:
+// (df_acc2: TwoProd + TwoSum), which runs ~64x the binary64 rate here:
 //   pass 1: G1 = W_hi^H W_hi in fp32, R1 = chol(G1) in binary64,
 //           X = W R1^-1 by double-float forward substitution;
 //   pass 2: G2 = X^H X in double-float, R2 = chol(G2) in binary64,

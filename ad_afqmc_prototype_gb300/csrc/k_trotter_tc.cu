@@ -64,14 +64,10 @@ constexpr uint32_t TT_IDESC64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)
                                 ((uint32_t)(128 >> 4) << 24);
 static_assert(TT_SMEM <= 227 * 1024, "tensor-core Trotter shared memory");
 
-// Byte offset of element (row r, K index k) of B (K-major, 128-byte swizzle:
-// 16-byte chunk index XOR row % 8 within each 8-row, 1024-byte atom).
-__device__ __forceinline__ uint32_t tt_boff(int r, int k) {
-    return (uint32_t)((k >> 6) * TT_BBLK + (r >> 3) * 1024 + (r & 7) * 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) +
-                      ((k & 7) << 1));
-}
-
-// tt_boff(r, k) = kb(k) + rb(r) + (kx(k) ^ ((r & 7) << 4)) with the K parts
+// B is K-major with the 128-byte swizzle (16-byte chunk index XOR row % 8
+// within each 8-row, 1024-byte atom): element (row r, K index k) sits at byte
+//   (k >> 6) TT_BBLK + (r >> 3) 1024 + (r & 7) 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) + 2 (k & 7)
+// = kb(k) + rb(r) + (kx(k) ^ ((r & 7) << 4)) with the K parts
 // kb(k) = (k >> 6) TT_BBLK + 2 (k & 7), kx(k) = ((k & 63) >> 3) << 4 fixed
 // per thread (its rows k = i and k = kb0 + i) and rb(r) = (r >> 3) 1024 +
 // (r & 7) 128 a constant once the column loops are unrolled.
@@ -116,21 +112,6 @@ __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefe
 #define TT_R8(i)                                                                                               \
     "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
         "=r"(r[i + 7])
-// Six 8-column loads of this warp's 32 lanes, one wait.
-__device__ __forceinline__ void tmem_ld8x6(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4,
-                                           uint32_t a5, uint32_t (&r)[48]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%48];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%49];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%50];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%51];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%32, %33, %34, %35, %36, %37, %38, %39}, [%52];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40, %41, %42, %43, %44, %45, %46, %47}, [%53];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
-        : TT_R8(0), TT_R8(8), TT_R8(16), TT_R8(24), TT_R8(32), TT_R8(40)
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(a4), "r"(a5)
-        : "memory");
-}
 // Two 8-column loads (one wait) and stores (then wait for the stores).
 __device__ __forceinline__ void tmem_ld8x2(uint32_t a0, uint32_t a1, uint32_t (&r)[16]) {
     asm volatile(
