@@ -27,6 +27,40 @@ int check_cuda(cudaError_t e, const char* what);
         AFQ_TRY(::afq::check_cuda(cudaGetLastError(), name));     \
     } while (0)
 
+// ------------------------------------------------ per-device launch facts --
+// One process may drive several GPUs.  What a launcher learns on its first
+// launch on a device (the SM count, a raised dynamic shared-memory limit) is
+// kept per device ordinal behind a lock, never once per process.
+constexpr int kMaxDevices = 64;
+// Ordinal of the current device; AFQ_E_UNSUPPORTED beyond kMaxDevices.
+int current_device(int* dev);
+// SM count of the current device (looked up once per device).
+int device_sms(int* sms);
+// Per-device "done" flags of one launcher's one-time set-up (zero-initialised
+// as a static object).
+struct DeviceOnce {
+    bool done[kMaxDevices];
+};
+// Runs fn(arg) once per current device for `once`, under a library-wide
+// recursive lock; a failing fn leaves the flag clear.  fn returns AFQ_*.
+int device_once_run(DeviceOnce& once, int (*fn)(void*), void* arg);
+// Raises kernel's dynamic shared-memory limit to `bytes`, once per device.
+template <class K>
+int raise_smem_once(DeviceOnce& once, K kernel, int bytes) {
+    struct A {
+        K k;
+        int b;
+    } a{kernel, bytes};
+    return device_once_run(
+        once,
+        [](void* p) -> int {
+            A* x = (A*)p;
+            AFQ_CUDA(cudaFuncSetAttribute(x->k, cudaFuncAttributeMaxDynamicSharedMemorySize, x->b));
+            return AFQ_OK;
+        },
+        &a);
+}
+
 // ---------------------------------------------------------------- tracing --
 // afq_trace.cu: a process-wide count of kernel launches, and (when enabled
 // with afq_timing_enable) CUDA events recorded on the launching stream around

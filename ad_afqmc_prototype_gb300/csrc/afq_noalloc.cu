@@ -22,7 +22,10 @@
 //    from an earlier call need no clearing;
 //  - the first call on each device looks up that device's copy of the array
 //    (cudaGetSymbolAddress, with the device current) and caches the address;
-//    make that first call before any stream capture begins.
+//    make that first call before any stream capture begins.  The cache lives
+//    as long as the process: after cudaDeviceReset (or any reset of the
+//    device's primary context) the cached address is stale, so a process that
+//    resets a device must not call this entry point on it again.
 #include <mutex>
 
 #include "afq_internal.cuh"
@@ -35,7 +38,6 @@ namespace afq {
 static __device__ __align__(256) double g_comb_scratch[2 * AFQ_STATIC_MAX_WALKERS];
 
 namespace {
-constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 double* g_scratch_addr[kMaxDevices] = {};
 }  // namespace
@@ -43,8 +45,7 @@ double* g_scratch_addr[kMaxDevices] = {};
 // Device address of g_comb_scratch on the current device, looked up once.
 static int comb_scratch(double** out) {
     int dev = -1;
-    AFQ_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(AFQ_E_UNSUPPORTED, "device ordinal %d out of range", dev);
+    AFQ_TRY(current_device(&dev));
     std::lock_guard<std::mutex> lk(g_scratch_mu);
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;

@@ -43,6 +43,44 @@ bool timing_enabled() { return g_timing; }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// ------------------------------------------------ per-device launch facts --
+namespace {
+std::recursive_mutex g_dev_mu;
+int g_dev_sms[kMaxDevices] = {};
+}  // namespace
+
+int current_device(int* dev) {
+    int d = -1;
+    AFQ_CUDA(cudaGetDevice(&d));
+    if (d < 0 || d >= kMaxDevices) return fail(AFQ_E_UNSUPPORTED, "device ordinal %d out of range", d);
+    *dev = d;
+    return AFQ_OK;
+}
+
+int device_sms(int* sms) {
+    int dev = 0;
+    AFQ_TRY(current_device(&dev));
+    std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
+    if (!g_dev_sms[dev]) {
+        int v = 0;
+        AFQ_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        if (v < 1) return fail(AFQ_E_CUDA, "device %d reports %d SMs", dev, v);
+        g_dev_sms[dev] = v;
+    }
+    *sms = g_dev_sms[dev];
+    return AFQ_OK;
+}
+
+int device_once_run(DeviceOnce& once, int (*fn)(void*), void* arg) {
+    int dev = 0;
+    AFQ_TRY(current_device(&dev));
+    std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
+    if (once.done[dev]) return AFQ_OK;
+    AFQ_TRY(fn(arg));
+    once.done[dev] = true;
+    return AFQ_OK;
+}
+
 Phase::Phase(const char* n, cudaStream_t s) : name(n), stream(s), start(nullptr) {
     if (!g_timing) return;
     std::lock_guard<std::mutex> lk(g_mu);

@@ -254,27 +254,17 @@ struct ExchOut {
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
 // exchange contraction of each 32 x 32 block (ExchOut) instead of C.
 //
-// CM > 1: launched in clusters of CM CTAs that take CM consecutive M tiles of
-// one N tile.  Each CTA loads its A tile and rows [r BNT / CM, (r + 1) BNT /
-// CM) of the B tile (r its rank) into the same stage offset of every CTA in
-// the cluster (TMA multicast), so the cluster reads each B tile from L2 once
-// instead of CM times.  A stage is refilled only after every CTA's MMAs have
-// consumed it: each MMA thread's commit arrives on the empty barrier of
-// every CTA (count CM).
-template <int BNT, int MODE, int CM, int EWN>
+// Each CTA loads its own A and B tiles with plain TMA copies; the tile order
+// (M tiles fastest) makes the CTAs resident at one time work on one or two N
+// tiles, so a B tile is read from DRAM about once and served from L2 to the
+// CTAs that share it.
+template <int BNT, int MODE, int EWN>
 __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
                     int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
     using D = Drain<BNT, EWN>;
     static_assert(MODE != 2 || EWN == 8, "the exchange epilogue's transpose buffers are sized for eight warps");
-    static_assert(CM == 1 || CM == 2 || CM == 4, "cluster of 1, 2 or 4 CTAs along M");
-    if (CM > 1 && cluster_nctarank() != (uint32_t)CM) {  // launched without the cluster shape: nothing runs
-        if (threadIdx.x == 0) atomicExch(err, 1);
-        return;
-    }
-    const int rank = CM > 1 ? (int)cluster_ctarank() : 0;
-    const uint16_t cmask = (uint16_t)((1u << CM) - 1);
     constexpr bool SPLIT = MODE == 1;
     static_assert(MODE != 2 || BNT % 64 == 0, "the exchange epilogue takes whole 32 x 32 blocks per warp");
     constexpr int STG = D::STG, SLOTS = D::SLOTS, CW = D::CW;
@@ -291,14 +281,12 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mt = (M + BM - 1) / BM, nt = (N + BNT - 1) / BNT, kt = K / BK;
-    // cluster tiles: CM consecutive M tiles of one N tile; this CTA's is mg CM + rank
-    const int mtc = (mt + CM - 1) / CM, ntiles = mtc * nt, np = (kt + kd - 1) / kd;  // partials per tile
-    const int cid = blockIdx.x / CM, ncl = gridDim.x / CM;
+    const int ntiles = mt * nt, np = (kt + kd - 1) / kd;  // np: partials per tile
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STG; ++s) {
             mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, CM);
+            mbar_init(empty0 + 8 * s, 1);
         }
         for (int a = 0; a < SLOTS; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
@@ -316,7 +304,6 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (CM > 1) cluster_sync();  // every CTA's barriers are initialised before any multicast lands
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -330,18 +317,14 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             uint32_t issued_par[STG];
             for (int s = 0; s < STG; ++s) issued[s] = 0;
             bool ok = true;
-            for (int t = cid; ok && t < ntiles; t += ncl) {
-                const int mb = (t % mtc) * CM + rank, nb = t / mtc;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                const int mb = t % mt, nb = t / mt;
                 for (int kb = 0; kb < kt; ++kb) {
                     if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
                     mbar_expect_tx(full0 + 8 * stage, D::STAGE);
                     tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
-                    if (CM == 1)
-                        tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
-                    else
-                        tma_load_2d_mc(smem_u32(sB + stage * D::B_BYTES + rank * (D::B_BYTES / CM)), &tmB, kb * BK,
-                                       nb * BNT + rank * (BNT / CM), full0 + 8 * stage, cmask);
+                    tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
                     issued[stage] = 1;
                     issued_par[stage] = phase;
                     if (++stage == STG) { stage = 0; phase ^= 1; }
@@ -359,7 +342,7 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             int stage = 0, slot = 0;
             uint32_t phase = 0, slot_phase = 0;
             bool ok = true;
-            for (int t = cid; ok && t < ntiles; t += ncl) {
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 for (int kb = 0; kb < kt; ++kb) {
                     const int g = kb % kd;  // position inside the current partial
                     if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
@@ -370,8 +353,7 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
                     for (int k = 0; k < BK / 16; ++k)
                         umma_bf16_i(tmem + slot * BNT, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), D::IDESC,
                                     (k != 0) || (g != 0));
-                    if (CM == 1) umma_commit(empty0 + 8 * stage);
-                    else umma_commit_mc(empty0 + 8 * stage, cmask);
+                    umma_commit(empty0 + 8 * stage);
                     if (g == kd - 1 || kb == kt - 1) {
                         umma_commit(tfull0 + 8 * slot);
                         if (++slot == SLOTS) { slot = 0; slot_phase ^= 1; }
@@ -393,8 +375,8 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
         const bool vec = SPLIT ? (ldc % 8) == 0 && ((((uintptr_t)Ch) | ((uintptr_t)Cm)) & 15) == 0
                                : (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
-        for (int t = cid; ok && t < ntiles; t += ncl) {
-            const int mb = (t % mtc) * CM + rank, nb = t / mtc;
+        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            const int mb = t % mt, nb = t / mt;
             float2 acc[CW / 2];
 #pragma unroll
             for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
@@ -520,7 +502,6 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (CM > 1) cluster_sync();  // no CTA leaves while a peer may still write its shared memory
     if (warp == 1) {
         __syncwarp();
         tc_fence_after();
@@ -530,7 +511,7 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
 
 }  // namespace tc
 
-static int g_num_sms = 0;
+static DeviceOnce g_tn_smem;
 
 int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                       long long ldc, int* err, cudaStream_t s) {
@@ -541,56 +522,35 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
     AFQ_TRY(make_map(&mb, B, N, K, ldb, BN));
-    if (!g_num_sms) {
-        int dev = 0;
-        AFQ_CUDA(cudaGetDevice(&dev));
-        AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    }
+    int sms = 0;
+    AFQ_TRY(device_sms(&sms));
+    AFQ_TRY(raise_smem_once(g_tn_smem, k_gemm_tn, SMEM_BYTES));
     const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
-    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+    const int grid = (int)(tiles < sms ? tiles : sms);
     k_gemm_tn<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, M, N, K, ldc, err);
     AFQ_LAUNCHED("k_gemm_tn");
     return AFQ_OK;
 }
 
-// Clusters of DRAIN_CM CTAs along M share each B tile by TMA multicast
-// (k_gemm_tn_drain); the grid is as many clusters as are resident at once.
-constexpr int DRAIN_CM = 2;
-
+// Persistent launch: one CTA per SM (the shared-memory ring admits one), or
+// one per tile when there are fewer tiles.
 template <int BNT, int MODE, int EWN>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                         __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
                         tc::ExchOut xo = tc::ExchOut{}) {
     using namespace tc;
-    constexpr int CM = DRAIN_CM;
-    static int max_clusters = 0;
+    static DeviceOnce smem_once;
     constexpr int SMEM = Drain<BNT, EWN>::SMEM + (MODE == 2 ? XT_BYTES : 0);
-    auto kern = k_gemm_tn_drain<BNT, MODE, CM, EWN>;
+    auto kern = k_gemm_tn_drain<BNT, MODE, EWN>;
     CUtensorMap ma, mb;
     AFQ_TRY(make_map(&ma, A, M, K, lda, BM));
-    AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT / CM));
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = CM;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(Drain<BNT, EWN>::THREADS);
-    cfg.dynamicSmemBytes = SMEM;
-    cfg.stream = s;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (!max_clusters) {
-        AFQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        cfg.gridDim = dim3(CM * (g_num_sms / CM));
-        AFQ_CUDA(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
-        if (max_clusters < 1) return fail(AFQ_E_CUDA, "drained GEMM: no cluster of %d CTAs fits", CM);
-    }
-    const long long ctiles = (long long)((M + BM * CM - 1) / (BM * CM)) * ((N + BNT - 1) / BNT);
-    const int ncl = (int)(ctiles < max_clusters ? ctiles : max_clusters);
-    cfg.gridDim = dim3(CM * ncl);
-    AFQ_CUDA(cudaLaunchKernelEx(&cfg, kern, ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo));
+    AFQ_TRY(make_map(&mb, B, N, K, ldb, BNT));
+    int sms = 0;
+    AFQ_TRY(device_sms(&sms));
+    AFQ_TRY(raise_smem_once(smem_once, kern, SMEM));
+    const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
+    const int grid = (int)(tiles < sms ? tiles : sms);
+    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo);
     AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }
@@ -600,15 +560,8 @@ static int drain_prologue(int K, int kd) {
     if (K <= 0 || K % BK) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: K=%d must be a positive multiple of %d", K, BK);
     if (kd < 1) return fail(AFQ_E_INVALID_ARGUMENT, "tc gemm: k blocks per partial %d < 1", kd);
     AFQ_TRY(get_encode());
-    if (!g_num_sms) {
-        int dev = 0;
-        AFQ_CUDA(cudaGetDevice(&dev));
-        AFQ_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-        AFQ_CUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    }
     return AFQ_OK;
 }
-
 int launch_tc_gemm_tn_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                             long long ldc, int* err, cudaStream_t s, int kd) {
     if (M <= 0 || N <= 0) return AFQ_OK;

@@ -424,16 +424,11 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
     if (!trotter_tc_supported(n, o))
         return fail(AFQ_E_UNSUPPORTED, "tensor-core Trotter: norb=%d nocc=%d (needs norb %% 8 == 0, <= 256, nocc <= 32)",
                     n, o);
-    static bool attr = false;
-    static int nsm = 0;
+    static DeviceOnce smem_once;
     AFQ_TRY(get_encode());
-    if (!attr) {
-        int dev = 0;
-        AFQ_CUDA(cudaGetDevice(&dev));
-        AFQ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        AFQ_CUDA(cudaFuncSetAttribute(k_trotter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_SMEM));
-        attr = true;
-    }
+    int nsm = 0;
+    AFQ_TRY(device_sms(&nsm));
+    AFQ_TRY(raise_smem_once(smem_once, k_trotter_tc, TT_SMEM));
     CUtensorMap mvh, mvm, meh, mem;
     AFQ_TRY(make_map3(&mvh, vh, 2LL * wc, n, n, n, 128));
     AFQ_TRY(make_map3(&mvm, vm, 2LL * wc, n, n, n, 128));

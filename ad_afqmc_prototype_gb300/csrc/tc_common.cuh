@@ -86,40 +86,6 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
-// Cluster helpers (thread-block clusters of CTAs on neighbouring SMs).
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t cluster_nctarank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-    return r;
-}
-// every thread of every CTA of the cluster (release / acquire of shared memory)
-__device__ __forceinline__ void cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-// 2-D tile load written to the same shared-memory offset of every CTA in mask,
-// each copy completing bytes on the mbarrier at bar's offset in its CTA.
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
-                                               uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
-        "[%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
-        : "memory");
-}
-// arrive once on the mbarrier at bar's offset in every CTA of mask when this
-// thread's previously issued MMAs have completed
-__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
-                     "r"(bar),
-                 "h"(mask)
-                 : "memory");
-}
-
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -194,16 +160,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 
 // ------------------------------------------------------------------- host --
+// The driver's tensor-map encoder (the same for every device), looked up on
+// first use; the function-local static makes the lookup thread-safe.
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;  // per translation unit
 
-static int get_encode() {
-    if (g_encode) return AFQ_OK;
+static PFN_cuTensorMapEncodeTiled_v12000 lookup_encode() {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-        return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess) return nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+}
+
+static int get_encode() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = lookup_encode();
+    if (!fn) return fail(AFQ_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    g_encode = fn;
     return AFQ_OK;
 }
 
