@@ -196,8 +196,12 @@ int afq_orthogonalize(const afq_dims* d, const double* walkers, double* walkers_
                       double* det_r, void* stream);
 
 /* _sr_indices (walkers.py:233-240): comb indices (int32) and the inclusive
- * prefix sum of |w| (optional, may be NULL) in the engine's association
- * order (32-wide Hillis-Steele segments, recursive on segment totals). */
+ * prefix sum of |w| (optional, may be NULL).  The prefix sum adds in the
+ * association order of jax.lax.associative_scan (what jnp.cumsum lowers to):
+ * an up-sweep of pairwise sums e'[k] = e[2k] + e[2k+1], recursively scanned,
+ * then s[2k+1] = s'[k] and s[2k] = s'[k-1] + e[2k]; the search repeats
+ * jnp.searchsorted's default probe sequence (ceil(log2(W+1)) halvings,
+ * side='left').  Same inputs -> the same bits and indices as the reference. */
 size_t afq_sr_workspace(int32_t n_walkers);
 int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_t* idx,
                    double* cumsum, void* workspace, size_t workspace_bytes, void* stream);
@@ -211,7 +215,9 @@ int afq_sr_indices(int32_t n_walkers, const double* weights, double zeta, int32_
  * AFQ_E_UNSUPPORTED.  All calls on a device share that array: calls that
  * overlap on the GPU race, so order them on one stream.  The first call on
  * each device looks the array up (cudaGetSymbolAddress) and should come
- * before any stream capture.  Allocates nothing. */
+ * before any stream capture; the looked-up address is kept for the life of
+ * the process, so do not call this again on a device after resetting it
+ * (cudaDeviceReset).  Allocates nothing. */
 int afq_sr_indices_static(int32_t n_walkers, const double* weights, double zeta, int32_t* idx,
                           double* cumsum, void* stream);
 

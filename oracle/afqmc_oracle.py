@@ -16,14 +16,23 @@ reference file:line it follows.  Two deliberate interface differences:
   lowers to on CPU/GPU) and the probe sequence of ``jnp.searchsorted``'s
   default method, so indices are compared bit-exactly.
 
-Parity pins: the reference's own known-answer tests (weights = exp(-dt) and
-population shift 0.1 with zero Hamiltonian; E_loc = h0 with zero h1/chol;
-force bias = 2 L~ vec(solve(m^T, w^T))) are restated in tests/ against this
-oracle; QR, comb, Taylor and full-energy numerics are pinned by the committed
-golden fixtures under tests/golden/ produced by tests/golden/make_golden.py.
-The reference itself (JAX) is not importable in this environment, so no
-output of the reference program is used: parity with the reference is pinned
-through its tests' known answers and formula restatements only.
+Parity pins:
+* outputs of the reference's own code: tests/golden/make_ref_golden.py runs
+  the reference's hot-path modules unmodified on NumPy (a stand-in for the
+  few JAX names they use; JAX itself cannot be installed here) and records
+  contexts, overlaps, Green's functions, force biases, local energies, the
+  Taylor action, apply_trotter, the phase-fixed QR, comb indices on dyadic
+  weights, and whole afqmc_step / afqmc_block runs on injected draws (the
+  12-orbital workload and the 200-orbital benchmark Hamiltonian);
+  tests/test_ref_pins.py holds this oracle to them (1e-11 Ha per block);
+* the reference's own known-answer tests (weights = exp(-dt) and population
+  shift 0.1 with zero Hamiltonian; E_loc = h0 with zero h1/chol; force bias
+  = 2 L~ vec(solve(m^T, w^T))), restated in tests/;
+* first principles (Fock-space mixed estimators, exact exponentials).
+The comb's association order (XLA's, restated by ``assoc_scan``) is the one
+thing the NumPy run of the reference cannot show: its jnp.cumsum runs as a
+sequential sum there, so comb indices are pinned on dyadic weights, whose
+prefix sums are exact in every order.
 """
 from __future__ import annotations
 
