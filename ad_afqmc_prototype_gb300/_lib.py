@@ -23,6 +23,11 @@ AFQ_PREC_FP64 = 0
 AFQ_PREC_MIXED = 1
 AFQ_PREC_MIXED_FAST = 2
 
+AFQ_STATUS_WAIT_EXPIRED = 1
+AFQ_STATUS_SINGULAR = 2
+AFQ_STATUS_BAD_INDEX = 3
+AFQ_STATUS_NONFINITE = 4
+
 AFQ_CV_OFF = 0
 AFQ_CV_RECORD = 1
 AFQ_CV_ESTIMATE = 2
@@ -72,6 +77,8 @@ _SIGS = {
     "afq_prepare_lowp": (c_int32, [POINTER(afq_dims), P, P, P, c_size_t, P]),
     "afq_lowp_gemm_tn": (c_int32, [c_int32, c_int32, c_int32, P, c_int64, P, c_int64, P, c_int64, P, c_int32, P]),
     "afq_workspace_status": (c_int32, [P, POINTER(c_int32), P]),
+    "afq_workspace_counters": (c_int32, [P, POINTER(c_int32), POINTER(c_int32), P]),
+    "afq_selftest_wait": (c_int32, [c_int64, c_int32, P, P]),
     "afq_overlap": (c_int32, [POINTER(afq_dims), P, P, P, P]),
     "afq_half_green": (c_int32, [POINTER(afq_dims), P, P, P, P, P]),
     "afq_force_bias_workspace": (c_size_t, [POINTER(afq_dims)]),
@@ -90,6 +97,8 @@ _SIGS = {
     "afq_fill_normal": (c_int32, [c_int64, c_uint64, c_uint64, P, P]),
     "afq_fill_uniform": (c_int32, [c_int64, c_uint64, c_uint64, P, P]),
     "afq_field_shift": (c_int32, [POINTER(afq_dims), c_double, P, P, P, P, P, P, P]),
+    "afq_field_shift_lowp_bytes": (c_size_t, [c_int32, c_int32, c_int32]),
+    "afq_field_shift_lowp": (c_int32, [c_int32, c_int32, c_int32, c_double, P, P, P, P, P, P, c_size_t, P]),
     "afq_weight_update": (c_int32, [POINTER(afq_dims), POINTER(afq_params), POINTER(afq_problem), P, P,
                                     P, POINTER(afq_state), P]),
     "afq_block_measure": (c_int32, [c_int32, c_double, c_double, P, P, P, P, P, P, P]),

@@ -286,8 +286,10 @@ static SplitOut fb_split(const afq_dims* d, const StepWS& ws) {
 // green_ready: ws.Ag already holds the split G_half of the current walkers
 // (written by the previous step's overlap kernel or by the overlap refresh
 // after a QR inside the same block).
+// green_out (optional): the overlap pass after the propagation also writes
+// the new walkers' Green's function (fp32 values in binary64 storage) there.
 static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
-                      const StepWS& ws, bool green_ready, cudaStream_t s) {
+                      const StepWS& ws, bool green_ready, cudaStream_t s, double2* green_out = nullptr) {
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const LowpDims L = lowp_dims(d);
@@ -338,11 +340,11 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     }
     // overlaps, and the next step's force-bias operand from the same factorisation
     { AFQ_PHASE("overlap", s);
-      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s, nullptr, ws.csplit)); }
+      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s, green_out, ws.csplit)); }
     AFQ_PHASE("weight_update", s);
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
-                                st->pop_control_ene_shift, st->e_estimate, s);
+                                st->pop_control_ene_shift, st->e_estimate, s, ws.status);
 }
 
 // Local energies of all walkers into ws.energy (meas/rhf.py:36-50).
@@ -408,7 +410,8 @@ static int check_params(const afq_params* p) {
 }
 
 static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state* st, const double* fields,
-                     uint64_t seed, uint64_t counter, const StepWS& ws, cudaStream_t s, bool green_ready = false) {
+                     uint64_t seed, uint64_t counter, const StepWS& ws, cudaStream_t s, bool green_ready = false,
+                     double2* green_out = nullptr) {
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const double2* mo = (const double2*)pb->mo_coeff;
@@ -418,7 +421,7 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
         AFQ_TRY(launch_philox((int64_t)W * G, seed, counter, 1, ws.fields, s));
         fields = ws.fields;
     }
-    if (is_mixed(d->precision)) return step_mixed(pb, p, st, fields, ws, green_ready, s);
+    if (is_mixed(d->precision)) return step_mixed(pb, p, st, fields, ws, green_ready, s, green_out);
     // force bias (prop/afqmc.py:90-95)
     { AFQ_PHASE("green", s); AFQ_TRY(launch_green(W, n, o, mo, d->trial_is_real, walk, nullptr, ws.green, s)); }
     { AFQ_PHASE("fb_gemm", s); AFQ_TRY(force_bias_from_green(d, ws.green, pb->rot_chol, ws.fb, s)); }
@@ -435,7 +438,7 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
     // weights (prop/afqmc.py:116-138)
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
-                                st->pop_control_ene_shift, st->e_estimate, s);
+                                st->pop_control_ene_shift, st->e_estimate, s, ws.status);
 }
 
 // QR and overlap refresh (prop/blocks.py:53-57); in the mixed form the same
@@ -443,15 +446,29 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
 // QR of the walkers, then their overlaps from the same pass that writes
 // either the next step's force-bias operand (mixed, ws given) or, with
 // green_out, the Green's function the block's energy needs.
+//
+// Mixed forms, when the Green's function of the walkers before the QR is
+// already in place (ws given: the force-bias operand the last overlap pass
+// wrote; green_kept: green_out written by the last step): Q = W R^-1 leaves
+// G_half = (W m^-1)^T unchanged (m_Q = m R^-1), and det(C^H Q)^2 =
+// det(C^H W)^2 / det(R)^2, so the QR's det(R) updates the overlaps and no
+// overlap pass runs.  The binary64 form recomputes them, as the reference
+// does (prop/blocks.py:53-57).
 static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s,
                                   const StepWS* ws = nullptr, double2* green_out = nullptr,
-                                  const float2* cs = nullptr) {
+                                  const float2* cs = nullptr, double2* det_buf = nullptr, bool green_kept = false) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
+    const bool keep = is_mixed(d->precision) && det_buf && (ws || green_kept);
     {
         AFQ_PHASE("qr", s);
-        if (is_mixed(d->precision)) AFQ_TRY(launch_cholqr2(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+        if (is_mixed(d->precision))
+            AFQ_TRY(launch_cholqr2(d->n_walkers, d->norb, d->nocc, walk, walk, keep ? det_buf : nullptr, s));
         else AFQ_TRY(launch_qr(d->n_walkers, d->norb, d->nocc, walk, walk, nullptr, s));
+    }
+    if (keep) {
+        AFQ_PHASE("overlap_rescale", s);
+        return launch_overlap_div_det2(d->n_walkers, det_buf, (double2*)st->overlaps, s);
     }
     AFQ_PHASE(green_out ? "green" : "overlap", s);
     if (ws && is_mixed(d->precision))
@@ -550,21 +567,26 @@ int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda
     return launch_tc_gemm_tn(M, N, K, A, lda, B, ldb, C, ldc, err, as_stream(stream));
 }
 
-int afq_workspace_status(void* workspace, int32_t* status, void* stream) {
+int afq_workspace_counters(void* workspace, int32_t* status, int32_t* nonfinite, void* stream) {
     AFQ_NOTNULL(workspace); AFQ_NOTNULL(status);
     cudaStream_t s = as_stream(stream);
-    int32_t v = 0;
-    AFQ_CUDA(cudaMemcpyAsync(&v, workspace, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    int32_t v[2] = {0, 0};
+    AFQ_CUDA(cudaMemcpyAsync(v, workspace, sizeof(v), cudaMemcpyDeviceToHost, s));
     AFQ_CUDA(cudaStreamSynchronize(s));
-    *status = v;
-    if (v != 0) {
-        AFQ_CUDA(cudaMemsetAsync(workspace, 0, sizeof(int32_t), s));
-        return fail(AFQ_E_DEVICE_CHECK, "device-side check failed (status %d: %s)", v,
-                    v == AFQ_STATUS_WAIT_EXPIRED ? "a bounded wait expired"
-                    : v == AFQ_STATUS_SINGULAR   ? "singular matrix in an adjoint kernel"
-                                                 : "comb indices out of order or range");
-    }
+    *status = v[0];
+    if (nonfinite) *nonfinite = v[1];
+    if (v[0] != 0 || v[1] != 0) AFQ_CUDA(cudaMemsetAsync(workspace, 0, sizeof(v), s));
+    if (v[0] != 0)
+        return fail(AFQ_E_DEVICE_CHECK, "device-side check failed (status %d: %s)", v[0],
+                    v[0] == AFQ_STATUS_WAIT_EXPIRED ? "a bounded wait expired"
+                    : v[0] == AFQ_STATUS_SINGULAR   ? "singular matrix in an adjoint kernel"
+                    : v[0] == AFQ_STATUS_NONFINITE  ? "non-finite walker overlaps or weights"
+                                                    : "comb indices out of order or range");
     return AFQ_OK;
+}
+
+int afq_workspace_status(void* workspace, int32_t* status, void* stream) {
+    return afq_workspace_counters(workspace, status, nullptr, stream);
 }
 
 size_t afq_lowp_bytes(const afq_dims* d) {
@@ -762,6 +784,28 @@ int afq_field_shift(const afq_dims* d, double sqrt_dt, const double* fields, con
                               (double2*)fb_term, as_stream(stream));
 }
 
+size_t afq_field_shift_lowp_bytes(int32_t n_walkers, int32_t nchol, int32_t sections) {
+    if (n_walkers < 1 || nchol < 1 || (sections != 3 && sections != 6)) return 0;
+    const size_t Kt = ((size_t)sections * nchol + 63) / 64 * 64;
+    return 2 * (size_t)n_walkers * Kt * sizeof(__nv_bfloat16);
+}
+
+int afq_field_shift_lowp(int32_t n_walkers, int32_t nchol, int32_t sections, double sqrt_dt, const double* fields,
+                         const float* force_bias_half, const double* mf_shifts, double* shift_term,
+                         double* fb_term, void* split_out, size_t split_bytes, void* stream) {
+    if (n_walkers < 1 || nchol < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_walkers=%d nchol=%d", n_walkers, nchol);
+    if (sections != 3 && sections != 6) return fail(AFQ_E_INVALID_ARGUMENT, "sections=%d must be 3 or 6", sections);
+    AFQ_NOTNULL(fields); AFQ_NOTNULL(force_bias_half); AFQ_NOTNULL(mf_shifts); AFQ_NOTNULL(shift_term);
+    AFQ_NOTNULL(fb_term); AFQ_NOTNULL(split_out);
+    if (split_bytes < afq_field_shift_lowp_bytes(n_walkers, nchol, sections))
+        return fail(AFQ_E_WORKSPACE, "split_out holds %zu bytes, needs %zu", split_bytes,
+                    afq_field_shift_lowp_bytes(n_walkers, nchol, sections));
+    const int Kt = (sections * nchol + 63) / 64 * 64;
+    return launch_field_shift_mixed(n_walkers, nchol, n_walkers, sqrt_dt, fields, force_bias_half, nchol,
+                                    (const double2*)mf_shifts, (__nv_bfloat16*)split_out, nchol, Kt, sections,
+                                    (double2*)shift_term, (double2*)fb_term, as_stream(stream));
+}
+
 int afq_weight_update(const afq_dims* d, const afq_params* p, const afq_problem* pb, const double* shift_term,
                       const double* fb_term, const double* overlaps_new, const afq_state* st, void* stream) {
     AFQ_TRY(check_dims(d, false));
@@ -847,20 +891,27 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
     cudaStream_t s = as_stream(stream);
     const int W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
     const size_t fstride = (size_t)W * G;
+    // the block-end measurement reads the fp32 Green's function that the last
+    // step's overlap pass writes (the QR leaves it unchanged): the three-section
+    // form's energy, and either mixed form's control-variate measurement
+    const bool green_kept = is_mixed(d->precision) && p->n_prop_steps > 0 &&
+                            (cvmode != AFQ_CV_OFF || d->precision == AFQ_PREC_MIXED_FAST);
     // prop/blocks.py:38-51
     for (int st_i = 0; st_i < p->n_prop_steps; ++st_i) {
         // from the second step on, the previous overlap kernel left the force-bias operand
+        const bool last = st_i + 1 == p->n_prop_steps;
         AFQ_TRY(step_impl(pb, p, st, fields ? fields + st_i * fstride : nullptr, seed, counter + st_i, ws.step, s,
-                          st_i > 0));
+                          st_i > 0, green_kept && last ? ws.green : nullptr));
         if (p->qr_every > 0 && (st_i + 1) % p->qr_every == 0 && st_i + 1 < p->n_prop_steps)
-            AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step));
+            AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step, nullptr, nullptr, ws.step.ovl_new));
     }
     // prop/blocks.py:53-57, with the energy's Green's function from the same pass
     if (is_mixed(d->precision))
         AFQ_TRY(launch_split_c(n * o, (const double2*)pb->mo_coeff, ws.step.csplit, s));
     if (cvmode == AFQ_CV_OFF) {
         AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green,
-                                       is_mixed(d->precision) ? ws.step.csplit : nullptr));
+                                       is_mixed(d->precision) ? ws.step.csplit : nullptr, ws.step.ovl_new,
+                                       green_kept));
         // prop/blocks.py:59-79
         AFQ_TRY(energy_impl(pb, st, ws, s, true));
         AFQ_PHASE("block_measure", s);
@@ -871,11 +922,15 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
         Arena la((void*)pb->lowp, (size_t)-1);
         const LowpBufs lb = layout_lowp(la, d);
         double2* walk = (double2*)st->walkers;
-        { AFQ_PHASE("qr", s); AFQ_TRY(launch_cholqr2(W, n, o, walk, walk, nullptr, s)); }
-        // overlaps, the Green's function and its force-bias operand in one pass; the GEMM gives c_g
-        { AFQ_PHASE("green", s);
-          AFQ_TRY(launch_overlap_split(W, n, o, (const double2*)pb->mo_coeff, walk, (double2*)st->overlaps,
-                                       fb_split(d, ws.step), s, ws.green, ws.step.csplit)); }
+        if (green_kept) {  // the Green's function and its force-bias operand are the last step's
+            AFQ_TRY(orthonormalize_refresh(pb, st, s, &ws.step, nullptr, nullptr, ws.step.ovl_new));
+        } else {
+            { AFQ_PHASE("qr", s); AFQ_TRY(launch_cholqr2(W, n, o, walk, walk, nullptr, s)); }
+            // overlaps, the Green's function and its force-bias operand in one pass; the GEMM gives c_g
+            { AFQ_PHASE("green", s);
+              AFQ_TRY(launch_overlap_split(W, n, o, (const double2*)pb->mo_coeff, walk, (double2*)st->overlaps,
+                                           fb_split(d, ws.step), s, ws.green, ws.step.csplit)); }
+        }
         { AFQ_PHASE("fb_gemm", s);
           AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.step.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.step.fbm, G,
                                           ws.step.status, s)); }

@@ -280,10 +280,13 @@ int launch_trotter(int W, int n, int o, int n_terms, double sqrt_dt, const doubl
 int launch_field_shift(int W, int G, double sqrt_dt, const double* x, const double2* fb,
                        const double2* mf, double2* xs, double2* shift_term, double2* fb_term,
                        cudaStream_t s);
+// overlaps[w] /= det_r[w]^2 (the overlaps of QR'd walkers from their QR's det(R))
+int launch_overlap_div_det2(int W, const double2* det_r, double2* overlaps, cudaStream_t s);
 int launch_weight_update(int W, const afq_params* p, double sqrt_dt, double dt,
                          double2 h0_prop, const double2* shift_term, const double2* fb_term,
                          const double2* ovlp_new, double* weights, double2* overlaps,
-                         double* pop_shift, const double* e_est, cudaStream_t s);
+                         double* pop_shift, const double* e_est, cudaStream_t s,
+                         int* status = nullptr);  // status: a workspace's status word, counts non-finite walkers
 int launch_energy(int W, int n, int o, int G, double h0, const double2* green,
                   const void* rot_chol, int trial_real, const double2* rot_h1,
                   double* partial, double2* energy, cudaStream_t s);

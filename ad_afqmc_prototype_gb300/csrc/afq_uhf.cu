@@ -212,7 +212,7 @@ int step_u(const afq_problem* pb, const afq_params* p, const afq_state* st, cons
     AFQ_PHASE("weight_update", s);
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 u.shift_term, u.fb_term, u.ov_new, st->weights, (double2*)st->overlaps,
-                                st->pop_control_ene_shift, st->e_estimate, s);
+                                st->pop_control_ene_shift, st->e_estimate, s, u.status);
 }
 
 // QR of both spins, then the pairs' overlaps (and G_half when green is given)

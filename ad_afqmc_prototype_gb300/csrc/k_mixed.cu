@@ -570,6 +570,7 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     __shared__ double2 s_rp;
     __shared__ float4 s_rpd;
     __shared__ double2 s_det;
+    __shared__ int s_zero;
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
@@ -644,7 +645,10 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
         for (int e = tid; e < o * o; e += blockDim.x)
             invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
     }
-    if (tid == 0) s_det = make_double2(1.0, 0.0);
+    if (tid == 0) {
+        s_det = make_double2(1.0, 0.0);
+        s_zero = 0;
+    }
     __syncthreads();
 
     // One pivot loop for both factorisations of m, three barriers a step:
@@ -698,6 +702,7 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
                 }
                 const double2 d = cmul(s_det, piv);
                 s_det = (bi != k) ? make_double2(-d.x, -d.y) : d;
+                if (piv.x == 0.0 && piv.y == 0.0) s_zero = 1;
             }
         } else if (k < o && wid == 1) {
             float best = -1.f;
@@ -793,7 +798,8 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
         }
         __syncthreads();
     }
-    if (tid == 0 && ovlp_out) ovlp_out[w] = cmul(s_det, s_det);
+    // an exactly zero pivot: m is singular and det(m) is exactly 0 (as LAPACK's LU gives it)
+    if (tid == 0 && ovlp_out) ovlp_out[w] = s_zero ? make_double2(0.0, 0.0) : cmul(s_det, s_det);
 
     // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
     __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;

@@ -111,10 +111,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                // let the copies this thread issued land before the CTA exits
-                for (int s = 0; s < STAGES; ++s)
-                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
             }
+            // every copy this thread issued lands before the CTA exits (after an
+            // abort elsewhere in the CTA nobody else waits for them)
+            for (int s = 0; s < STAGES; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -142,10 +143,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                // MMAs already issued must finish before the tensor memory is freed
-                umma_commit(drain);
-                mbar_wait(drain, 0, nullptr);
             }
+            // every MMA issued finishes before the tensor memory is freed, also
+            // when the epilogue gave up waiting for it
+            umma_commit(drain);
+            mbar_wait(drain, 0, nullptr);
         }
     } else {
         const int q = warp & 3;  // TMEM lane quarter this warp may access
@@ -333,9 +335,11 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                for (int s = 0; s < STG; ++s)
-                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
             }
+            // every copy this thread issued lands before the CTA exits (after an
+            // abort elsewhere in the CTA nobody else waits for them)
+            for (int s = 0; s < STG; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -364,9 +368,11 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                umma_commit(drain);
-                mbar_wait(drain, 0, nullptr);
             }
+            // every MMA issued finishes before the tensor memory is freed, also
+            // when the epilogue gave up waiting for it
+            umma_commit(drain);
+            mbar_wait(drain, 0, nullptr);
         }
     } else if (warp >= D::EW0) {
         const int q = warp & 3, cb = ((warp - D::EW0) >> 2) * CW;

@@ -231,9 +231,11 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                for (int s = 0; s < TT_STG; ++s)
-                    if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
             }
+            // every copy this thread issued lands before the CTA exits (after an
+            // abort elsewhere in the CTA nobody else waits for them)
+            for (int s = 0; s < TT_STG; ++s)
+                if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -274,9 +276,11 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             if (!ok) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
-                umma_commit(drain);
-                mbar_wait(drain, 0, nullptr);
             }
+            // every MMA issued finishes before the tensor memory is freed, also
+            // when the epilogue gave up waiting for it
+            umma_commit(drain);
+            mbar_wait(drain, 0, nullptr);
         }
     } else {
         const int q = warp & 3, mt = (warp - 2) >> 2;

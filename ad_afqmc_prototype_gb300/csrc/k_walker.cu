@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
     extern __shared__ double2 sm[];
     double2* m = sm;          // o x o
     double2* inv = sm + o * o;  // o x o
-    __shared__ int s_piv;
+    __shared__ int s_piv, s_zero;
     __shared__ double2 s_det;
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
@@ -71,7 +71,10 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
         for (int e = tid; e < o * o; e += blockDim.x)
             inv[e] = make_double2((e / o) == (e % o) ? 1.0 : 0.0, 0.0);
     }
-    if (tid == 0) s_det = make_double2(1.0, 0.0);
+    if (tid == 0) {
+        s_det = make_double2(1.0, 0.0);
+        s_zero = 0;
+    }
     __syncthreads();
 
     for (int k = 0; k < o; ++k) {
@@ -106,6 +109,7 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
         if (tid == 0) {
             double2 d = cmul(s_det, piv);
             s_det = (p != k) ? make_double2(-d.x, -d.y) : d;
+            if (piv.x == 0.0 && piv.y == 0.0) s_zero = 1;
         }
         const double2 rp = cdiv(make_double2(1.0, 0.0), piv);
         __syncthreads();
@@ -128,7 +132,12 @@ __global__ void __launch_bounds__(256) k_green(int n, int o, const double2* __re
         }
         __syncthreads();
     }
-    if (ovlp_out && tid == 0) ovlp_out[w] = ov_square ? cmul(s_det, s_det) : s_det;
+    // An exactly zero pivot (the rest of its column is zero too: m is singular)
+    // makes det(m) exactly 0, as LAPACK's LU gives it (getrf leaves the zero
+    // on U's diagonal); the division by it has made the inverse, and so the
+    // Green's function, non-finite, as the reference's solve does.
+    if (ovlp_out && tid == 0)
+        ovlp_out[w] = s_zero ? make_double2(0.0, 0.0) : ov_square ? cmul(s_det, s_det) : s_det;
     if (!green_out && !split.ptr) return;
     // G_half[b, i] = sum_a W[i, a] inv[a, b]
     if (green_out) {
@@ -389,12 +398,18 @@ int launch_field_shift(int W, int G, double sqrt_dt, const double* x, const doub
 // walker are a few hundred binary64 operations), then one CTA reduces the
 // mean weight feeding the population-control shift in a fixed order
 // (thread t sums walkers t, t + 1024, ...; then the warps and the CTA).
+//
+// Non-finite walkers: a NaN or infinite new overlap or weight propagates as
+// in the reference (its floor and cap comparisons are false for NaN, so the
+// weight stays NaN and the mean weight, hence the population shift, turns
+// NaN).  With a status word (status != nullptr) every such walker is counted
+// into status[1] and status[0] is set to AFQ_STATUS_NONFINITE if it was 0.
 // =====================================================================
 __global__ void __launch_bounds__(256) k_weight_update(
     int W, double dt, double sqrt_dt, double w_floor, double w_cap, double2 h0_prop,
     const double2* __restrict__ shift_term, const double2* __restrict__ fb_term,
     const double2* __restrict__ ovlp_new, double* __restrict__ weights, double2* __restrict__ overlaps,
-    const double* __restrict__ pop_shift) {
+    const double* __restrict__ pop_shift, int* __restrict__ status) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
     const double ps = pop_shift[0];
@@ -406,6 +421,10 @@ __global__ void __launch_bounds__(256) k_weight_update(
     if (wn > w_cap) wn = 0.0;
     weights[w] = wn;
     overlaps[w] = on;
+    if (status && !(isfinite(wn) && isfinite(on.x) && isfinite(on.y))) {
+        atomicAdd(status + 1, 1);
+        atomicCAS(status, 0, AFQ_STATUS_NONFINITE);
+    }
 }
 
 __global__ void __launch_bounds__(1024) k_weight_mean(int W, double dt, double damping,
@@ -429,13 +448,30 @@ __global__ void __launch_bounds__(1024) k_weight_mean(int W, double dt, double d
     }
 }
 
+// Overlaps after a QR from those before it: det(C^H Q)^2 = det(C^H W)^2 /
+// det(R)^2 for Q = W R^-1 (walkers.py:183-203's restricted normalisation).
+__global__ void k_overlap_div_det2(int W, const double2* __restrict__ det_r, double2* __restrict__ overlaps) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    const double2 r = det_r[w];
+    overlaps[w] = cdiv(overlaps[w], cmul(r, r));
+}
+
+int launch_overlap_div_det2(int W, const double2* det_r, double2* overlaps, cudaStream_t s) {
+    if (W <= 0) return AFQ_OK;
+    k_overlap_div_det2<<<(W + 255) / 256, 256, 0, s>>>(W, det_r, overlaps);
+    AFQ_LAUNCHED("k_overlap_div_det2");
+    return AFQ_OK;
+}
+
 int launch_weight_update(int W, const afq_params* p, double sqrt_dt, double dt, double2 h0_prop,
                          const double2* shift_term, const double2* fb_term, const double2* ovlp_new,
                          double* weights, double2* overlaps, double* pop_shift, const double* e_est,
-                         cudaStream_t s) {
+                         cudaStream_t s, int* status) {
     if (W <= 0) return AFQ_OK;
     k_weight_update<<<(W + 255) / 256, 256, 0, s>>>(W, dt, sqrt_dt, p->weight_floor, p->weight_cap, h0_prop,
-                                                    shift_term, fb_term, ovlp_new, weights, overlaps, pop_shift);
+                                                    shift_term, fb_term, ovlp_new, weights, overlaps, pop_shift,
+                                                    status);
     AFQ_LAUNCHED("k_weight_update");
     k_weight_mean<<<1, 1024, 0, s>>>(W, dt, p->pop_control_damping, weights, pop_shift, e_est);
     AFQ_LAUNCHED("k_weight_mean");

@@ -43,30 +43,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with `parity`; false on timeout or abort.
-// The abort flag and the timer are read every 16th poll: a poll that has
-// just failed costs no timer read on the way to the next one.
-__device__ __forceinline__ bool mbar_wait_inl(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+// Bounded wait for the phase with `parity`; false on timeout (limit_ns of
+// the global timer) or abort.  The abort flag and the timer are read every
+// 16th poll: a poll that has just failed costs no timer read on the way to
+// the next one.
+__device__ __forceinline__ bool mbar_wait_inl(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                              unsigned long long limit_ns = WAIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = now_ns();
     for (unsigned it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 15u) == 0u) {
             if (abort_flag && *abort_flag) return false;
-            if (now_ns() - t0 > WAIT_NS) return false;
+            if (now_ns() - t0 > limit_ns) return false;
         }
     }
 }
-static __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (unsigned it = 1;; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 15u) == 0u) {
-            if (abort_flag && *abort_flag) return false;
-            if (now_ns() - t0 > WAIT_NS) return false;
-        }
-    }
+static __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                              unsigned long long limit_ns = WAIT_NS) {
+    return mbar_wait_inl(bar, parity, abort_flag, limit_ns);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {

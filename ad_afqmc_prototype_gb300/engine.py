@@ -326,6 +326,27 @@ def workspace_status():
     return v.value
 
 
+def workspace_counters():
+    """(status, nonfinite): the status word of the step / block workspace and
+    the number of walker updates that produced a NaN or infinite overlap or
+    weight since the last read; both are cleared (synchronises the stream).
+    Does not raise on a set status."""
+    b = _arena.buf.get(torch.cuda.current_device())
+    if b is None:
+        return 0, 0
+    v, nf = ctypes.c_int32(0), ctypes.c_int32(0)
+    _lib.load().afq_workspace_counters(ptr(b), ctypes.byref(v), ctypes.byref(nf), stream_ptr())
+    return v.value, nf.value
+
+
+def selftest_wait(limit_ns: int, arrive: bool) -> int:
+    """Runs the bounded-wait self-test (afq_selftest_wait) and returns the
+    device status it wrote: AFQ_STATUS_WAIT_EXPIRED when nothing arrived."""
+    out = torch.full((1,), -1, dtype=torch.int32, device=device())
+    _lib.call("afq_selftest_wait", int(limit_ns), 1 if arrive else 0, ptr(out), stream_ptr())
+    return int(out.item())
+
+
 def make_params(params, n_prop_steps: Optional[int] = None) -> afq_params:
     return afq_params(float(params.dt), float(params.pop_control_damping), float(params.weight_floor),
                       float(params.weight_cap), float(params.shift_ema), int(params.n_exp_terms),

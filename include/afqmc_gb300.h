@@ -146,11 +146,28 @@ int afq_lowp_gemm_tn(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda
 
 /* Device status word of a step / block / gradient workspace: synchronises
  * `stream`, copies the word to *status (0 = fine, AFQ_STATUS_* otherwise)
- * and clears it.  Returns AFQ_E_DEVICE_CHECK when the word was set. */
+ * and clears it (and the non-finite walker count).  Returns
+ * AFQ_E_DEVICE_CHECK when the word was set.  The first condition raised
+ * since the last clear is the one reported. */
 #define AFQ_STATUS_WAIT_EXPIRED 1 /* a bounded device-side wait expired */
 #define AFQ_STATUS_SINGULAR 2     /* adjoint: a singular overlap matrix or QR factor R */
 #define AFQ_STATUS_BAD_INDEX 3    /* adjoint: comb indices out of range or not non-decreasing */
+#define AFQ_STATUS_NONFINITE 4    /* a walker's new overlap or weight was NaN or infinite */
 int afq_workspace_status(void* workspace, int32_t* status, void* stream);
+/* As afq_workspace_status, and *nonfinite receives how many walker updates
+ * produced a NaN or infinite overlap or weight since the last clear.  Such a
+ * walker propagates as in the reference (prop/afqmc.py:116-138: its NaN
+ * weight passes the floor and cap and turns the mean weight NaN); the count
+ * only reports it. */
+int afq_workspace_counters(void* workspace, int32_t* status, int32_t* nonfinite, void* stream);
+
+/* Bounded-wait self-test (no counterpart in the reference): one thread waits
+ * on a fresh mbarrier with the same bounded wait the tensor-core pipelines
+ * use, for at most limit_ns nanoseconds of the GPU's global timer.  With
+ * arrive = 0 nothing ever arrives, the wait expires and *status (device
+ * int32) is set to AFQ_STATUS_WAIT_EXPIRED; with arrive = 1 the thread
+ * arrives first and *status is set to 0.  limit_ns must be in (0, 10 s]. */
+int afq_selftest_wait(int64_t limit_ns, int32_t arrive, int32_t* status, void* stream);
 
 /* ---- per-walker kernels, batched over walkers --------------------------- */
 
@@ -244,6 +261,20 @@ int afq_fill_uniform(int64_t count, uint64_t seed, uint64_t counter, double* out
 int afq_field_shift(const afq_dims* d, double sqrt_dt, const double* fields,
                     const double* force_bias, const double* mf_shifts, double* shifted_fields,
                     double* shift_term, double* fb_term, void* stream);
+
+/* The mixed forms' field shift (prop/afqmc.py:97-101, as afq_field_shift)
+ * from the fp32 force bias the tensor-core GEMM gives: force_bias_half is
+ * (2W, G) fp32, rows w = Re fb_w / 2 and W + w = Im fb_w / 2.  sections 6
+ * (AFQ_PREC_MIXED) forms the shifts and the four weight sums in binary64;
+ * sections 3 (AFQ_PREC_MIXED_FAST) forms them in fp32 (its operands carry 24
+ * bits), sums each lane's terms in fp32 and the lanes in binary64.
+ * shift_term, fb_term (W,) c128; split_out receives the shifted fields as
+ * the V-build's bf16 split rows (afq_field_shift_lowp_bytes bytes). */
+size_t afq_field_shift_lowp_bytes(int32_t n_walkers, int32_t nchol, int32_t sections);
+int afq_field_shift_lowp(int32_t n_walkers, int32_t nchol, int32_t sections, double sqrt_dt,
+                         const double* fields, const float* force_bias_half, const double* mf_shifts,
+                         double* shift_term, double* fb_term, void* split_out, size_t split_bytes,
+                         void* stream);
 
 /* prop/afqmc.py:116-138: importance weights with the phaseless cut, floor and
  * cap, population-control shift.  Updates st->weights, st->overlaps (copied

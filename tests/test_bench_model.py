@@ -1,7 +1,8 @@
 """CPU checks of bench.py's work model and roofline selection (no GPU):
-the tensor-core Taylor products count as tensor work, the mixed forms'
-double-float phases never become the roofline kernel, and the roofline's
-numbers follow from the phase times."""
+the tensor-core Taylor products run on the tensor pipe, the roofline counts
+algorithmic work (the executed split-operand work beside it), the mixed
+forms' double-float phases are measured against the fp32 pipe, and the
+roofline's numbers follow from the phase times."""
 import math
 
 import pytest
@@ -25,19 +26,26 @@ def test_phase_work_pipes_per_precision():
     assert bench.phase_work(200, 30, 1000, 4096, precision="mixed")["trotter"][1] == "fp32"
 
 
-def test_roofline_skips_double_float_phases():
+def test_roofline_is_algorithmic_with_executed_beside(monkeypatch):
+    monkeypatch.setitem(bench._FMA_PEAK, False, (70.0, "given"))  # fp32 SIMT peak (the probe needs a GPU)
     work = bench.phase_work(200, 30, 1000, 4096, precision="mixed_fast")
-    # (calls, device ms) over 2 blocks; the overlap is the largest phase but has no flop roofline
-    phases = {"overlap": (20, 60.0), "trotter": (20, 49.0), "vbuild_gemm": (20, 44.0), "e_gemm": (2, 20.0),
+    alg = bench.algorithmic_work(200, 30, 1000, 4096)
+    # (calls, device ms) over 2 blocks
+    phases = {"overlap": (20, 30.0), "trotter": (20, 49.0), "vbuild_gemm": (20, 44.0), "e_gemm": (2, 20.0),
               "energy": (2, 22.0), "qr": (4, 17.0)}
-    r = bench.roofline_for(phases, work, None, 2)
+    r = bench.roofline_for(phases, work, None, 2, alg=alg)
     assert r["kernel"] == "trotter" and r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
-    flops_block = work["trotter"][0] * bench.STEPS_PER_BLOCK
+    # achieved counts the reference's flops (8 n_terms + 8) n^2 o per walker, not the three bf16 sections
+    flops_block = (8 * 6 + 8) * 200 ** 2 * 30 * 4096 * bench.STEPS_PER_BLOCK
     assert r["achieved"] == pytest.approx(flops_block / (49.0 / 2 / 1000.0) / 1e12, rel=1e-4)
     assert math.isclose(r["frac"], r["achieved"] / r["peak"], rel_tol=1e-3)
+    assert r["executed_achieved"] == pytest.approx(3 * r["achieved"], rel=1e-3)
     # the share excludes the composite energy phase that encloses e_gemm
-    assert r["share_of_step"] == pytest.approx(49.0 / (60 + 49 + 44 + 20 + 17), rel=1e-3)
-    assert bench.roofline_for(phases, work, None, 2, name="overlap") is None
+    assert r["share_of_step"] == pytest.approx(49.0 / (30 + 49 + 44 + 20 + 17), rel=1e-3)
+    # the double-float phases are measured against the fp32 pipe they run on
+    ov = bench.roofline_for(phases, work, None, 2, name="overlap", alg=alg)
+    assert ov["bound"] == "fp32" and ov["peak"] == 70.0 and "executed_achieved" not in ov
+    assert ov["achieved"] == pytest.approx(alg["overlap"] * 10 / (30.0 / 2 / 1000.0) / 1e12, rel=1e-4)
 
 
 def test_roofline_binary64_form_keeps_fp64_phases(monkeypatch):

@@ -163,3 +163,48 @@ def test_c5_block_matches_fp64(cuda, prec):
     assert engine.workspace_status() == 0
     print(f"C5 {prec}: E_fp64 {float(ea):.8f}  |dE| {abs(float(ea) - float(eb)):.2e}")
     assert abs(float(ea) - float(eb)) < 1e-4
+
+
+def test_three_section_field_shift_against_binary64(cuda):
+    """The three-section form's field shift (fp32 terms, fp32 lane sums, binary64
+    warp sum) against the six-section kernel (binary64 throughout) on the same
+    fp32 force bias, at the 200-orbital workload's 1000 Cholesky vectors with
+    the binary64 force bias of its trial walkers: shift_term and fb_term (the
+    two weight sums in the exponent of the walker weight) to 2e-6 relative of
+    their magnitude (observed: about 2e-7)."""
+    import ctypes
+    from ad_afqmc_prototype_gb300 import _lib, engine
+    from tests.test_gpu_step import cpu
+    pb, params, st = _setup("c4_n200_o30_g1000_w4096", 256, "fp64")
+    W, G = 256, pb.nchol
+    rng = np.random.default_rng(11)
+    w = st.walkers + 0.05 * torch.as_tensor(rng.normal(size=tuple(st.walkers.shape)), device="cuda")
+    fb = engine.force_bias(w.contiguous(), pb.mo, pb.rot_chol, True)  # (W, G) c128
+    half = torch.cat([fb.real, fb.imag], 0).mul(0.5).to(torch.float32).contiguous()  # (2W, G)
+    x = torch.as_tensor(rng.standard_normal((W, G)), device="cuda")
+    lib = _lib.load()
+    out = {}
+    for sec in (3, 6):
+        nb = int(lib.afq_field_shift_lowp_bytes(W, G, sec))
+        split = torch.empty((nb,), dtype=torch.uint8, device="cuda")
+        sh = torch.empty((W,), dtype=torch.complex128, device="cuda")
+        ft = torch.empty((W,), dtype=torch.complex128, device="cuda")
+        _lib.call("afq_field_shift_lowp", W, G, sec, float(np.sqrt(params.dt)), engine.ptr(x), engine.ptr(half),
+                  engine.ptr(pb.mf_shifts), engine.ptr(sh), engine.ptr(ft), engine.ptr(split), nb,
+                  engine.stream_ptr())
+        out[sec] = (cpu(sh), cpu(ft))
+    for k in range(2):
+        a, b = out[3][k], out[6][k]
+        err = np.max(np.abs(a - b)) / np.max(np.abs(b))
+        assert err < 2e-6, (k, err)
+    # the binary64 kernel is the binary64 field shift of the fp32-rounded force bias
+    fb32 = (half[:W].double() + 1j * half[W:].double()) * 2.0
+    d = engine.make_dims(W, pb.norb, pb.nocc, G, True)
+    xs = torch.empty((W, G), dtype=torch.complex128, device="cuda")
+    sh = torch.empty((W,), dtype=torch.complex128, device="cuda")
+    ft = torch.empty((W,), dtype=torch.complex128, device="cuda")
+    _lib.call("afq_field_shift", ctypes.byref(d), float(np.sqrt(params.dt)), engine.ptr(x),
+              engine.ptr(fb32.contiguous()), engine.ptr(pb.mf_shifts), engine.ptr(xs), engine.ptr(sh), engine.ptr(ft),
+              engine.stream_ptr())
+    np.testing.assert_allclose(out[6][0], cpu(sh), rtol=1e-12, atol=1e-12 * np.max(np.abs(cpu(sh))))
+    np.testing.assert_allclose(out[6][1], cpu(ft), rtol=1e-12, atol=1e-12 * np.max(np.abs(cpu(ft))))
