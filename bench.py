@@ -162,47 +162,89 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64", n_terms=6):
     return work
 
 
-def roofline_for(phases, work, lib, steps, name=None):
+def algorithmic_work(n, o, G, W, trial_real=True, n_terms=6):
+    """Algorithmic work per logical call over all walkers: the real-flop
+    counts of the reference's formulas (complex x real multiply-add = 4,
+    complex x complex = 8), whatever precision form executes them -- the
+    three-section bf16 products execute 3x these flops on the tensor cores,
+    the double-float phases ~10 fp32 instructions per flop.  Per walker:
+    V-build 4 G n^2, Taylor + E_half products (8 n_terms + 8) n^2 o, force
+    bias 4 G o n, m = C^H W with its LU cm o^2 n + 16 o^3 (+ 8 n o^2 for
+    G_half), energy cm G o^2 n + 8 G o^2, QR 32 n o^2 - 10.7 o^3.  The
+    exchange finish is counted in bytes (it reads the GEMM's sums)."""
+    cm = 4 if trial_real else 8
+    e_total = (cm * G * o * o * n + 8.0 * G * o * o) * W
+    return {
+        "vbuild_gemm": 4.0 * G * n * n * W,
+        "trotter": (8.0 * n_terms + 8.0) * n * n * o * W,
+        "fb_gemm": cm * G * o * n * W,
+        "green": (cm * o * o * n + 16.0 * o ** 3 + 8.0 * n * o * o) * W,
+        "overlap": (cm * o * o * n + 16.0 * o ** 3) * W,
+        "energy": e_total,
+        "e_gemm": e_total,
+        "qr": (32.0 * n * o * o - 10.7 * o ** 3) * W,
+    }
+
+
+def _peak_for(pipe, lib):
+    peaks = load_peaks() or {}
+    if pipe == "hbm":
+        peak = peaks.get("hbm_gbs")
+        return (peak, "MEASURED_PEAKS.json hbm_gbs") if peak else (6800.0, "fallback (no MEASURED_PEAKS.json)")
+    if pipe == "tensor":
+        peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
+        if peak:
+            return peak, "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)"
+        return 1700.0, "fallback (no MEASURED_PEAKS.json)"
+    return fma_peak(lib, pipe == "fp64")  # SIMT fp64, or fp32 for the fp32 and double-float phases
+
+
+def roofline_for(phases, work, lib, steps, name=None, alg=None):
     """Roofline object of phase `name`, or of the phase with the largest
     device time (composite phases that enclose timed sub-phases are not
-    candidates).  work[] is per logical call over all walkers; phases that
-    launch once per walker chunk make several launches per call, so achieved
-    = work x calls per block / device time per block."""
+    candidates).  work[] is (executed work, pipe) per logical call over all
+    walkers, alg[] the algorithmic work of the same call (algorithmic_work);
+    phases that launch once per walker chunk make several launches per
+    call, so achieved = algorithmic work x calls per block / device time per
+    block.  For the split-operand tensor phases the executed rate and
+    fraction are reported beside it.  The double-float phases (overlap,
+    Green's function, QR of the mixed forms) are measured against the fp32
+    SIMT pipe they run on."""
     leaf = {k: v for k, v in phases.items() if not (k == "energy" and "e_gemm" in phases)}
-    cand = {k: v for k, v in leaf.items() if k in work and work[k][1] != "df32"}
+    cand = {k: v for k, v in leaf.items() if k in work}
     if not cand:
         return None
     dname = name or max(cand.items(), key=lambda kv: kv[1][1])[0]
-    if dname not in work or dname not in phases or work[dname][1] == "df32":
+    if dname not in work or dname not in phases:
         return None
     dcalls, dms = phases[dname]
-    flops, pipe = work[dname]
+    executed, pipe = work[dname]
+    algo = (alg or {}).get(dname, executed)
     chunked = {"vbuild_gemm": STEPS_PER_BLOCK, "trotter": STEPS_PER_BLOCK, "e_gemm": 1, "e_exchange": 1,
                "e_green_rows": 1, "energy": 1}
-    flops *= chunked.get(dname, dcalls / steps)
+    mult = chunked.get(dname, dcalls / steps)
     ms_block = dms / steps
     common = {"kernel": dname, "traffic": None, "avg_launch_ms": round(dms / dcalls, 4),
               "launches_per_step": round(dcalls / steps, 2),
               "share_of_step": round(dms / sum(v[1] for v in leaf.values()), 4)}
-    peaks = load_peaks() or {}
+    ppipe = "fp32" if pipe == "df32" else pipe
+    peak, src = _peak_for(ppipe, lib)
     if pipe == "hbm":
-        achieved = flops / (ms_block / 1000.0) / 1e9
-        peak = peaks.get("hbm_gbs")
-        src = "MEASURED_PEAKS.json hbm_gbs" if peak else None
-        if not peak:
-            peak, src = 6800.0, "fallback (no MEASURED_PEAKS.json)"
+        achieved = algo * mult / (ms_block / 1000.0) / 1e9
         return {**common, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": src}
-    achieved = flops / (ms_block / 1000.0) / 1e12
-    if pipe == "tensor":
-        peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
-        src = "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)" if peak else None
-        if not peak:
-            peak, src = 1700.0, "fallback (no MEASURED_PEAKS.json)"
-    else:
-        peak, src = fma_peak(lib, pipe == "fp64")
-    return {**common, "bound": pipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
-            "frac": round(achieved / peak, 4) if peak else None, "peak_source": src}
+                "frac": round(achieved / peak, 4), "peak_source": src, "work": "algorithmic bytes"}
+    achieved = algo * mult / (ms_block / 1000.0) / 1e12
+    out = {**common, "bound": ppipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
+           "frac": round(achieved / peak, 4) if peak else None, "peak_source": src,
+           "work": "algorithmic flops (the reference's formulas, FP64-counted)"}
+    if pipe == "df32":
+        out["executed"] = "double-float (fp32 pairs) arithmetic on the fp32 pipe, ~10 instructions per flop"
+    elif executed != algo:
+        ex = executed * mult / (ms_block / 1000.0) / 1e12
+        out.update(executed_achieved=round(ex, 4), executed_frac=round(ex / peak, 4) if peak else None,
+                   executed="bf16 split-operand products the tensor cores execute (%.2fx the algorithmic flops)"
+                            % (executed / algo))
+    return out
 
 
 # ------------------------------------------------------------ our engine ---
@@ -292,7 +334,8 @@ def run_ours(args, rank, world):
 
     # dominant kernel and its roofline
     work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=args.precision)
-    roof = roofline_for(phases, work, lib, args.steps)
+    alg = algorithmic_work(n, o, G, W, trial_real=prob.trial_is_real)
+    roof = roofline_for(phases, work, lib, args.steps, alg=alg)
     leaf = {k: v for k, v in phases.items() if not (k == "energy" and "e_gemm" in phases)}
     top = max(leaf.items(), key=lambda kv: kv[1][1])[0]
     dominant = {"phase": top, "share_of_step": round(leaf[top][1] / sum(v[1] for v in leaf.values()), 4),
@@ -311,16 +354,17 @@ def run_ours(args, rank, world):
                 # V hi + mid of every walker read once (2 planes x n^2 x 2 pieces x 2 bytes), walkers read
                 # and written in binary64 (16 n o bytes each way)
                 roof["traffic_algorithmic"] = int(W * (8 * n * n + 32 * n * o))
-    tc = {k: roofline_for(phases, work, lib, args.steps, name=k) for k in phases
-          if k in work and work[k][1] in ("tensor", "hbm")}
+    tc = {k: roofline_for(phases, work, lib, args.steps, name=k, alg=alg) for k in phases
+          if k in work and k != roof["kernel"]} if roof else {}
     for k, r in tc.items():
         t = MEASURED_TRAFFIC.get((args.workload, args.precision, W, k))
         if r is not None and t is not None:
             r["traffic"] = t
 
-    compare = None
+    compare = oracle_cmp = None
     if args.precision in SPLIT_SECTIONS and not args.no_fp64:
         compare = compare_with_fp64(env, st, W)
+        oracle_cmp = compare_with_oracle(wl, args.precision, st)
 
     e2e = None
     if not args.no_e2e:
@@ -339,8 +383,13 @@ def run_ours(args, rank, world):
                       "precision": args.precision, "parallelism": f"replicas{world}",
                       "step": "one block: 10 propagation steps, QR after step 5, QR + energy + comb at the end",
                       "l2": "inputs larger than L2 (walkers %d MB, V %d MB per step)"
-                            % (W * n * o * 16 >> 20, W * n * n * 16 >> 20)},
-           "roofline": roof, "dominant_phase": dominant, "tensor_kernels": tc,
+                            % (W * n * o * 16 >> 20, W * n * n * 16 >> 20),
+                      "synthetic": {"seed": wl.seed, "chol_scale": env["H"]["scale"], "chol_decay": env["H"]["decay"],
+                                    "rule": "h1 = diag(linspace(-2, 0.5)) + sym(N(0, 0.1)) off-diagonal; "
+                                            "L_g = sym(N(0, 1)) * chol_scale * exp(-g / chol_decay), "
+                                            "chol_scale = 0.3 * 12 / norb, chol_decay = nchol / 4; trial = "
+                                            "lowest nocc eigenvectors of h1"}},
+           "roofline": roof, "dominant_phase": dominant, "other_kernels": tc,
            "phases_ms": {k: round(v[1] / args.steps, 3) for k, v in phases.items()},
            "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
     if cvline:
@@ -352,6 +401,8 @@ def run_ours(args, rank, world):
     if compare:
         out["plain_fp64"] = compare
         out["ratio_vs_plain_fp64"] = round(value / compare["value"], 2)
+    if oracle_cmp:
+        out["vs_fp64_oracle"] = oracle_cmp
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     return out
@@ -524,11 +575,12 @@ def run_cv(args, env, st, W, world, seed, ctr):
             "measured": "noise: 16 estimates of one block-end state's energy (zero-step blocks, different samples)"}
 
 
-def compare_with_fp64(env, st_mixed, W):
+def compare_with_fp64(env, st_mixed, W, timed_blocks=3):
     """The metric's denominator and accuracy check, on the same workload:
     one block of the plain binary64 form and one of the mixed form from the
-    same state with the same fields and comb uniform.  Returns the FP64
-    walker-steps/s and |E_mixed - E_fp64| of that block."""
+    same state with the same fields and comb uniform (|E_mixed - E_fp64|);
+    the binary64 block also warms its form up, then `timed_blocks` more
+    binary64 blocks are timed for the walker-steps/s."""
     import dataclasses
 
     import torch
@@ -543,18 +595,60 @@ def compare_with_fp64(env, st_mixed, W):
         return engine.DeviceState(*[t.clone() for t in (s.walkers, s.weights, s.overlaps, s.pop_shift,
                                                           s.e_estimate)])
     a, b = clone(st_mixed), clone(st_mixed)
+    ea, _ = engine.block(prob64, kw["params"], a, 77, 0, zeta=0.5)
+    eb, _ = engine.block(env["prob"], env["params"], b, 77, 0, zeta=0.5)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    ea, _ = engine.block(prob64, kw["params"], a, 77, 0, zeta=0.5)
+    for k in range(timed_blocks):
+        engine.block(prob64, kw["params"], a, 77, (k + 1) * (STEPS_PER_BLOCK + 1))
     e1.record()
-    eb, _ = engine.block(env["prob"], env["params"], b, 77, 0, zeta=0.5)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = e0.elapsed_time(e1) / timed_blocks
     return {"value": round(W * STEPS_PER_BLOCK / (ms / 1000.0), 3), "unit": UNIT, "ms_per_step": round(ms, 1),
-            "measured": "one block of the binary64 form on the same workload (no warm-up of its own)",
+            "measured": "binary64 blocks on the same workload: one untimed (the accuracy block), then %d timed"
+                        % timed_blocks,
             "energy_error_per_block_ha": float(abs(float(ea) - float(eb))),
             "energy_fp64_ha": float(ea), "energy_mixed_ha": float(eb)}
+
+
+def compare_with_oracle(wl, precision, st, n_sub=16, seed=5):
+    """|dE| of the chosen form against the FP64 oracle itself: the first
+    n_sub walkers of the benchmark's state (off the trial after the warm-up
+    and timed blocks) with their weights, overlaps and shifts, one block of
+    the engine in the chosen form and one of the oracle (oracle/afqmc_oracle.py)
+    on the same fields and comb uniform; the binary64 engine beside it."""
+    import dataclasses
+
+    import torch
+    from oracle import afqmc_oracle as O
+    from ad_afqmc_prototype_gb300 import engine
+    sub = make_engine_state(wl, n_sub, precision)
+    H = sub["H"]
+    walkers = st.walkers[:n_sub].clone()
+    weights = st.weights[:n_sub].clone()
+    overlaps = st.overlaps[:n_sub].clone()
+    shift, e_est = float(st.pop_shift.reshape(-1)[0]), float(st.e_estimate.reshape(-1)[0])
+    rng = np.random.default_rng(seed)
+    fields = rng.standard_normal((STEPS_PER_BLOCK, n_sub, wl.nchol))
+    zeta = float(rng.random())
+    prob = O.make_problem(H["h0"], H["h1"], H["chol"], H["mo_coeff"], 0.005)
+    P = O.Params(dt=0.005, n_prop_steps=STEPS_PER_BLOCK, qr_every=QR_EVERY)
+    ost = O.State(walkers=walkers.cpu().numpy(), weights=weights.cpu().numpy(), overlaps=overlaps.cpu().numpy(),
+                  pop_control_ene_shift=shift, e_estimate=e_est)
+    ost, oobs, _ = O.afqmc_block(prob, P, ost, fields, zeta)
+    out = {"walkers": n_sub, "energy_oracle_ha": oobs["energy"]}
+    for form in (precision, "fp64"):
+        env = sub if form == precision else make_engine_state(wl, n_sub, "fp64")
+        dev = lambda t: t.to(device="cuda", copy=True)  # noqa: E731
+        ds = engine.DeviceState(dev(walkers), dev(weights), dev(overlaps),
+                                torch.tensor([shift], dtype=torch.float64, device="cuda"),
+                                torch.tensor([e_est], dtype=torch.float64, device="cuda"))
+        e, _ = engine.block(env["prob"], env["params"], ds, 0, 0, fields=fields, zeta=zeta)
+        out["energy_error_ha" if form == precision else "fp64_engine_error_ha"] = abs(float(e) - oobs["energy"])
+    out["measured"] = ("one block (10 steps, QR after step 5) of %d walkers of the benchmark state, engine vs the "
+                       "NumPy FP64 oracle on the same fields" % n_sub)
+    return out
 
 
 _FMA_PEAK = {}
