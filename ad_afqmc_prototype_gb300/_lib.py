@@ -72,6 +72,7 @@ _SIGS = {
     "afq_build_prop_ctx_workspace": (c_size_t, [c_int32, c_int32]),
     "afq_build_prop_ctx": (c_int32, [c_int32, c_int32, c_double, c_double, P, P, P, c_int32, P, P, P,
                                      P, c_size_t, P]),
+    "afq_trial_rdm1": (c_int32, [c_int32, c_int32, P, P, P]),
     "afq_build_meas_ctx": (c_int32, [c_int32, c_int32, c_int32, P, P, P, c_int32, P, P, P]),
     "afq_lowp_bytes": (c_size_t, [POINTER(afq_dims)]),
     "afq_prepare_lowp": (c_int32, [POINTER(afq_dims), P, P, P, c_size_t, P]),
@@ -138,6 +139,7 @@ _SIGS = {
     "afq_mlp_param_count": (c_size_t, [c_int32, c_int32]),
     "afq_mlp_forward": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P]),
     "afq_mlp_train_workspace": (c_size_t, [c_int32, c_int32, c_int32]),
+    "afq_mlp_gradient": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P, P, P, c_size_t, P]),
     "afq_mlp_train_step": (c_int32, [c_int32, c_int32, c_int32, P, P, P, P, P, P, ctypes.c_float, c_int32, P,
                                      c_size_t, P, P]),
     "afq_mlp_sync": (c_int32, [c_int32, c_int32, P, P, P]),

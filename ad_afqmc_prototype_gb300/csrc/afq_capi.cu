@@ -546,6 +546,12 @@ int afq_build_prop_ctx(int32_t norb, int32_t nchol, double h0, double dt, const 
     return AFQ_OK;
 }
 
+int afq_trial_rdm1(int32_t norb, int32_t nocc, const double* mo_coeff, double* rdm1, void* stream) {
+    if (norb < 1 || nocc < 1 || nocc > norb) return fail(AFQ_E_INVALID_ARGUMENT, "norb=%d nocc=%d", norb, nocc);
+    AFQ_NOTNULL(mo_coeff); AFQ_NOTNULL(rdm1);
+    return launch_trial_rdm1(norb, nocc, (const double2*)mo_coeff, (double2*)rdm1, as_stream(stream));
+}
+
 int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* h1, const double* chol,
                        const double* mo_coeff, int32_t trial_is_real, double* rot_h1, double* rot_chol,
                        void* stream) {
@@ -881,8 +887,8 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
         if (cvmode == AFQ_CV_ESTIMATE) {
             AFQ_NOTNULL(cv->net); AFQ_NOTNULL(cv->feat_shift); AFQ_NOTNULL(cv->feat_scale);
             if (cv->n_sample < 1) return fail(AFQ_E_INVALID_ARGUMENT, "cv n_sample=%d < 1", cv->n_sample);
-            if (cv->hidden < 32 || cv->hidden > 1024 || cv->hidden % 32)
-                return fail(AFQ_E_INVALID_ARGUMENT, "cv hidden=%d (multiple of 32, <= 1024)", cv->hidden);
+            if (!mlp_shape_supported(AFQ_CV_FEATURES, cv->hidden))
+                return fail(AFQ_E_INVALID_ARGUMENT, "cv hidden=%d (multiple of 32, <= 256)", cv->hidden);
         }
     }
     Arena a(workspace, workspace_bytes);
@@ -949,7 +955,7 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
         } else {
             { AFQ_PHASE("cv_network", s);
               AFQ_TRY(launch_mlp_forward(W, AFQ_CV_FEATURES, cv->hidden, (const __nv_bfloat16*)cv->net, ws.cv_feat,
-                                         ws.cv_y, nullptr, s)); }
+                                         ws.cv_y, s)); }
             const int stride = cv->n_sample >= W ? 1 : W / cv->n_sample;
             const int m_max = (W + stride - 1) / stride;
             // the sample's offset: its own Philox stream (seed offset by a constant), this block's counter
@@ -1150,7 +1156,7 @@ int afq_run_blocks(const afq_problem* pb, const afq_params* p, const afq_state* 
 
 // ---------------------------------------------------------------- network
 size_t afq_mlp_param_count(int32_t n_features, int32_t hidden) {
-    if (n_features < 1 || hidden < 32 || hidden > 1024 || hidden % 32) return 0;
+    if (!mlp_shape_supported(n_features, hidden)) return 0;
     return mlp_param_count(n_features, hidden);
 }
 
@@ -1158,32 +1164,43 @@ int afq_mlp_forward(int32_t batch, int32_t n_features, int32_t hidden, const voi
                     float* y, void* stream) {
     if (!afq_mlp_param_count(n_features, hidden)) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: F=%d H=%d", n_features, hidden);
     if (batch < 0) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: batch %d < 0", batch);
-    if ((size_t)32 * (n_features + hidden) * sizeof(float) > 200 * 1024)
-        return fail(AFQ_E_UNSUPPORTED, "mlp: F + H = %d too large", n_features + hidden);
     AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(x); AFQ_NOTNULL(y);
-    return launch_mlp_forward(batch, n_features, hidden, (const __nv_bfloat16*)params_bf16, x, y, nullptr,
-                              as_stream(stream));
+    return launch_mlp_forward(batch, n_features, hidden, (const __nv_bfloat16*)params_bf16, x, y, as_stream(stream));
 }
 
 size_t afq_mlp_train_workspace(int32_t batch, int32_t n_features, int32_t hidden) {
-    const size_t P = afq_mlp_param_count(n_features, hidden);
-    if (!P || batch < 1) return 0;
-    return ((size_t)6 * batch * hidden + batch + P + 1) * sizeof(float);
+    if (!afq_mlp_param_count(n_features, hidden) || batch < 1) return 0;
+    return mlp_train_ws_floats(batch, n_features, hidden) * sizeof(float);
+}
+
+static int mlp_train_args(int32_t batch, int32_t n_features, int32_t hidden, const float* x, const float* target,
+                          size_t workspace_bytes) {
+    const size_t need = afq_mlp_train_workspace(batch, n_features, hidden);
+    if (!need) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: batch=%d F=%d H=%d", batch, n_features, hidden);
+    if (workspace_bytes < need) return fail(AFQ_E_WORKSPACE, "mlp workspace %zu < %zu bytes", workspace_bytes, need);
+    AFQ_NOTNULL(x); AFQ_NOTNULL(target);
+    return AFQ_OK;
+}
+
+int afq_mlp_gradient(int32_t batch, int32_t n_features, int32_t hidden, const void* params_bf16, const float* x,
+                     const float* target, float* grad, float* loss_out, void* workspace, size_t workspace_bytes,
+                     void* stream) {
+    AFQ_TRY(mlp_train_args(batch, n_features, hidden, x, target, workspace_bytes));
+    AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(grad); AFQ_NOTNULL(workspace);
+    return launch_mlp_grad_adam(batch, n_features, hidden, (const __nv_bfloat16*)params_bf16, x, target,
+                                (float*)workspace, grad, loss_out, nullptr, nullptr, nullptr, nullptr, 0.f, 1,
+                                as_stream(stream));
 }
 
 int afq_mlp_train_step(int32_t batch, int32_t n_features, int32_t hidden, float* master, void* params_bf16,
                        float* adam_m, float* adam_v, const float* x, const float* target, float lr, int32_t step,
                        void* workspace, size_t workspace_bytes, float* loss_out, void* stream) {
-    const size_t need = afq_mlp_train_workspace(batch, n_features, hidden);
-    if (!need) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: batch=%d F=%d H=%d", batch, n_features, hidden);
-    if (workspace_bytes < need) return fail(AFQ_E_WORKSPACE, "mlp workspace %zu < %zu bytes", workspace_bytes, need);
+    AFQ_TRY(mlp_train_args(batch, n_features, hidden, x, target, workspace_bytes));
+    AFQ_NOTNULL(master); AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(adam_m); AFQ_NOTNULL(adam_v); AFQ_NOTNULL(workspace);
     if (step < 1) return fail(AFQ_E_INVALID_ARGUMENT, "mlp: step %d < 1", step);
-    if ((size_t)32 * (n_features + hidden) * sizeof(float) > 200 * 1024)
-        return fail(AFQ_E_UNSUPPORTED, "mlp: F + H = %d too large", n_features + hidden);
-    AFQ_NOTNULL(master); AFQ_NOTNULL(params_bf16); AFQ_NOTNULL(adam_m); AFQ_NOTNULL(adam_v);
-    AFQ_NOTNULL(x); AFQ_NOTNULL(target); AFQ_NOTNULL(workspace);
-    return launch_mlp_train_step(batch, n_features, hidden, master, (__nv_bfloat16*)params_bf16, adam_m, adam_v, x,
-                                 target, lr, step, (float*)workspace, loss_out, as_stream(stream));
+    return launch_mlp_grad_adam(batch, n_features, hidden, (const __nv_bfloat16*)params_bf16, x, target,
+                                (float*)workspace, nullptr, loss_out, master, (__nv_bfloat16*)params_bf16, adam_m,
+                                adam_v, lr, step, as_stream(stream));
 }
 
 int afq_mlp_sync(int32_t n_features, int32_t hidden, const float* master, void* params_bf16, void* stream) {

@@ -254,6 +254,7 @@ int launch_h1_eff(int n, int G, const double* h1, const double* chol, const doub
                   double* h1_eff, cudaStream_t s);
 int launch_expm(int n, double scale, const double* a, double* out, double* tmp0, double* tmp1,
                 double* tmp2, double* norm_dev, cudaStream_t s);
+int launch_trial_rdm1(int n, int o, const double2* mo, double2* rdm1, cudaStream_t s);
 int launch_rot(int n, int o, int G, const double* h1, const double* chol, const double2* mo,
                int trial_real, double2* rot_h1, void* rot_chol, cudaStream_t s);
 int launch_h0_prop(int G, double h0, const double2* mf, double2* h0_prop, cudaStream_t s);
@@ -364,10 +365,12 @@ int launch_cv_measure(int W, double dt, double alpha, const double* weights, con
                       const double2* partial, const double* e_est, double* pop_shift, double* block_energy,
                       double* block_weight, double2* energy, double* stats, cudaStream_t s);
 size_t mlp_param_count(int F, int H);
-int launch_mlp_forward(int B, int F, int H, const __nv_bfloat16* p, const float* x, float* y, float* act,
-                       cudaStream_t s);
-int launch_mlp_train_step(int B, int F, int H, float* w, __nv_bfloat16* wb, float* m, float* v, const float* x,
-                          const float* t, float lr, int step, float* ws, float* loss_out, cudaStream_t s);
+bool mlp_shape_supported(int F, int H);  // F a multiple of 16, H a multiple of 32 in [32, 256]
+int launch_mlp_forward(int B, int F, int H, const __nv_bfloat16* p, const float* x, float* y, cudaStream_t s);
+size_t mlp_train_ws_floats(int B, int F, int H);
+int launch_mlp_grad_adam(int B, int F, int H, const __nv_bfloat16* wb_in, const float* x, const float* t, float* ws,
+                         float* g_out, float* loss_out, float* w, __nv_bfloat16* wb, float* m, float* v, float lr,
+                         int step, cudaStream_t s);
 int launch_mlp_sync_bf16(size_t n, const float* w, __nv_bfloat16* wb, cudaStream_t s);
 // k_trotter_tc.cu
 bool trotter_tc_supported(int n, int o);

@@ -18,6 +18,31 @@ int launch_sum_spin_blocks(int n, const double2* rdm1, double2* dm, cudaStream_t
     return AFQ_OK;
 }
 
+// get_rdm1 (trial/rhf.py:29-32): dm = C C^H (n x n), written twice, as the
+// (2, n, n) spin-block stack [dm, dm].  One thread an entry.
+__global__ void k_trial_rdm1(int n, int o, const double2* __restrict__ mo, double2* __restrict__ rdm1) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * n) return;
+    const int i = e / n, j = e % n;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int a = 0; a < o; ++a) {
+        const double2 x = mo[i * o + a], y = mo[j * o + a];  // x conj(y)
+        acc.x = fma(x.x, y.x, acc.x);
+        acc.x = fma(x.y, y.y, acc.x);
+        acc.y = fma(x.y, y.x, acc.y);
+        acc.y = fma(-x.x, y.y, acc.y);
+    }
+    rdm1[e] = acc;
+    rdm1[n * n + e] = acc;
+}
+
+int launch_trial_rdm1(int n, int o, const double2* mo, double2* rdm1, cudaStream_t s) {
+    const int nn = n * n;
+    k_trial_rdm1<<<(nn + 255) / 256, 256, 0, s>>>(n, o, mo, rdm1);
+    AFQ_LAUNCHED("k_trial_rdm1");
+    return AFQ_OK;
+}
+
 // mf_g = i * sum_ij L_g[i,j] dm[j,i]   (prop/chol_afqmc_ops.py:59-63)
 __global__ void __launch_bounds__(256) k_mf_shifts(int n, const double* __restrict__ chol,
                                                    const double2* __restrict__ dm,

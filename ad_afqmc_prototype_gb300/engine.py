@@ -117,6 +117,15 @@ def build_prop_ctx(h0: float, h1: torch.Tensor, chol: torch.Tensor, rdm1: torch.
     return e, mf, h0p
 
 
+def trial_rdm1(mo: torch.Tensor) -> torch.Tensor:
+    """(2, n, n) complex128 [C C^H, C C^H] of the trial orbitals (n, o)."""
+    mo = as_device(mo, C128)
+    n, o = mo.shape
+    out = torch.empty((2, n, n), dtype=C128, device=mo.device)
+    _lib.call("afq_trial_rdm1", int(n), int(o), ptr(mo), ptr(out), stream_ptr())
+    return out
+
+
 def build_meas_ctx(h1: torch.Tensor, chol: torch.Tensor, mo: torch.Tensor, trial_is_real: bool):
     """meas/rhf.py:141-150.  Returns (rot_h1 (o,n) c128, rot_chol (G,o,n))."""
     n, o, G = h1.shape[0], mo.shape[1], chol.shape[0]
@@ -699,7 +708,7 @@ def grad_backward(prob: Problem, params, h1: torch.Tensor, n_blocks: int, seed: 
 def mlp_param_count(n_features: int, hidden: int) -> int:
     n = int(_lib.load().afq_mlp_param_count(int(n_features), int(hidden)))
     if n == 0:
-        raise ValueError(f"network shape F={n_features} H={hidden} (H a multiple of 32, <= 1024)")
+        raise ValueError(f"network shape F={n_features} H={hidden} (F a multiple of 16, H a multiple of 32, <= 256)")
     return n
 
 
@@ -716,15 +725,32 @@ def mlp_sync(master: torch.Tensor, params_bf16: torch.Tensor, n_features: int, h
     _lib.call("afq_mlp_sync", int(n_features), int(hidden), ptr(master), ptr(params_bf16), stream_ptr())
 
 
-def mlp_train_step(master, params_bf16, m, v, x, target, lr: float, step: int, hidden: int, ws=None):
-    """One Adam step on a batch; returns (device loss (1,), workspace tensor)."""
+def mlp_gradient(params_bf16, x, target, hidden: int, ws=None):
+    """(gradient (P,) fp32, loss (1,), workspace) of mean (y - t)^2 / 2 at the bf16 parameters."""
     x = x.to(torch.float32).contiguous()
     target = target.to(torch.float32).contiguous()
     B, F = x.shape
     need = int(_lib.load().afq_mlp_train_workspace(int(B), int(F), int(hidden)))
     if ws is None or ws.numel() * 4 < need:
         ws = torch.empty((need + 3) // 4, dtype=torch.float32, device=x.device)
+    g = torch.empty((mlp_param_count(F, hidden),), dtype=torch.float32, device=x.device)
     loss = torch.empty((1,), dtype=torch.float32, device=x.device)
+    _lib.call("afq_mlp_gradient", int(B), int(F), int(hidden), ptr(params_bf16), ptr(x), ptr(target), ptr(g),
+              ptr(loss), ptr(ws), ws.numel() * 4, stream_ptr())
+    return g, loss, ws
+
+
+def mlp_train_step(master, params_bf16, m, v, x, target, lr: float, step: int, hidden: int, ws=None,
+                   loss_out=None):
+    """One Adam step on a batch; returns (device loss (1,), workspace tensor).
+    loss_out: a device float32 slot for the loss (default: a new tensor)."""
+    x = x.to(torch.float32).contiguous()
+    target = target.to(torch.float32).contiguous()
+    B, F = x.shape
+    need = int(_lib.load().afq_mlp_train_workspace(int(B), int(F), int(hidden)))
+    if ws is None or ws.numel() * 4 < need:
+        ws = torch.empty((need + 3) // 4, dtype=torch.float32, device=x.device)
+    loss = torch.empty((1,), dtype=torch.float32, device=x.device) if loss_out is None else loss_out
     _lib.call("afq_mlp_train_step", int(B), int(F), int(hidden), ptr(master), ptr(params_bf16), ptr(m), ptr(v),
               ptr(x), ptr(target), float(lr), int(step), ptr(ws), ws.numel() * 4, ptr(loss), stream_ptr())
     return loss, ws

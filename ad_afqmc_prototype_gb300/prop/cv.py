@@ -2,8 +2,8 @@
 
 An engine form beside the reference's exact measurement (prop/blocks.py:59-79,
 meas/rhf.py:36-50); it has no counterpart in the reference.  A small network
-(64 -> H -> H -> 1, GELU, bf16 weights, fp32 arithmetic; the engine's own
-forward, backward and Adam kernels) predicts each walker's exchange energy
+(64 -> H -> H -> 1, GELU, bf16 weights; the engine's own tensor-core
+forward, gradient and Adam kernels) predicts each walker's exchange energy
 X_w = sum_g tr(f_g f_g) from cheap per-walker features (Coulomb-vector block
 norms, the Coulomb and one-body terms, log|overlap|; `afq_cv` in the C
 header lists them).  It is trained on exact exchange values the engine
@@ -43,8 +43,8 @@ class ExchangeControlVariate:
     correction) or "off" (the plain exact measurement)."""
 
     def __init__(self, hidden: int = 256, sample_fraction: float = 0.125, seed: int = 0, device=None):
-        if hidden % 32 or not 32 <= hidden <= 1024:
-            raise ValueError("hidden must be a multiple of 32 in [32, 1024]")
+        if hidden % 32 or not 32 <= hidden <= 256:
+            raise ValueError("hidden must be a multiple of 32 in [32, 256]")
         if not 0.0 < sample_fraction <= 1.0:
             raise ValueError("sample_fraction must be in (0, 1]")
         self.hidden = int(hidden)
@@ -143,19 +143,19 @@ class ExchangeControlVariate:
         n = Xs.shape[0]
         g = torch.Generator(device=self.device).manual_seed(int(seed))
         ws = None
-        losses = []
-        for _ in range(int(epochs)):
+        nb = max(1, n // batch) if n >= batch else 1
+        bsz = batch if n >= batch else n
+        # one device slot per step for the batch losses: the loop issues kernels only
+        lbuf = torch.zeros((int(epochs), nb), dtype=torch.float32, device=self.device)
+        for ep in range(int(epochs)):
             perm = torch.randperm(n, generator=g, device=self.device)
-            tot = torch.zeros((), dtype=torch.float64, device=self.device)
-            nb = 0
-            for b0 in range(0, n - batch + 1 if n >= batch else 1, batch):
-                idx = perm[b0:b0 + batch]
+            Xp, Yp = Xs[perm].contiguous(), Ys[perm].contiguous()  # one gather an epoch; batches are slices
+            for k in range(nb):
                 self.adam_step += 1
-                loss, ws = engine.mlp_train_step(self.master, self.params, self.adam_m, self.adam_v, Xs[idx],
-                                                 Ys[idx], lr, self.adam_step, self.hidden, ws)
-                tot += loss.double()[0]
-                nb += 1
-            losses.append(float(tot) / max(nb, 1))
+                _, ws = engine.mlp_train_step(self.master, self.params, self.adam_m, self.adam_v,
+                                              Xp[k * bsz:(k + 1) * bsz], Yp[k * bsz:(k + 1) * bsz], lr,
+                                              self.adam_step, self.hidden, ws, loss_out=lbuf[ep, k:k + 1])
+        losses = lbuf.double().mean(1).tolist()
         self.loss_history.extend(losses)
         return losses
 

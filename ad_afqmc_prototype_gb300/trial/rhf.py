@@ -36,10 +36,8 @@ class rhf_trial:
 
 
 def get_rdm1(trial_data: rhf_trial) -> torch.Tensor:
-    """Stacked [C C^H, C C^H] (trial/rhf.py:29-32)."""
-    c = trial_data.mo_coeff
-    dm = c @ c.conj().T
-    return torch.stack([dm, dm], dim=0)
+    """Stacked [C C^H, C C^H] (trial/rhf.py:29-32), formed by the engine's kernel."""
+    return engine.trial_rdm1(trial_data.mo_coeff)
 
 
 def _overlap_batched(walkers, trial_data: rhf_trial):

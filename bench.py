@@ -396,6 +396,8 @@ def run_ours(args, rank, world):
         out["control_variate"] = cvline
     if rank == 0 and not args.no_grad:
         out["differentiation"] = run_grad(n_blocks=args.grad_blocks)
+        # the 200-orbital benchmark Hamiltonian: 256 walkers, 4 blocks (40 steps), binary64
+        out["differentiation_c4"] = run_grad("c4_n200_o30_g1000_w4096", n_blocks=4, n_walkers=256)
     if rank == 0 and not args.no_large and args.workload != "c5_n400_o50_g2000_w1024":
         out["large_workload"] = run_large(args.precision)
     if compare:
@@ -408,12 +410,13 @@ def run_ours(args, rank, world):
     return out
 
 
-def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20, eps=1e-4):
-    """The differentiated energy on the 60-orbital workload: E = sum_b W_b e_b
-    / sum_b W_b over 20 blocks (200 steps, QR every 5, checkpoints every 20
-    steps) with h1 + lam D at lam = 0; dE/dlam by the adjoint kernels against
-    central differences at lam = +-eps on the same fields, the comb held at
-    the unperturbed run's indices (and, for information, left free)."""
+def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20, eps=1e-4, n_walkers=None):
+    """The differentiated energy: E = sum_b W_b e_b / sum_b W_b over n_blocks
+    blocks (QR every 5 steps, checkpoints every 20 steps) with h1 + lam D at
+    lam = 0; dE/dlam by the adjoint kernels against central differences at
+    lam = +-eps on the same fields, the comb held at the unperturbed run's
+    indices (and, for information, left free).  Default: the 60-orbital
+    workload, 20 blocks (200 steps); n_walkers overrides its walker count."""
     import torch
     from ad_afqmc_prototype_gb300 import synth
     from ad_afqmc_prototype_gb300.core.system import system
@@ -424,6 +427,8 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
     from ad_afqmc_prototype_gb300.prop.types import afqmc_params
     from ad_afqmc_prototype_gb300.trial.rhf import make_rhf_trial_ops, rhf_trial
     wl = synth.WORKLOADS[workload]
+    if n_walkers:
+        wl = dataclasses.replace(wl, n_walkers=int(n_walkers))
     H = synth.make_workload(wl)
     sys_ = system(norb=wl.nbasis, nelec=(wl.nocc, wl.nocc), walker_kind="restricted")
     ham = ham_chol(h0=H["h0"], h1=H["h1"], chol=H["chol"])
@@ -469,7 +474,7 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
 
     fd, _ = central(idx)
     free, moved = central(None)
-    return {"workload": workload, "n_blocks": n_blocks, "steps": n_blocks * STEPS_PER_BLOCK,
+    return {"workload": workload, "n_walkers": wl.n_walkers, "n_blocks": n_blocks, "steps": n_blocks * STEPS_PER_BLOCK,
             "checkpoint_every_steps": checkpoint_every, "precision": "fp64",
             "energy": round(e_val, 10), "dE_dlambda_adjoint": adj, "dE_dlambda_fd_fixed_comb": fd,
             "rel_diff": abs(adj - fd) / abs(fd), "fd_eps": eps,
@@ -504,21 +509,33 @@ def run_large(precision, workload="c5_n400_o50_g2000_w1024", blocks=2):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / blocks
     value = W * STEPS_PER_BLOCK / (ms / 1000.0)
-    cmp = compare_with_fp64(env, st, W)
+    cmp = compare_with_fp64(env, st, W, timed_blocks=1)
     return {"workload": workload, "precision": precision, "value": round(value, 3), "unit": UNIT,
             "ms_per_step": round(ms, 2), "plain_fp64": cmp, "ratio_vs_plain_fp64": round(value / cmp["value"], 2),
             "note": "norb 400 > 256: the Taylor series runs on the fp32 SIMT kernel; the QRs in global memory"}
 
 
-def run_cv(args, env, st, W, world, seed, ctr):
-    """The mixed + control-variate form: five recorded blocks (50 steps) train
-    the exchange network with the engine's kernels (not timed), then
-    args.steps blocks are timed with exact exchange on 1/8 of the walkers.
-    Its noise against the exact measurement of the same state, and against
-    the same sample without the network, from zero-step blocks."""
+def run_cv(args, env, st, W, world, seed, ctr, chain_blocks=40, run_steps=400):
+    """The mixed + control-variate form against the exact measurement.
+
+    Five recorded blocks (the first 50 steps) train the exchange network
+    with the engine's kernels (timed).  Then two chains of `chain_blocks`
+    blocks run from the same state on the same random stream: the exact
+    measurement, and the control variate with exact exchange on 1/8 of the
+    walkers.  Each chain's block energies give the standard error of its
+    mean (blocking analysis, stat_utils.blocking_analysis_ratio), and
+
+      efficiency = (se_exact^2 t_exact) / (se_cv^2 t_cv)
+
+    per block, with the training time spread over a `run_steps`-step run
+    (the learned-control-variate workload's 400 steps): > 1 means the control
+    variate reaches a given error bar sooner.  The noise the sampling adds to
+    one block's estimate is also measured on a fixed state (zero-step
+    blocks, different samples)."""
     import torch
     from ad_afqmc_prototype_gb300 import engine
     from ad_afqmc_prototype_gb300.prop.cv import ExchangeControlVariate
+    from ad_afqmc_prototype_gb300.stat_utils import blocking_analysis_ratio
 
     prob, params = env["prob"], env["params"]
     cv = ExchangeControlVariate(hidden=256, sample_fraction=1 / 8, seed=seed)
@@ -527,33 +544,49 @@ def run_cv(args, env, st, W, world, seed, ctr):
         engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
         cv.after_block()
         ctr += STEPS_PER_BLOCK + 1
+    torch.cuda.synchronize()
     t0 = time.time()
     losses = cv.fit(epochs=20, batch=1024, lr=1e-3)
     torch.cuda.synchronize()
     fit_s = time.time() - t0
-    cv.mode = "estimate"
-    for _ in range(args.warmup):
-        engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
-        cv.after_block()
-        ctr += STEPS_PER_BLOCK + 1
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
-        cv.after_block()
-        ctr += STEPS_PER_BLOCK + 1
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-
-    # noise of one block's estimate on a fixed state (zero-step blocks)
-    z = dataclasses.replace(params, n_prop_steps=0)
+    n_steps_fit = cv.adam_step
 
     def clone():
         return engine.DeviceState(*[t.clone() for t in (st.walkers, st.weights, st.overlaps, st.pop_shift,
                                                           st.e_estimate)])
+    stream = torch.cuda.current_stream()
+
+    def chain(use_cv):
+        s0 = clone()
+        cv.mode = "estimate" if use_cv else "off"
+        engine.block(prob, params, clone(), seed, ctr, cv=cv.block_args(W))  # warm-up on a copy
+        cv.after_block()
+        es, ws = [], []
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c = ctr
+        for _ in range(chain_blocks):
+            e, w = engine.block(prob, params, s0, seed, c, cv=cv.block_args(W))
+            cv.after_block()
+            es.append(e)
+            ws.append(w)
+            c += STEPS_PER_BLOCK + 1
+        e1.record(stream)
+        torch.cuda.synchronize()
+        E = torch.cat(es).double().cpu().numpy()
+        Wt = torch.cat(ws).double().cpu().numpy()
+        r = blocking_analysis_ratio(E, Wt, print_q=False)
+        return e0.elapsed_time(e1) / chain_blocks, float(r["mu"]), float(r["se_star"]), E
+
+    ms_x, mu_x, se_x, _ = chain(False)
+    ms_cv, mu_cv, se_cv, _ = chain(True)
+    fit_ms_per_block = 1000.0 * fit_s / (run_steps / STEPS_PER_BLOCK)
+    eff = (se_x ** 2 * ms_x) / (se_cv ** 2 * (ms_cv + fit_ms_per_block)) if se_cv > 0 else None
+
+    # noise of one block's estimate on a fixed state (zero-step blocks)
+    cv.mode = "estimate"
+    z = dataclasses.replace(params, n_prop_steps=0)
     exact = float(engine.block(prob, z, clone(), seed, 0, zeta=0.5)[0])
 
     def draws(shift, scale, k=16):
@@ -565,14 +598,21 @@ def run_cv(args, env, st, W, world, seed, ctr):
             cv.after_block()
         return np.array(out)
     net, alone = draws(cv.y_shift, cv.y_scale), draws(0.0, 0.0)
-    return {"value": round(world * W * STEPS_PER_BLOCK / (ms / 1000.0), 3), "unit": UNIT, "ms_per_step": round(ms, 3),
-            "exact_exchange_fraction": 1 / 8, "network": "64-256-256-1 GELU, bf16 weights, fp32 arithmetic",
-            "training": {"blocks": 5, "samples": 5 * W, "epochs": 20, "seconds": round(fit_s, 2),
+    return {"value": round(world * W * STEPS_PER_BLOCK / (ms_cv / 1000.0), 3), "unit": UNIT,
+            "ms_per_step": round(ms_cv, 3), "exact_exchange_fraction": 1 / 8,
+            "network": "64-256-256-1 GELU, bf16 weights, mma.sync bf16 products (two-piece activations)",
+            "training": {"blocks": 5, "samples": 5 * W, "epochs": 20, "adam_steps": n_steps_fit,
+                         "seconds": round(fit_s, 3), "ms_per_adam_step": round(1000.0 * fit_s / max(n_steps_fit, 1), 3),
                          "loss_first": round(losses[0], 5), "loss_last": round(losses[-1], 5)},
+            "chains": {"blocks": chain_blocks, "exact_ms_per_block": round(ms_x, 3),
+                       "cv_ms_per_block": round(ms_cv, 3), "training_ms_per_block": round(fit_ms_per_block, 3),
+                       "exact_mean_ha": mu_x, "exact_se_ha": se_x, "cv_mean_ha": mu_cv, "cv_se_ha": se_cv},
+            "efficiency_vs_exact": round(eff, 4) if eff is not None else None,
             "noise_std_ha": float(net.std(ddof=1)), "noise_std_sample_alone_ha": float(alone.std(ddof=1)),
             "variance_ratio": float(net.var(ddof=1) / max(alone.var(ddof=1), 1e-300)),
             "mean_minus_exact_ha": float(net.mean() - exact),
-            "measured": "noise: 16 estimates of one block-end state's energy (zero-step blocks, different samples)"}
+            "measured": "chains: %d blocks each from one state on the same random stream; noise: 16 estimates of "
+                        "one block-end state's energy (zero-step blocks, different samples)" % chain_blocks}
 
 
 def compare_with_fp64(env, st_mixed, W, timed_blocks=3):

@@ -116,6 +116,10 @@ int afq_build_prop_ctx(int32_t norb, int32_t nchol, double h0, double dt,
                        double* h0_prop, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* get_rdm1, trial/rhf.py:29-32: rdm1 (2, n, n) c128 = [C C^H, C C^H] of the
+ * trial orbitals mo_coeff (n, o) c128. */
+int afq_trial_rdm1(int32_t norb, int32_t nocc, const double* mo_coeff, double* rdm1, void* stream);
+
 /* build_meas_ctx, meas/rhf.py:141-150.  rot_h1 (o,n) c128; rot_chol (G,o,n)
  * f64 when trial_is_real else c128. */
 int afq_build_meas_ctx(int32_t norb, int32_t nocc, int32_t nchol, const double* h1,
@@ -353,7 +357,7 @@ int afq_run_blocks(const afq_problem* pb, const afq_params* p, const afq_state* 
 
 typedef struct afq_cv {
     int32_t mode;            /* AFQ_CV_* */
-    int32_t hidden;          /* network width (multiple of 32, <= 1024) */
+    int32_t hidden;          /* network width (multiple of 32, <= 256) */
     int32_t n_sample;        /* ESTIMATE: walkers with exact exchange per block (>= 1) */
     int32_t pad_;
     const void* net;         /* ESTIMATE: bf16 parameters, afq_mlp_param_count entries */
@@ -372,18 +376,29 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
                  double* block_energy, double* block_weight, int32_t* sr_idx, const afq_cv* cv,
                  void* workspace, size_t workspace_bytes, void* stream);
 
-/* The network: F -> H -> H -> 1, GELU, bf16 weights, fp32 arithmetic.
- * Parameters (bf16 copy and fp32 master, same layout): W1 (H x F), b1 (H),
- * W2 (H x H), b2 (H), w3 (H), b3 (1). */
+/* The network: F -> H -> H -> 1, GELU, bf16 weights.  Every product runs on
+ * the tensor cores (mma.sync bf16, fp32 accumulation) with the fp32 operands
+ * (inputs, activations, their gradients) as two bf16 pieces, so the sums are
+ * fp32-accurate.  F a multiple of 16, H a multiple of 32 in [32, 256]
+ * (afq_mlp_param_count returns 0 otherwise).  Parameters (bf16 copy and fp32
+ * master, same layout): W1 (H x F), b1 (H), W2 (H x H), b2 (H), w3 (H), b3 (1). */
 size_t afq_mlp_param_count(int32_t n_features, int32_t hidden);
 /* y (B,) = network(x (B, F) fp32), all device. */
 int afq_mlp_forward(int32_t batch, int32_t n_features, int32_t hidden, const void* params_bf16,
                     const float* x, float* y, void* stream);
-/* One Adam step (beta 0.9 / 0.999, bias-corrected by `step` >= 1) on the
- * loss mean (y - target)^2 / 2 of a batch: updates master, its bf16 copy and
- * the moments m, v.  loss_out (optional, device) receives the batch loss
- * before the update.  workspace: afq_mlp_train_workspace bytes. */
+/* Gradient of the loss mean (y - target)^2 / 2 over a batch with respect to
+ * every parameter (fp32, P entries, device) at the bf16 parameters; the
+ * batch's rows are split over CTAs of 32 whose partial gradients are added in
+ * a fixed order (the same inputs give the same bits).  loss_out (optional,
+ * device) receives the loss.  workspace: afq_mlp_train_workspace bytes. */
 size_t afq_mlp_train_workspace(int32_t batch, int32_t n_features, int32_t hidden);
+int afq_mlp_gradient(int32_t batch, int32_t n_features, int32_t hidden, const void* params_bf16,
+                     const float* x, const float* target, float* grad, float* loss_out, void* workspace,
+                     size_t workspace_bytes, void* stream);
+/* One Adam step (beta 0.9 / 0.999, bias-corrected by `step` >= 1) with that
+ * gradient: updates master, its bf16 copy and the moments m, v (two kernel
+ * launches).  loss_out (optional, device) receives the batch loss before the
+ * update. */
 int afq_mlp_train_step(int32_t batch, int32_t n_features, int32_t hidden, float* master, void* params_bf16,
                        float* adam_m, float* adam_v, const float* x, const float* target, float lr,
                        int32_t step, void* workspace, size_t workspace_bytes, float* loss_out,

@@ -2,9 +2,9 @@
 Adam kernels against the host restatement (oracle/mlp_oracle.py), and the
 control-variate block measurement against the exact one.
 
-Tolerances: forward 1e-4 relative (fp32 sums of bf16-weight products against
-float64 sums of the same weights); gradients 2e-3 relative in norm (fp32
-atomics and sums); Adam to fp32 rounding of the weights; the control-variate energy is
+Tolerances: forward 1e-4 relative (tensor-core sums of bf16 weights times
+two-piece bf16 activations, against float64 sums of the same weights);
+gradients 2e-3 relative in norm; Adam to fp32 rounding of the weights; the control-variate energy is
 unbiased, so with every walker sampled it equals the exact energy up to the
 Coulomb term's source (force-bias GEMM instead of energy GEMM, 1e-5 Ha), and
 over random samples its mean is within 4 standard errors of the exact one."""
@@ -43,21 +43,25 @@ def test_mlp_gradient_and_adam_match_oracle(cuda):
     from ad_afqmc_prototype_gb300 import engine
     cv = _params(2)
     rng = np.random.default_rng(1)
-    B = 96
+    B = 96  # three CTA tiles of 32 rows
     x = rng.normal(size=(B, F)).astype(np.float32)
     t = rng.normal(size=B).astype(np.float32)
     p0 = cv.master.double().cpu().numpy()
     pb = _bf16_host(cv.master)
-    loss, ws = engine.mlp_train_step(cv.master, cv.params, cv.adam_m, cv.adam_v,
-                                     torch.tensor(x, device="cuda"), torch.tensor(t, device="cuda"), 1e-3, 1, H)
-    torch.cuda.synchronize()
-    P = p0.size
-    g_gpu = ws[6 * B * H + B: 6 * B * H + B + P].double().cpu().numpy()
+    xd, td = torch.tensor(x, device="cuda"), torch.tensor(t, device="cuda")
+    g, gloss, _ = engine.mlp_gradient(cv.params, xd, td, H)
+    g2, _, _ = engine.mlp_gradient(cv.params, xd, td, H)
+    assert torch.equal(g, g2)  # the tiles' partial gradients are added in a fixed order
+    g_gpu = g.double().cpu().numpy()
     ref_loss, g_ref = O.loss_and_grad(pb, x.astype(np.float64), t.astype(np.float64), H)
-    assert abs(float(loss.item()) - ref_loss) <= 1e-4 * abs(ref_loss)
+    assert abs(float(gloss.item()) - ref_loss) <= 1e-4 * abs(ref_loss)
     rel = np.linalg.norm(g_gpu - g_ref) / np.linalg.norm(g_ref)
     assert rel < 2e-3, rel
+    loss, ws = engine.mlp_train_step(cv.master, cv.params, cv.adam_m, cv.adam_v, xd, td, 1e-3, 1, H)
+    torch.cuda.synchronize()
+    assert float(loss.item()) == float(gloss.item())
     # the Adam step applied to the GPU's own gradient
+    P = p0.size
     p1, _, _ = O.adam(p0, g_gpu, np.zeros(P), np.zeros(P), 1e-3, 1)
     got = cv.master.double().cpu().numpy()
     # fp32 master weights: a few ulp of the weight, plus fp32 error in the step of size lr

@@ -211,3 +211,13 @@ def test_field_shift_and_weight_update_match_oracle(E):
     assert np.sum(cpu(dst.weights) == 0) == np.sum(rw == 0)
     assert abs(float(cpu(dst.pop_shift)[0]) - rpop) < 1e-10
     np.testing.assert_array_equal(cpu(dst.overlaps), ov_new)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_trial_rdm1_matches_oracle(E, cplx):
+    """get_rdm1 (trial/rhf.py:29-32) by the engine's kernel: [C C^H, C C^H]."""
+    rng = np.random.default_rng(21)
+    n, o = 37, 9
+    c = rng.normal(size=(n, o)) + (1j * rng.normal(size=(n, o)) if cplx else 0)
+    out = cpu(E.trial_rdm1(dev(c, E.C128)))
+    np.testing.assert_allclose(out, O.get_rdm1(c), rtol=0, atol=1e-13)
