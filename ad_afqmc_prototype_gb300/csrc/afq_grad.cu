@@ -159,7 +159,12 @@ int check_grad(const afq_problem* pb, const afq_params* p, int n_blocks, int ck)
     const afq_dims* d = &pb->dims;
     if (d->precision != AFQ_PREC_FP64) return fail(AFQ_E_UNSUPPORTED, "the gradient runs the binary64 form");
     if (!d->trial_is_real) return fail(AFQ_E_UNSUPPORTED, "the gradient supports real trial orbitals");
-    if (d->nocc > 32) return fail(AFQ_E_UNSUPPORTED, "the gradient supports nocc <= 32 (nocc=%d)", d->nocc);
+    // per-walker adjoint algebra in shared memory: the Taylor adjoint holds two n x o complex
+    // blocks, the overlap and QR adjoints four o x o blocks and 32 staged rows
+    const size_t no = (size_t)d->norb * d->nocc, oo = (size_t)d->nocc * d->nocc;
+    if (2 * no * sizeof(double2) > 227 * 1024 || (4 * oo + 32 * (size_t)d->nocc) * sizeof(double2) > 227 * 1024)
+        return fail(AFQ_E_UNSUPPORTED, "the gradient needs 32 norb nocc <= 227 KiB and 64 nocc^2 + 512 nocc <= "
+                    "227 KiB (norb %d, nocc %d)", d->norb, d->nocc);
     if (n_blocks < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_blocks=%d < 1", n_blocks);
     if (ck < 1) return fail(AFQ_E_INVALID_ARGUMENT, "checkpoint_blocks=%d < 1", ck);
     if (p->n_prop_steps < 1) return fail(AFQ_E_INVALID_ARGUMENT, "n_prop_steps=%d < 1", p->n_prop_steps);

@@ -75,6 +75,8 @@ int launch_taylor_tape(int W, int n, int o, int K, double sqrt_dt, const double*
                        const double2* win, double2* terms, double2* w2, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     const size_t smem = 2 * sizeof(double2) * (size_t)n * o;
+    if (smem > 227 * 1024)
+        return fail(AFQ_E_UNSUPPORTED, "Taylor adjoint: norb %d x nocc %d needs %zu bytes of shared memory", n, o, smem);
     AFQ_TRY(allow_smem(k_taylor_tape, smem));
     k_taylor_tape<<<W, 256, smem, s>>>(n, o, K, sqrt_dt, E, V, win, terms, w2);
     AFQ_LAUNCHED("k_taylor_tape");
@@ -138,6 +140,8 @@ int launch_taylor_adj(int W, int n, int o, int K, double sqrt_dt, const double* 
                       const double2* wbar_post, double2* tbar, double2* wbar_pre, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
     const size_t smem = 2 * sizeof(double2) * (size_t)n * o;
+    if (smem > 227 * 1024)
+        return fail(AFQ_E_UNSUPPORTED, "Taylor adjoint: norb %d x nocc %d needs %zu bytes of shared memory", n, o, smem);
     AFQ_TRY(allow_smem(k_taylor_adj, smem));
     k_taylor_adj<<<W, 256, smem, s>>>(n, o, K, sqrt_dt, E, V, wbar_post, tbar, wbar_pre);
     AFQ_LAUNCHED("k_taylor_adj");
@@ -406,8 +410,8 @@ __global__ void __launch_bounds__(256) k_green_adj(int n, int o, const double2* 
 int launch_green_adj(int W, int n, int o, const double2* mo, const double2* walkers, const double2* gbar,
                      const double2* ov, const double2* ovbar, double2* wbar, int* err, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
-    if (o > 32) return fail(AFQ_E_UNSUPPORTED, "green adjoint: nocc=%d > 32", o);
     const size_t smem = sizeof(double2) * ((size_t)4 * o * o + (size_t)RT * o);
+    if (smem > 227 * 1024) return fail(AFQ_E_UNSUPPORTED, "green adjoint: nocc=%d needs %zu bytes of shared memory", o, smem);
     AFQ_TRY(allow_smem(k_green_adj, smem));
     k_green_adj<<<W, 256, smem, s>>>(n, o, mo, walkers, gbar, ov, ovbar, wbar, err);
     AFQ_LAUNCHED("k_green_adj");
@@ -471,8 +475,8 @@ __global__ void __launch_bounds__(256) k_qr_adj(int n, int o, const double2* __r
 int launch_qr_adj(int W, int n, int o, const double2* A, const double2* Q, const double2* qbar, double2* abar,
                   int* err, cudaStream_t s) {
     if (W <= 0) return AFQ_OK;
-    if (o > 32) return fail(AFQ_E_UNSUPPORTED, "QR adjoint: nocc=%d > 32", o);
     const size_t smem = sizeof(double2) * ((size_t)4 * o * o + (size_t)RT * o);
+    if (smem > 227 * 1024) return fail(AFQ_E_UNSUPPORTED, "QR adjoint: nocc=%d needs %zu bytes of shared memory", o, smem);
     AFQ_TRY(allow_smem(k_qr_adj, smem));
     k_qr_adj<<<W, 256, smem, s>>>(n, o, A, Q, qbar, abar, err);
     AFQ_LAUNCHED("k_qr_adj");

@@ -256,15 +256,17 @@ struct ExchOut {
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
 // exchange contraction of each 32 x 32 block (ExchOut) instead of C.
 //
-// Each CTA loads its own A and B tiles with plain TMA copies; the tile order
-// (M tiles fastest) makes the CTAs resident at one time work on one or two N
-// tiles, so a B tile is read from DRAM about once and served from L2 to the
-// CTAs that share it.
+// Each CTA loads its own A and B tiles with plain TMA copies.  Tile order:
+// with M tiles fastest (nfast = 0) the CTAs resident at one time work on one
+// or two N tiles, so a B tile is read from DRAM about once and served from L2
+// to the CTAs that share it, while A is re-read from L2 once per N tile; the
+// launcher picks N tiles fastest (nfast = 1) when A is the large operand and
+// B fits in L2.
 template <int BNT, int MODE, int EWN>
 __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
-                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo) {
+                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo, int nfast) {
     using D = Drain<BNT, EWN>;
     static_assert(MODE != 2 || EWN == 8, "the exchange epilogue's transpose buffers are sized for eight warps");
     constexpr bool SPLIT = MODE == 1;
@@ -320,13 +322,14 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             for (int s = 0; s < STG; ++s) issued[s] = 0;
             bool ok = true;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-                const int mb = t % mt, nb = t / mt;
+                const int mb = nfast ? t / nt : t % mt, nb = nfast ? t % nt : t / mt;
                 for (int kb = 0; kb < kt; ++kb) {
                     if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
                     mbar_expect_tx(full0 + 8 * stage, D::STAGE);
-                    tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, full0 + 8 * stage);
-                    tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, full0 + 8 * stage);
+                    const uint32_t fb = full0 + 8 * stage;
+                    tma_load_2d(smem_u32(sA + stage * A_BYTES), &tmA, kb * BK, mb * BM, fb);
+                    tma_load_2d(smem_u32(sB + stage * D::B_BYTES), &tmB, kb * BK, nb * BNT, fb);
                     issued[stage] = 1;
                     issued_par[stage] = phase;
                     if (++stage == STG) { stage = 0; phase ^= 1; }
@@ -382,7 +385,7 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
                                : (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
         for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-            const int mb = t % mt, nb = t / mt;
+            const int mb = nfast ? t / nt : t % mt, nb = nfast ? t % nt : t / mt;
             float2 acc[CW / 2];
 #pragma unroll
             for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
@@ -476,8 +479,9 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
                             ph[u] = *(const uint32_t*)&h;
                             pm[u] = *(const uint32_t*)&m;
                         }
-                        *(uint4*)(dh + 2 * j) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
-                        *(uint4*)(dm + 2 * j) = make_uint4(pm[0], pm[1], pm[2], pm[3]);
+                        // streaming stores: the output is read once, by another kernel
+                        __stcs((uint4*)(dh + 2 * j), make_uint4(ph[0], ph[1], ph[2], ph[3]));
+                        __stcs((uint4*)(dm + 2 * j), make_uint4(pm[0], pm[1], pm[2], pm[3]));
                     }
                 } else {
 #pragma unroll
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
                 if (vec && col0 + CW <= N) {
 #pragma unroll
                     for (int j = 0; j < CW / 2; j += 2)
-                        *(float4*)(dst + 2 * j) = make_float4(acc[j].x, acc[j].y, acc[j + 1].x, acc[j + 1].y);
+                        __stcs((float4*)(dst + 2 * j), make_float4(acc[j].x, acc[j].y, acc[j + 1].x, acc[j + 1].y));
                 } else {
 #pragma unroll
                     for (int j = 0; j < CW / 2; ++j) {
@@ -556,7 +560,14 @@ static int launch_drain(int M, int N, int K, const void* A, long long lda, const
     AFQ_TRY(raise_smem_once(smem_once, kern, SMEM));
     const long long tiles = (long long)((M + BM - 1) / BM) * ((N + BNT - 1) / BNT);
     const int grid = (int)(tiles < sms ? tiles : sms);
-    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo);
+    // tile order: the operand re-read once per tile of the other should fit in
+    // L2 beside the streams; if A does not and B does, N tiles run fastest (the
+    // force-bias and energy GEMMs: full-size DRAM reads within 1.1x of the
+    // operands' bytes)
+    constexpr long long kL2Keep = 48LL << 20;
+    const long long a_bytes = (long long)M * K * 2, b_bytes = (long long)N * K * 2;
+    const int nfast = (a_bytes > kL2Keep && b_bytes <= kL2Keep) ? 1 : 0;
+    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo, nfast);
     AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }

@@ -487,31 +487,82 @@ def run_grad(workload="c3_n60_o10_g300_w1024", n_blocks=20, checkpoint_every=20,
 
 def run_large(precision, workload="c5_n400_o50_g2000_w1024", blocks=2):
     """The 400-orbital workload (nocc 50, nchol 2000, 1024 walkers) in the
-    chosen form: one warm-up and `blocks` timed blocks, then one block of the
-    binary64 form from the same state and fields for the ratio and |dE|."""
+    chosen form: one warm-up and `blocks` timed blocks with per-phase device
+    times and each phase's roofline (algorithmic work), the device memory the
+    run holds, the control-variate form timed on the same state (network
+    trained on 3 recorded blocks), then one block of the binary64 form from
+    the same state and fields for the ratio and |dE|."""
+    import ctypes
+
     import torch
-    from ad_afqmc_prototype_gb300 import engine, synth
+    from ad_afqmc_prototype_gb300 import _lib, engine, synth
     from ad_afqmc_prototype_gb300.prop.afqmc import device_state
+    from ad_afqmc_prototype_gb300.prop.cv import ExchangeControlVariate
     wl = synth.WORKLOADS[workload]
-    W = wl.n_walkers
+    W, n, o, G = wl.n_walkers, wl.nbasis, wl.nocc, wl.nchol
     env = make_engine_state(wl, W, precision)
     st = device_state(env["state"], inplace=True)
+    prob, params = env["prob"], env["params"]
+    lib = _lib.load()
     ctr = 0
-    engine.block(env["prob"], env["params"], st, 11, ctr)
+    engine.block(prob, params, st, 11, ctr)
     ctr += STEPS_PER_BLOCK + 1
     torch.cuda.synchronize()
+    lib.afq_timing_reset()
+    lib.afq_timing_enable(1)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(blocks):
-        engine.block(env["prob"], env["params"], st, 11, ctr)
+        engine.block(prob, params, st, 11, ctr)
         ctr += STEPS_PER_BLOCK + 1
     e1.record()
     torch.cuda.synchronize()
+    lib.afq_timing_enable(0)
+    phases = _lib.timing_report()
     ms = e0.elapsed_time(e1) / blocks
     value = W * STEPS_PER_BLOCK / (ms / 1000.0)
+    work = phase_work(n, o, G, W, trial_real=prob.trial_is_real, precision=precision)
+    alg = algorithmic_work(n, o, G, W, trial_real=prob.trial_is_real)
+    roofs = {k: roofline_for(phases, work, lib, blocks, name=k, alg=alg) for k in phases if k in work}
+    d = engine.make_dims(W, n, o, G, True, prob.precision)
+    mib = 1 << 20
+    footprint = {"chol_f64_mib": round(G * n * n * 8 / mib, 1),
+                 "rot_chol_f64_mib": round(G * o * n * 8 / mib, 1),
+                 "lowp_split_operands_mib": round(int(lib.afq_lowp_bytes(ctypes.byref(d))) / mib, 1),
+                 "walkers_c128_mib": round(W * n * o * 16 / mib, 1),
+                 "block_workspace_mib": round(int(lib.afq_block_workspace(ctypes.byref(d), int(params.n_chunks))) / mib, 1),
+                 "torch_peak_allocated_mib": round(torch.cuda.max_memory_allocated() / mib, 1)}
+    # control variate: 3 recorded blocks train the network, then timed estimate blocks
+    cv = ExchangeControlVariate(hidden=256, sample_fraction=1 / 8, seed=5)
+    cv.mode = "record"
+    for _ in range(3):
+        engine.block(prob, params, st, 11, ctr, cv=cv.block_args(W))
+        cv.after_block()
+        ctr += STEPS_PER_BLOCK + 1
+    cv.fit(epochs=20, batch=1024, lr=1e-3)
+    cv.mode = "estimate"
+    engine.block(prob, params, st, 11, ctr, cv=cv.block_args(W))
+    cv.after_block()
+    ctr += STEPS_PER_BLOCK + 1
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(blocks):
+        engine.block(prob, params, st, 11, ctr, cv=cv.block_args(W))
+        cv.after_block()
+        ctr += STEPS_PER_BLOCK + 1
+    e1.record()
+    torch.cuda.synchronize()
+    ms_cv = e0.elapsed_time(e1) / blocks
     cmp = compare_with_fp64(env, st, W, timed_blocks=1)
     return {"workload": workload, "precision": precision, "value": round(value, 3), "unit": UNIT,
-            "ms_per_step": round(ms, 2), "plain_fp64": cmp, "ratio_vs_plain_fp64": round(value / cmp["value"], 2),
+            "ms_per_step": round(ms, 2), "phases_ms": {k: round(v[1] / blocks, 3) for k, v in phases.items()},
+            "kernels": {k: {kk: r[kk] for kk in ("achieved", "frac", "bound", "unit", "executed_frac")
+                            if kk in r} for k, r in roofs.items() if r},
+            "hbm_footprint": footprint,
+            "control_variate": {"value": round(W * STEPS_PER_BLOCK / (ms_cv / 1000.0), 3), "unit": UNIT,
+                                "ms_per_step": round(ms_cv, 2), "exact_exchange_fraction": 1 / 8,
+                                "training_blocks": 3},
+            "plain_fp64": cmp, "ratio_vs_plain_fp64": round(value / cmp["value"], 2),
             "note": "norb 400 > 256: the Taylor series runs on the fp32 SIMT kernel; the QRs in global memory"}
 
 

@@ -418,7 +418,9 @@ int afq_mlp_sync(int32_t n_features, int32_t hidden, const float* master, void* 
  * (prop/blocks.py:59-66) are held at their values; the initial state is a
  * constant.  Fields and comb uniforms come from the Philox stream (seed,
  * counter + b (n_prop_steps + 1) + step) as in afq_run_blocks.  Binary64
- * form, real trial orbitals, nocc <= 32.
+ * form, real trial orbitals; the per-walker adjoint algebra sits in shared
+ * memory: 32 norb nocc and 64 nocc^2 + 512 nocc bytes must each fit in
+ * 227 KiB (nocc up to 52; norb nocc up to 7264, e.g. 200 x 36).
  *
  * afq_grad_forward runs the blocks like afq_block (state updated in place;
  * block b's energy and weight to block_energies[b], block_weights[b], its

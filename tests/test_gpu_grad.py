@@ -139,6 +139,17 @@ def test_derivative_matches_fixed_comb_fd(cuda, loss):
     assert engine.workspace_status() == 0
 
 
+def test_derivative_past_32_occupied_orbitals(cuda):
+    """nocc 36 (the per-walker adjoint algebra past one warp's width): the
+    adjoint against fixed-comb central differences."""
+    c = _case(48, 36, 60, 32, steps=4, qr_every=2, dt=0.005)
+    B, seed = 2, 5
+    g, e, w, run = _grad(c, B, seed, 8)
+    adj = float((g * c["D"]).sum())
+    fd, _ = _fd(c, B, seed, 1e-5, run.sr_idx)
+    assert abs(adj - fd) <= 1e-5 * abs(fd) + 1e-10, (adj, fd)
+
+
 def test_checkpoint_interval_does_not_change_the_gradient(cuda):
     c = _case(12, 4, 24, 64, steps=4, qr_every=2)
     gs = [_grad(c, 5, 3, ck)[0] for ck in (4, 8, 20, 400)]
