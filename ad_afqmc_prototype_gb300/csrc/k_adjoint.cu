@@ -17,7 +17,7 @@ namespace afq {
 namespace {
 template <class K>
 int allow_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
+    if (bytes > 32 * 1024)  // with the kernel's static shared memory the default limit is below 48 KB
         AFQ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return AFQ_OK;
 }

@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(512) k_trotter_mixed(int n, int o, int n_terms
 template <class K>
 static int smem_attr(K kernel, size_t bytes) {
     if (bytes > 227 * 1024) return fail(AFQ_E_UNSUPPORTED, "mixed kernel needs %zu bytes of shared memory", bytes);
-    if (bytes > 48 * 1024)
+    if (bytes > 32 * 1024)  // with the kernel's static shared memory the default limit is below 48 KB
         AFQ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return AFQ_OK;
 }

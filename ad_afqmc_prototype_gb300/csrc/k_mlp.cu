@@ -399,7 +399,7 @@ int launch_mlp_forward(int B, int F, int H, const __nv_bfloat16* p, const float*
     if (B <= 0) return AFQ_OK;
     if (!mlp_shape_supported(F, H)) return fail(AFQ_E_UNSUPPORTED, "mlp: F=%d H=%d", F, H);
     const size_t smem = mlp_smem_bytes(F, H);
-    if (smem > 48 * 1024)
+    if (smem > 32 * 1024)  // with the kernel's static shared memory the default limit is below 48 KB
         AFQ_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_mlp_forward<<<(B + MLP_TR - 1) / MLP_TR, MLP_THREADS, smem, s>>>(B, F, H, p, x, y);
     AFQ_LAUNCHED("k_mlp_forward");
@@ -423,7 +423,7 @@ int launch_mlp_grad_adam(int B, int F, int H, const __nv_bfloat16* wb_in, const 
     float* part = ws;
     float* lpart = ws + (size_t)nt * off.total;
     const size_t smem = mlp_smem_bytes(F, H);
-    if (smem > 48 * 1024)
+    if (smem > 32 * 1024)  // with the kernel's static shared memory the default limit is below 48 KB
         AFQ_CUDA(cudaFuncSetAttribute(k_mlp_grad_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_mlp_grad_tile<<<nt, MLP_THREADS, smem, s>>>(B, F, H, wb_in, x, t, part, lpart);
     AFQ_LAUNCHED("k_mlp_grad_tile");

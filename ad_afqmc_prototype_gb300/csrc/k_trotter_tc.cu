@@ -4,180 +4,250 @@
 //   W' = out + (E - I) out
 // with E = exp(-dt h1 / 2) and V = sum_g x_g L_g of the walker.
 //
-// Each complex product is one real GEMM per 128-row tile of the walker:
-//   [Yr | Yi] = [Vr | Vi] . B,   B = [[Tr, Ti], [-Ti, Tr]]   (K = 2n)
-// on tcgen05.mma kind::f16 (M = 128, K = 16).  Operands are two-piece bf16
-// splits, x = hi + mid, and each K step issues A_hi . [B_hi; B_mid] (N = 128,
-// the hi.hi and hi.mid products land in separate accumulator columns and A is
-// read once) and A_mid . B_hi (N = 64, into the hi.mid columns): hi.hi +
-// hi.mid + mid.hi, ~2^-17 relative, the precision of the three-section
-// GEMMs.  Keeping hi.hi in an accumulator of its own bounds the tensor
-// cores' truncating fp32 accumulation to one add per K step of the dominant
-// sum.  The E - I products
-// use A = [(E - I) | 0], i.e. only the top half of B's K range.
+// Each complex product Y = V T (T the current n x o term) is one real GEMM
+// in transposed form, D = A B^T on tcgen05.mma kind::f16 (M = 128, K = 16):
+//   B = V itself, row j over K = [Vr[j, :] | Vi[j, :]] (two K halves of
+//       N = n rounded up to 16 each), streamed by TMA from the V-build's
+//       output; N = the orbital rows j (one MMA covers all of them, N <= 256);
+//   A = the term's embedding, one row per (orbital c, piece p, part q), held
+//       in tensor memory: row (c, p, Re) = piece p of [Tr[:, c] | -Ti[:, c]],
+//       row (c, p, Im) = piece p of [Ti[:, c] | Tr[:, c]], so that
+//       D[(c, p, Re), j] = (V T_p)r[j, c] and D[(c, p, Im), j] = (V T_p)i[j, c].
+// Pieces are two-piece bf16 splits x = hi + mid of both operands; each K step
+// issues A.B_hi and A.B_mid into the same accumulator, so the sum over the
+// two A rows of a (c, q) pair is (T_hi + T_mid)(V_hi + V_mid), ~2^-17
+// relative, the precision of the three-section GEMMs.  The E - I products use
+// B = (E - I) and the top K half only.  Tensor memory (512 columns): the
+// accumulator in columns [0, N), the A operand in [256, 256 + N) (two bf16 a
+// column, K index k in column k / 2, even k in the low half).
 //
-// A (V of the walker, or E - I: hi and mid tiles of 128 rows x 64 K) streams
-// by TMA through a three-stage ring.  B, the current Taylor term, lives in
-// shared memory in the 128-byte-swizzled K-major layout the MMA reads, and is
-// rewritten by the epilogue warps after each product: rows c < o hold
-// [Tr; -Ti] of column c, rows 32 + c hold [Ti; Tr] (so output column c is Yr
-// and 32 + c is Yi), rows 64.. the same for the mid piece.  The top half of
-// B's K range holds rows 0..n-1 at K = i, the bottom half at K = 16 S + i
-// (S = ceil(n / 16) K steps per half), so no K step straddles the two halves.
-// Tensor memory (512 columns): per 128-row tile 128 accumulator columns
-// (hi.hi | hi.mid + mid.hi, summed by the epilogue with a round-to-nearest
-// add), then per tile 64 columns of the running walker update and 64 of the
-// fp32 copy of the walker's rows.
+// With the term as the tensor-memory operand the MMA reads only B from
+// shared memory, and N = n per instruction instead of the 2 o columns of a
+// term-as-B layout: a 128 x 208 x 16 MMA issues in the time of a 128 x 64 x 16
+// one from shared memory.
 //
-// The walker update W' - W = (E - I) W + sum_k T_k + (E - I) out is summed in
-// fp32 by the epilogue thread that owns the row (in tensor memory, next to
-// an fp32 copy of the row for the operand sums), and added to the binary64
-// walker once: per entry the binary64 pipe converts W once and the update
-// once and adds once.
+// The running sum U = W + (E - I) W + sum_k T_k (= out after the last V
+// product) is kept in fp32 registers; W' = W + ((U - W32) + (E - I) out) is
+// formed with one binary64 add per entry, W32 being W cut to fp32 by integer
+// operations (the same bits in the first and the last use).  Lane (c, p, q)
+// of the accumulator belongs to the epilogue thread that holds TMEM lane
+// 4c + 2p + q; the four lanes of an orbital c are in one warp and exchange
+// the piece sums and the Re/Im parts by shuffles.  U(j, c, q) is held by
+// lane (c, j & 1, q).  Between two walkers the walker passes through shared
+// memory in its own element order (coalesced loads and stores), in the B
+// ring's memory: the producer starts the next walker's copies only after the
+// epilogue is done with it.
 //
-// Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-9 epilogue
-// (warp w reads lanes 32 (w % 4).. of the accumulator of tile (w - 2) / 4,
-// as tcgen05.ld allows).  Persistent over the chunk's walkers, one walker at
-// a time per CTA.  Every mbarrier wait is bounded; on a timeout the CTA
-// raises *err and unwinds (the producer waits for its copies in flight, the
-// MMA thread for its MMAs, and the tensor memory is freed).
+// Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-17 epilogue
+// (warp w reads lanes 32 (w % 4).. of tensor memory, as tcgen05.ld allows;
+// the four warps of a lane quarter take a quarter of the columns each).
+// Persistent over the chunk's walkers, one walker at a time per CTA.  Every
+// mbarrier wait is bounded; on a timeout the CTA raises *err and unwinds (the
+// producer waits for its copies in flight, the MMA thread for its MMAs, and
+// the tensor memory is freed).
 #include "afq_internal.cuh"
 #include "tc_common.cuh"
 
 namespace afq {
 namespace tc {
 
-constexpr int TT_THREADS = 320;
-constexpr int TT_N = 64;                 // output columns: 32 Yr, 32 Yi (nocc <= 32)
-constexpr int TT_STG = 3;                // A stages
-constexpr int TT_TILE = 128 * 64 * 2;    // one 128 x 64 bf16 tile, 16 KB
-constexpr int TT_STAGE = 2 * TT_TILE;    // hi + mid
-constexpr int TT_BBLK = 2 * TT_N * 128;  // one 64-wide K block of B (hi rows 0-63, mid rows 64-127), 16 KB
-constexpr int TT_MAXKBB = 8;             // B K blocks for norb <= 256
-constexpr int TT_TCOLS = 2 * TT_N;       // accumulator columns per tile: hi.hi | hi.mid + mid.hi
-constexpr int TT_SCOL = 2 * TT_TCOLS;    // running update: tile t at TT_SCOL + t TT_N (Re 32, Im 32)
-constexpr int TT_FCOL = TT_SCOL + 2 * TT_N;  // fp32 copy of the rows, same layout
-constexpr int TT_SMEM = TT_MAXKBB * TT_BBLK + TT_STG * TT_STAGE + 1024 + 256;
-constexpr uint32_t TT_IDESC128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
-                                 ((uint32_t)(128 >> 4) << 24);
-constexpr uint32_t TT_IDESC64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
-                                ((uint32_t)(128 >> 4) << 24);
-static_assert(TT_SMEM <= 227 * 1024, "tensor-core Trotter shared memory");
+constexpr int TT_THREADS = 576;          // 18 warps
+constexpr int TT_EPI = TT_THREADS - 64;  // epilogue threads
+constexpr uint32_t TT_ACOL = 256;        // tensor-memory column of the A operand
+constexpr int TT_SMEM_MAX = 227 * 1024;
+constexpr int TT_MAXCH = 16;             // 4-column chunks of an epilogue thread (N / 16 <= 16)
 
-// B is K-major with the 128-byte swizzle (16-byte chunk index XOR row % 8
-// within each 8-row, 1024-byte atom): element (row r, K index k) sits at byte
-//   (k >> 6) TT_BBLK + (r >> 3) 1024 + (r & 7) 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) + 2 (k & 7)
-// = kb(k) + rb(r) + (kx(k) ^ ((r & 7) << 4)) with the K parts
-// kb(k) = (k >> 6) TT_BBLK + 2 (k & 7), kx(k) = ((k & 63) >> 3) << 4 fixed
-// per thread (its rows k = i and k = kb0 + i) and rb(r) = (r >> 3) 1024 +
-// (r & 7) 128 a constant once the column loops are unrolled.
-struct TTRow {
-    uint32_t kb0, kx0;  // k = i: the top half of B's K range
-    uint32_t kb1, kx1;  // k = kb0 + i: the bottom half
+__host__ __device__ constexpr uint32_t tt_idesc(int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+struct TTGeo {
+    int N;     // n rounded up to 16: the MMA's N, the B tiles' rows, the K extent of each half
+    int S;     // K steps of 16 per half
+    int kbh;   // 64-wide K blocks per half (the last may hold fewer than four steps)
+    int stg;   // B ring stages (hi + mid tiles of N rows x 64 K each)
+    int smem;  // dynamic shared memory
 };
-__device__ __forceinline__ TTRow tt_row(int i, int kbot) {
-    const int k1 = kbot + i;
-    return TTRow{(uint32_t)((i >> 6) * TT_BBLK + ((i & 7) << 1)), (uint32_t)(((i & 63) >> 3) << 4),
-                 (uint32_t)((k1 >> 6) * TT_BBLK + ((k1 & 7) << 1)), (uint32_t)(((k1 & 63) >> 3) << 4)};
-}
-__device__ __forceinline__ void tt_st16(uint8_t* p, uint32_t v) { *(uint16_t*)p = (uint16_t)v; }
 
-// B <- the embedding of T(i, c) = t, c < o, for this thread's row: rows c
-// and 32 + c of the hi piece (64 + ... of the mid piece) get [Tr; -Ti] and
-// [Ti; Tr] over the two K halves.  Re and Im are rounded together; -Ti's
-// pieces are Ti's with the sign bit flipped (round-to-nearest is odd).
-__device__ __forceinline__ void tt_write_b(uint8_t* b, const TTRow& q, int c, float2 t) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(t.x, t.y);
-    const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 m = __floats2bfloat162_rn(t.x - hf.x, t.y - hf.y);
-    const uint32_t hv = *(const uint32_t*)&h, mv = *(const uint32_t*)&m;
-    const uint32_t sw = (uint32_t)((c & 7) << 4);
-    uint8_t* p0 = b + q.kb0 + (q.kx0 ^ sw);
-    uint8_t* p1 = b + q.kb1 + (q.kx1 ^ sw);
-    const int rc = (c >> 3) * 1024 + (c & 7) * 128;  // rb(c); rb(32 + c) = rc + 4096, +8192 for the mid piece
-    tt_st16(p0 + rc, hv);                            // (c, i) = Tr
-    tt_st16(p0 + rc + 8192, mv);
-    tt_st16(p1 + rc, (hv >> 16) ^ 0x8000u);          // (c, kb0 + i) = -Ti
-    tt_st16(p1 + rc + 8192, (mv >> 16) ^ 0x8000u);
-    tt_st16(p0 + rc + 4096, hv >> 16);               // (32 + c, i) = Ti
-    tt_st16(p0 + rc + 4096 + 8192, mv >> 16);
-    tt_st16(p1 + rc + 4096, hv);                     // (32 + c, kb0 + i) = Tr
-    tt_st16(p1 + rc + 4096 + 8192, mv);
+static TTGeo tt_geo(int n, int o) {
+    TTGeo g;
+    g.N = (n + 15) / 16 * 16;
+    g.S = g.N / 16;
+    g.kbh = (g.N + 63) / 64;
+    const int stage = 2 * g.N * 128;
+    g.stg = (TT_SMEM_MAX - 1024 - 256) / stage;
+    if (g.stg > 4) g.stg = 4;
+    // the walker staging (N x nocc x 2 floats) reuses the ring between walkers
+    if ((long long)g.N * 2 * o * 4 > (long long)g.stg * stage) g.stg = 0;
+    g.smem = 1024 + g.stg * stage + 256;
+    return g;
 }
-static_assert(TT_N == 64, "tt_write_b: row offsets of 32 + c (4096) and of the mid piece (8192)");
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-#define TT_R8(i)                                                                                               \
-    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
-        "=r"(r[i + 7])
-// Two 8-column loads (one wait) and stores (then wait for the stores).
-__device__ __forceinline__ void tmem_ld8x2(uint32_t a0, uint32_t a1, uint32_t (&r)[16]) {
+__device__ __forceinline__ void umma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%16];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%17];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
-        : TT_R8(0), TT_R8(8)
-        : "r"(a0), "r"(a1)
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-#undef TT_R8
-// Four 8-column loads, one wait.
-#define TT_R8(i)                                                                                               \
-    "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), "=r"(r[i + 6]), \
-        "=r"(r[i + 7])
-__device__ __forceinline__ void tmem_ld8x4(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t (&r)[32]) {
+__device__ __forceinline__ void tmem_ld4(uint32_t a, uint32_t (&r)[4]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%32];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%33];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%34];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%35];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
-        : TT_R8(0), TT_R8(8), TT_R8(16), TT_R8(24)
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3)
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+        : "r"(a)
         : "memory");
 }
-#undef TT_R8
-__device__ __forceinline__ void tmem_st8x2(uint32_t a0, uint32_t a1, const uint32_t (&v)[16]) {
+__device__ __forceinline__ void tmem_st2(uint32_t a, uint32_t v0, uint32_t v1) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(a), "r"(v0), "r"(v1) : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Piece p of (a, b) as a bf16 pair (a in the low half): p = 0 the
+// round-to-nearest bf16 of each, p = 1 the bf16 of the remainder.
+__device__ __forceinline__ uint32_t tt_piece2(float a, float b, int p) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 m = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    const __nv_bfloat162 x = p ? m : h;
+    return *(const uint32_t*)&x;
+}
+// W entry cut to fp32 (24 significant bits, toward zero) by integer
+// operations only (no binary64 instruction on any path): magnitudes below
+// the fp32 normal range give a signed zero, above it infinity, nan a nan.
+__device__ __forceinline__ float tt_w32(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
+    const unsigned e = (h >> 20) & 0x7ffu, sign = h & 0x80000000u;
+    const unsigned nrm = sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29));
+    const unsigned big = ((e == 0x7ffu) && ((h & 0xfffffu) | l)) ? 0x7fc00000u : (sign | 0x7f800000u);
+    return __uint_as_float(e < 897u ? sign : (e > 1150u ? big : nrm));
+}
+// Exact fp32 -> binary64 by integer operations only (fp32 subnormals give a
+// signed zero; inf and nan keep their class).
+__device__ __forceinline__ double tt_f2d(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    const unsigned long long ex = e == 0u ? 0ull : (e == 0xffu ? 2047ull : (unsigned long long)(e + 896u));
+    const unsigned long long m = e == 0u ? 0ull : (unsigned long long)(u & 0x7fffffu) << 29;
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (ex << 52) | m));
+}
+
+// 16 and 8 consecutive fp32 columns of this warp's lanes; the wait is part
+// of the same statement, so no use of the registers can move above it.
+#define TT_O8(i)                                                                                               \
+    "=r"(v[i]), "=r"(v[i + 1]), "=r"(v[i + 2]), "=r"(v[i + 3]), "=r"(v[i + 4]), "=r"(v[i + 5]), "=r"(v[i + 6]), \
+        "=r"(v[i + 7])
+__device__ __forceinline__ void tmem_ld16_wait(uint32_t a, uint32_t (&v)[16]) {
     asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%2, %3, %4, %5, %6, %7, %8, %9};\n\t"
-        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%1], {%10, %11, %12, %13, %14, %15, %16, %17};\n\t"
-        "tcgen05.wait::st.sync.aligned;" ::"r"(a0),
-        "r"(a1), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
-        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : TT_O8(0), TT_O8(8)
+        : "r"(a)
         : "memory");
+}
+__device__ __forceinline__ void tmem_ld8_wait(uint32_t a, uint32_t (&v)[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : TT_O8(0)
+        : "r"(a)
+        : "memory");
+}
+#undef TT_O8
+
+// Bounded barrier of the epilogue threads (an mbarrier with their count):
+// false on timeout or abort.
+__device__ __forceinline__ bool tt_epi_sync(uint32_t bar, uint32_t& ph, volatile int* abort_flag) {
+    mbar_arrive(bar);
+    const bool ok = mbar_wait_inl(bar, ph, abort_flag);
+    ph ^= 1u;
+    return ok;
+}
+
+// Staging of a walker through U, coalesced, TT_SPT loads of a thread in
+// flight at once (passes of TT_SPT x 512 entries: three at norb 200 x nocc 30).
+constexpr int TT_SPT = 12;
+
+// U <- W32 of a walker in its own element order (j, c, Re/Im); entries
+// ne..nu-1 (rows n..N-1) zero.
+__device__ __forceinline__ void tt_fill_u(float* Us, const double* __restrict__ W, int ne, int nu, int et) {
+    for (int e0 = et; e0 < nu; e0 += TT_SPT * TT_EPI) {
+        double x[TT_SPT];
+#pragma unroll
+        for (int u = 0; u < TT_SPT; ++u) {
+            const int e = e0 + u * TT_EPI;
+            x[u] = e < ne ? W[e] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < TT_SPT; ++u) {
+            const int e = e0 + u * TT_EPI;
+            if (e < ne) Us[e] = tt_w32(x[u]);
+            else if (e < nu) Us[e] = 0.f;
+        }
+    }
+}
+
+// W' = W + (U - W32): the walker's one binary64 add per entry (win and wout
+// may alias: each entry is read and written by one thread).
+__device__ __forceinline__ void tt_final(const double2* win, double2* wout, const float* Us, int ne, int et) {
+    const double* W = (const double*)win;
+    double* Wo = (double*)wout;
+    for (int e0 = et; e0 < ne; e0 += TT_SPT * TT_EPI) {
+        double x[TT_SPT];
+#pragma unroll
+        for (int u = 0; u < TT_SPT; ++u) {
+            const int e = e0 + u * TT_EPI;
+            x[u] = e < ne ? W[e] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < TT_SPT; ++u) {
+            const int e = e0 + u * TT_EPI;
+            if (e < ne) Wo[e] = x[u] + tt_f2d(Us[e] - tt_w32(x[u]));
+        }
+    }
 }
 
 __global__ void __launch_bounds__(TT_THREADS, 1)
     k_trotter_tc(const __grid_constant__ CUtensorMap mVh, const __grid_constant__ CUtensorMap mVm,
                  const __grid_constant__ CUtensorMap mEh, const __grid_constant__ CUtensorMap mEm, int wc, int n,
-                 int o, int n_terms, float sqrt_dt, const double2* win, double2* wout, int* __restrict__ err) {
+                 int o, int n_terms, float sqrt_dt, TTGeo g, const double2* win, double2* wout,
+                 int* __restrict__ err) {
     extern __shared__ uint8_t tt_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)tt_raw + 1023) & ~(uintptr_t)1023);
-    const int S = (n + 15) >> 4;             // K steps per half
-    const int KBB = (2 * S + 3) >> 2;        // B K blocks
-    const int kbh = (n + 63) >> 6;           // A K blocks per half
-    const int MT = (n + 127) >> 7;           // 128-row tiles
-    const int R = n_terms + 2;               // products per walker
-    uint8_t* sB = smem;
-    uint8_t* sA = smem + TT_MAXKBB * TT_BBLK;
-    uint64_t* bars = (uint64_t*)(sA + TT_STG * TT_STAGE);
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TT_STG + 3);
+    const int N = g.N, S = g.S, kbh = g.kbh, STG = g.stg;
+    const uint32_t TILE = (uint32_t)N * 128u, STAGE = 2u * TILE;
+    const int R = n_terms + 2;  // products per walker: E, n_terms V, E
+    const int o2 = 2 * o;
+    uint8_t* ring = smem;
+    // walker staging U[j][c][q] (N x o x 2 floats): the ring's memory, used
+    // between two walkers while no copy is in flight
+    float* Us = (float*)ring;
+    uint64_t* bars = (uint64_t*)(smem + (size_t)STG * STAGE);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STG + 5);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TT_STG);
-    const uint32_t dfull = smem_u32(bars + 2 * TT_STG), bready = smem_u32(bars + 2 * TT_STG + 1);
-    const uint32_t drain = smem_u32(bars + 2 * TT_STG + 2);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STG);
+    const uint32_t dfull = smem_u32(bars + 2 * STG), bready = smem_u32(bars + 2 * STG + 1);
+    const uint32_t drain = smem_u32(bars + 2 * STG + 2), ebar = smem_u32(bars + 2 * STG + 3);
+    const uint32_t sdone = smem_u32(bars + 2 * STG + 4);  // the epilogue is done with the staging
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TT_STG; ++s) {
+        for (int s = 0; s < STG; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
         mbar_init(dfull, 1);
-        mbar_init(bready, TT_THREADS - 64);
+        mbar_init(bready, TT_EPI);
         mbar_init(drain, 1);
+        mbar_init(ebar, TT_EPI);
+        mbar_init(sdone, TT_EPI);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -200,32 +270,33 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mEm) : "memory");
             int stage = 0;
             uint32_t phase = 0;
-            int issued[TT_STG];
-            uint32_t issued_par[TT_STG];
-            for (int s = 0; s < TT_STG; ++s) issued[s] = 0;
+            int issued[4] = {0, 0, 0, 0};
+            uint32_t issued_par[4] = {0, 0, 0, 0};
             bool ok = true;
-            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
+            uint32_t wit = 0;
+            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x, ++wit) {
+                // the ring's memory holds the walker staging until the epilogue is done with it
+                if (!mbar_wait(sdone, wit & 1u, abort_flag)) { ok = false; break; }
                 for (int r = 0; ok && r < R; ++r) {
                     const bool e = (r == 0 || r == R - 1);
-                    for (int mt = 0; ok && mt < MT; ++mt)
-                        for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
-                            for (int kb = 0; kb < kbh; ++kb) {
-                                if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
-                                issued[stage] = 0;
-                                const uint32_t full = full0 + 8 * stage;
-                                const uint32_t dh = smem_u32(sA + stage * TT_STAGE), dm = dh + TT_TILE;
-                                mbar_expect_tx(full, TT_STAGE);
-                                if (e) {
-                                    tma_load_2d(dh, &mEh, kb * 64, mt * 128, full);
-                                    tma_load_2d(dm, &mEm, kb * 64, mt * 128, full);
-                                } else {  // rows past n of the last tile read as zero
-                                    tma_load_3d(dh, &mVh, kb * 64, mt * 128, hf * wc + w, full);
-                                    tma_load_3d(dm, &mVm, kb * 64, mt * 128, hf * wc + w, full);
-                                }
-                                issued[stage] = 1;
-                                issued_par[stage] = phase;
-                                if (++stage == TT_STG) { stage = 0; phase ^= 1; }
+                    for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
+                        for (int kb = 0; kb < kbh; ++kb) {
+                            if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
+                            issued[stage] = 0;
+                            const uint32_t full = full0 + 8 * stage;
+                            const uint32_t dh = smem_u32(ring + stage * STAGE), dm = dh + TILE;
+                            mbar_expect_tx(full, STAGE);
+                            if (e) {  // rows and columns past n read as zero
+                                tma_load_2d(dh, &mEh, kb * 64, 0, full);
+                                tma_load_2d(dm, &mEm, kb * 64, 0, full);
+                            } else {
+                                tma_load_3d(dh, &mVh, kb * 64, 0, hf * wc + w, full);
+                                tma_load_3d(dm, &mVm, kb * 64, 0, hf * wc + w, full);
                             }
+                            issued[stage] = 1;
+                            issued_par[stage] = phase;
+                            if (++stage == STG) { stage = 0; phase ^= 1; }
+                        }
                 }
             }
             if (!ok) {
@@ -234,7 +305,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             }
             // every copy this thread issued lands before the CTA exits (after an
             // abort elsewhere in the CTA nobody else waits for them)
-            for (int s = 0; s < TT_STG; ++s)
+            for (int s = 0; s < STG; ++s)
                 if (issued[s]) mbar_wait(full0 + 8 * s, issued_par[s], nullptr);
         }
     } else if (warp == 1) {
@@ -242,34 +313,29 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             int stage = 0;
             uint32_t phase = 0, rr = 0;
             bool ok = true;
-            const uint32_t b0 = smem_u32(sB);
+            const uint32_t idesc = tt_idesc(N);
+            const uint32_t rb = smem_u32(ring);
             for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
                 for (int r = 0; ok && r < R; ++r, ++rr) {
                     const bool e = (r == 0 || r == R - 1);
                     if (!mbar_wait(bready, rr & 1, abort_flag)) { ok = false; break; }
                     tc_fence_after();
-                    for (int mt = 0; ok && mt < MT; ++mt) {
-                        uint32_t acc = 0;
-                        const uint32_t d = tmem + mt * TT_TCOLS;
-                        for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
-                            for (int kb = 0; kb < kbh; ++kb) {
-                                if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
-                                tc_fence_after();
-                                const uint32_t ah = smem_u32(sA + stage * TT_STAGE), am = ah + TT_TILE;
-                                for (int s = 0; s < 4; ++s) {
-                                    const int t = kb * 4 + s;
-                                    if (t >= S) break;
-                                    const int g = hf * S + t;  // K step within B
-                                    const uint64_t db = desc_k128(b0 + (uint32_t)((g >> 2) * TT_BBLK + (g & 3) * 32));
-                                    // hi . [hi; mid] -> columns 0-127, mid . hi added to columns 64-127
-                                    umma_bf16_i(d, desc_k128(ah + 32 * s), db, TT_IDESC128, acc);
-                                    umma_bf16_i(d + TT_N, desc_k128(am + 32 * s), db, TT_IDESC64, 1);
-                                    acc = 1;
-                                }
-                                umma_commit(empty0 + 8 * stage);
-                                if (++stage == TT_STG) { stage = 0; phase ^= 1; }
+                    uint32_t acc = 0;
+                    for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
+                        for (int kb = 0; kb < kbh; ++kb) {
+                            if (!mbar_wait(full0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                            tc_fence_after();
+                            const uint32_t bh = rb + stage * STAGE, bm = bh + TILE;
+                            const int t0 = kb * 4, nt = S - t0 < 4 ? S - t0 : 4;
+                            uint32_t a = tmem + TT_ACOL + 8u * (uint32_t)(hf * S + t0);
+                            for (int s = 0; s < nt; ++s, a += 8) {
+                                umma_ts(tmem, a, desc_k128(bh + 32 * s), idesc, acc);
+                                umma_ts(tmem, a, desc_k128(bm + 32 * s), idesc, 1);
+                                acc = 1;
                             }
-                    }
+                            umma_commit(empty0 + 8 * stage);
+                            if (++stage == STG) { stage = 0; phase ^= 1; }
+                        }
                     if (ok) umma_commit(dfull);
                 }
             }
@@ -283,128 +349,141 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             mbar_wait(drain, 0, nullptr);
         }
     } else {
-        const int q = warp & 3, mt = (warp - 2) >> 2;
-        const int i = mt * 128 + q * 32 + lane;
-        const bool row = i < n;
-        const int kb0 = 16 * S;  // K index of the bottom half
-        const TTRow trow = tt_row(i, kb0);
-        // B starts (and its padding stays) zero
-        for (int e = threadIdx.x - 64; e < KBB * TT_BBLK / 16; e += TT_THREADS - 64)
-            ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
-        asm volatile("bar.sync 1, %0;" ::"r"(TT_THREADS - 64) : "memory");
-        uint32_t rr = 0;
+        const int ew = warp - 2, q4 = warp & 3, et = threadIdx.x - 64;
+        const int L = 32 * q4 + lane, c = L >> 2, p = (L >> 1) & 1, q = L & 1;
+        const bool valid = c < o;
+        const float sg = q ? 1.f : -1.f;  // an A row's bottom half is sg times the other part
+        const int NC = N >> 2, nch = NC >> 2, j0 = (ew >> 2) * NC;  // columns j0 .. j0 + NC - 1, nch chunks of 4
+        const uint32_t lf = (uint32_t)(32 * q4) << 16;
+        const uint32_t tD = tmem + lf + (uint32_t)j0;
+        const uint32_t tA = tmem + lf + TT_ACOL + (uint32_t)(j0 >> 1), tAb = tA + (uint32_t)(N >> 1);
+        float* Uc = Us + (size_t)j0 * o2 + 2 * c + q;  // staging: own part of column j0 + jj at Uc[jj * o2]
+        const float* Uo = Uc + (q ? -1 : 1);          // the other part
+        const int ne = n * o2, nu = N * o2;
+        uint32_t rr = 0, eph = 0;
         bool ok = true;
+        // U in registers: U[2 k + i] = own part q of column j0 + 4 k + 2 i + p
+        float U[2 * TT_MAXCH];
+#pragma unroll
+        for (int m = 0; m < 2 * TT_MAXCH; ++m) U[m] = 0.f;
+        // U <- the first walker's W32, rows past n zero
+        if ((int)blockIdx.x < wc) tt_fill_u(Us, (const double*)(win + (size_t)blockIdx.x * n * o), ne, nu, et);
         for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
-            double2* Wr = wout + ((size_t)w * n + i) * o;  // this thread's row
-            const double2* Wi = win + ((size_t)w * n + i) * o;
-            const uint32_t lq = (uint32_t)(q * 32) << 16;
-            const uint32_t ta = tmem + mt * TT_TCOLS + lq;            // accumulator
-            const uint32_t ts = tmem + TT_SCOL + mt * TT_N + lq;      // running update
-            const uint32_t tf = tmem + TT_FCOL + mt * TT_N + lq;      // fp32 copy of the row
-            // the row's loads go out 16 at a time ahead of the shared-memory
-            // writes (which the compiler may not move loads across)
+            if (!tt_epi_sync(ebar, eph, abort_flag)) { ok = false; break; }
+            // A <- the split of W32; U <- its own entries
 #pragma unroll
-            for (int hb = 0; hb < 32; hb += 16) {
-                float2 f[16];
+            for (int k = 0; k < TT_MAXCH; ++k) {
+                if (k >= nch) break;
+                float t[4], b[4];
 #pragma unroll
-                for (int u = 0; u < 16; ++u) {
-                    const int c = hb + u;
-                    const double2 v = (row && c < o) ? Wi[c] : make_double2(0.0, 0.0);
-                    f[u] = make_float2((float)v.x, (float)v.y);
+                for (int u = 0; u < 4; ++u) {
+                    t[u] = valid ? Uc[(4 * k + u) * o2] : 0.f;
+                    b[u] = valid ? sg * Uo[(4 * k + u) * o2] : 0.f;
                 }
-#pragma unroll
-                for (int cb = 0; cb < 16; cb += 8) {
-                    uint32_t fv[16];
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int c = hb + cb + u;
-                        if (row && c < o) tt_write_b(sB, trow, c, f[cb + u]);
-                        fv[u] = __float_as_uint(f[cb + u].x);
-                        fv[8 + u] = __float_as_uint(f[cb + u].y);
-                    }
-                    tmem_st8x2(tf + hb + cb, tf + 32 + hb + cb, fv);
-                }
+                U[2 * k] = p ? t[1] : t[0];
+                U[2 * k + 1] = p ? t[3] : t[2];
+                tmem_st2(tA + 2 * k, tt_piece2(t[0], t[1], p), tt_piece2(t[2], t[3], p));
+                tmem_st2(tAb + 2 * k, tt_piece2(b[0], b[1], p), tt_piece2(b[2], b[3], p));
             }
+            fence_proxy_async();  // the staging's generic accesses before the ring's next copies
+            mbar_arrive(sdone);
+            tmem_wait_st();
             tc_fence_before();
-            fence_proxy_async();
             mbar_arrive(bready);
+            if (w + (int)gridDim.x < wc) {  // the next walker's rows, read after this walker
+                const char* nx = (const char*)(win + (size_t)(w + gridDim.x) * n * o);
+                for (int b = et * 128; b < n * o * 16; b += TT_EPI * 128) prefetch_l2(nx + b);
+            }
             for (int r = 0; r < R; ++r, ++rr) {
-                if (row && r == R - 1) {  // rows read after the last product: this walker's, the next one's
-                    for (int b = 0; b < o * 16; b += 128) prefetch_l2((const char*)Wi + b);
-                    if (w + (int)gridDim.x < wc)
-                        for (int b = 0; b < o * 16; b += 128)
-                            prefetch_l2((const char*)(Wi + (size_t)gridDim.x * n * o) + b);
-                }
-                if (!mbar_wait_inl(dfull, rr & 1, abort_flag)) {
-                    atomicExch(err, 1);
-                    *abort_flag = 1;
-                    ok = false;
-                    break;
-                }
+                if (!mbar_wait_inl(dfull, rr & 1, abort_flag)) { ok = false; break; }
                 tc_fence_after();
-                const float sk = sqrt_dt / (float)(r > 0 ? r : 1);
-                if (r == R - 1) {  // W' = W + (S + (E - I) out): the one binary64 update
-#pragma unroll
-                    for (int cb = 0; cb < 32; cb += 8) {
-                        double2 wv[8];  // loaded ahead of the stores (Wi and Wr alias)
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            wv[u] = (row && cb + u < o) ? Wi[cb + u] : make_double2(0.0, 0.0);
-                        uint32_t y[32], sv[16];
-                        tmem_ld8x4(ta + cb, ta + TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb, y);
-                        tmem_ld8x2(ts + cb, ts + 32 + cb, sv);
-                        if (row) {
-#pragma unroll
-                            for (int u = 0; u < 8; ++u) {
-                                const int c = cb + u;
-                                const float yr = __uint_as_float(y[u]) + __uint_as_float(y[8 + u]);
-                                const float yi = __uint_as_float(y[16 + u]) + __uint_as_float(y[24 + u]);
-                                const float sr = __uint_as_float(sv[u]), si = __uint_as_float(sv[8 + u]);
-                                if (c < o) Wr[c] = make_double2(wv[u].x + (double)(sr + yr), wv[u].y + (double)(si + yi));
-                            }
-                        }
-                    }
-                    tc_fence_before();
-                    continue;
+                if (r == R - 2) {  // this walker's rows, read again by the final pass
+                    const char* me = (const char*)(win + (size_t)w * n * o);
+                    for (int b = et * 128; b < n * o * 16; b += TT_EPI * 128) prefetch_l2(me + b);
                 }
+                const float sk = sqrt_dt / (float)(r > 0 ? r : 1), sgsk = sg * sk;
+                const bool last = r == R - 1;
+                const bool x_is_u = !last && (r == 0 || r == R - 2);  // the next operand is U (W1, or out)
+                const bool term_is_y = r == 0 || last;                // the term added to U: Y, else T_r
 #pragma unroll
-                for (int cb = 0; cb < 32; cb += 8) {
-                    // Y columns cb..cb+7 of Yr and Yi (hi.hi + corrections); S and the row copy
-                    uint32_t y[32], sf[32];
-                    tmem_ld8x4(ta + cb, ta + TT_N + cb, ta + 32 + cb, ta + TT_N + 32 + cb, y);
-                    tmem_ld8x4(ts + cb, ts + 32 + cb, tf + cb, tf + 32 + cb, sf);
-                    uint32_t sv[16];
-                    if (row) {
+                for (int kb = 0; kb < TT_MAXCH / 4; ++kb) {  // 16-column batches of the accumulator
+                    if (4 * kb >= nch) break;
+                    uint32_t v[16];
+                    if (4 * kb + 4 <= nch) {
+                        tmem_ld16_wait(tD + 16 * kb, v);
+                    } else {
 #pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const int c = cb + u;
-                            const float yr = __uint_as_float(y[u]) + __uint_as_float(y[8 + u]);
-                            const float yi = __uint_as_float(y[16 + u]) + __uint_as_float(y[24 + u]);
-                            float sr = __uint_as_float(sf[u]), si = __uint_as_float(sf[8 + u]);
-                            const float fr = __uint_as_float(sf[16 + u]), fi = __uint_as_float(sf[24 + u]);
-                            if (c < o) {
-                                if (r == 0) {  // W1 = W + (E - I) W
-                                    sr = yr;
-                                    si = yi;
-                                    tt_write_b(sB, trow, c, make_float2(fr + yr, fi + yi));
-                                } else {  // T_r = (i sqrt_dt / r) Y
-                                    const float2 t = make_float2(-sk * yi, sk * yr);
-                                    sr += t.x;
-                                    si += t.y;
-                                    if (r < n_terms) tt_write_b(sB, trow, c, t);
-                                    else tt_write_b(sB, trow, c, make_float2(fr + sr, fi + si));  // out = W1 + sum T_k
-                                }
-                            }
-                            sv[u] = __float_as_uint(sr);
-                            sv[8 + u] = __float_as_uint(si);
+                        for (int cc = 0; cc < 3; ++cc) {
+                            if (4 * kb + cc >= nch) break;
+                            uint32_t v4[4];
+                            tmem_ld4(tD + 16 * kb + 4 * cc, v4);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) v[4 * cc + u] = v4[u];
                         }
                     }
-                    tmem_st8x2(ts + cb, ts + 32 + cb, sv);
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const int k = 4 * kb + cc;
+                        if (k >= nch) break;
+                        float yp[4], tq[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float y = __uint_as_float(v[4 * cc + u]);
+                            yp[u] = y + __shfl_xor_sync(0xffffffffu, y, 2);           // own part of Y
+                            const float yo = __shfl_xor_sync(0xffffffffu, yp[u], 1);  // the other part
+                            tq[u] = term_is_y ? yp[u] : sgsk * yo;  // own part of T_r = (i sqrt_dt / r) Y
+                        }
+                        U[2 * k] += p ? tq[1] : tq[0];
+                        U[2 * k + 1] += p ? tq[3] : tq[2];
+                        if (last) continue;
+                        float xq[4], xo[4];
+                        if (x_is_u) {
+#pragma unroll
+                            for (int i = 0; i < 2; ++i) {
+                                const float mine = U[2 * k + i];
+                                const float other = __shfl_xor_sync(0xffffffffu, mine, 2);
+                                xq[2 * i] = p ? other : mine;
+                                xq[2 * i + 1] = p ? mine : other;
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) xo[u] = sg * __shfl_xor_sync(0xffffffffu, xq[u], 1);
+                        } else {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                xq[u] = tq[u];
+                                xo[u] = -sk * yp[u];  // sg times the other part of T_r
+                            }
+                        }
+                        tmem_st2(tA + 2 * k, valid ? tt_piece2(xq[0], xq[1], p) : 0u,
+                                 valid ? tt_piece2(xq[2], xq[3], p) : 0u);
+                        tmem_st2(tAb + 2 * k, valid ? tt_piece2(xo[0], xo[1], p) : 0u,
+                                 valid ? tt_piece2(xo[2], xo[3], p) : 0u);
+                    }
                 }
                 tc_fence_before();
-                fence_proxy_async();
-                mbar_arrive(bready);
+                if (!last) {
+                    tmem_wait_st();
+                    tc_fence_before();
+                    mbar_arrive(bready);
+                }
             }
+            if (!ok) break;
+            // W' = W + ((U - W32) + (E - I) out), U <- the next walker's W32
+            if (valid) {
+#pragma unroll
+                for (int k = 0; k < TT_MAXCH; ++k) {
+                    if (k >= nch) break;
+                    Uc[(4 * k + p) * o2] = U[2 * k];
+                    Uc[(4 * k + 2 + p) * o2] = U[2 * k + 1];
+                }
+            }
+            if (!tt_epi_sync(ebar, eph, abort_flag)) { ok = false; break; }
+            tt_final(win + (size_t)w * n * o, wout + (size_t)w * n * o, Us, ne, et);
+            if (w + (int)gridDim.x < wc) tt_fill_u(Us, (const double*)(win + (size_t)(w + gridDim.x) * n * o), ne, nu, et);
+        }
+        if (!ok) {
+            atomicExch(err, 1);
+            *abort_flag = 1;
         }
     }
     tc_fence_before();
@@ -418,7 +497,10 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
 
 }  // namespace tc
 
-bool trotter_tc_supported(int n, int o) { return n % 8 == 0 && n <= 256 && o <= 32; }
+bool trotter_tc_supported(int n, int o) {
+    if (!(n % 8 == 0 && n > 0 && n <= 256 && o > 0 && o <= 32)) return false;
+    return tc::tt_geo(n, o).stg >= 2;
+}
 
 int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const __nv_bfloat16* eh,
                       const __nv_bfloat16* em, const __nv_bfloat16* vh, const __nv_bfloat16* vm, const double2* win,
@@ -428,24 +510,27 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
     if (!trotter_tc_supported(n, o))
         return fail(AFQ_E_UNSUPPORTED, "tensor-core Trotter: norb=%d nocc=%d (needs norb %% 8 == 0, <= 256, nocc <= 32)",
                     n, o);
+    if (n_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_exp_terms=%d must be >= 0", n_terms);
+    const TTGeo g = tt_geo(n, o);
     static DeviceOnce smem_once;
     AFQ_TRY(get_encode());
     int nsm = 0;
     AFQ_TRY(device_sms(&nsm));
-    AFQ_TRY(raise_smem_once(smem_once, k_trotter_tc, TT_SMEM));
+    AFQ_TRY(raise_smem_once(smem_once, k_trotter_tc, TT_SMEM_MAX));
     CUtensorMap mvh, mvm, meh, mem;
-    AFQ_TRY(make_map3(&mvh, vh, 2LL * wc, n, n, n, 128));
-    AFQ_TRY(make_map3(&mvm, vm, 2LL * wc, n, n, n, 128));
-    AFQ_TRY(make_map(&meh, eh, n, n, n, 128));
-    AFQ_TRY(make_map(&mem, em, n, n, n, 128));
+    AFQ_TRY(make_map3(&mvh, vh, 2LL * wc, n, n, n, g.N));
+    AFQ_TRY(make_map3(&mvm, vm, 2LL * wc, n, n, n, g.N));
+    AFQ_TRY(make_map(&meh, eh, n, n, n, g.N));
+    AFQ_TRY(make_map(&mem, em, n, n, n, g.N));
     const int grid = wc < nsm ? wc : nsm;
-    k_trotter_tc<<<grid, TT_THREADS, TT_SMEM, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, win, wout,
-                                                 err);
+    k_trotter_tc<<<grid, TT_THREADS, g.smem, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, g, win, wout,
+                                                err);
     AFQ_LAUNCHED("k_trotter_tc");
     return AFQ_OK;
 }
 
-// (E - I) as bf16 hi and mid pieces (n x n), the A operand of the E products.
+// (E - I) as bf16 hi and mid pieces (n x n), the B operand of the E products
+// (row j over K = k: (E - I)[j, k]).
 __global__ void k_e_minus_i_split(int n, const double* __restrict__ E, __nv_bfloat16* __restrict__ eh,
                                   __nv_bfloat16* __restrict__ em) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {

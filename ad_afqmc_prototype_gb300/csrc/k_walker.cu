@@ -10,7 +10,7 @@ namespace afq {
 template <class K>
 static int set_smem(K kernel, size_t bytes) {
     if (bytes > 227 * 1024) return fail(AFQ_E_UNSUPPORTED, "kernel needs %zu bytes of shared memory", bytes);
-    if (bytes > 48 * 1024)
+    if (bytes > 32 * 1024)  // with the kernel's static shared memory the default limit is below 48 KB
         AFQ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return AFQ_OK;
 }

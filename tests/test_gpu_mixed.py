@@ -11,7 +11,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def _setup(wl_name, W, precision, **pkw):
+def _setup(wl_name, W, precision, asym=0.0, **pkw):
     from ad_afqmc_prototype_gb300 import synth
     from ad_afqmc_prototype_gb300.core.system import system
     from ad_afqmc_prototype_gb300.ham.chol import ham_chol
@@ -20,8 +20,11 @@ def _setup(wl_name, W, precision, **pkw):
     from ad_afqmc_prototype_gb300.prop.chol_afqmc_ops import make_chol_afqmc_ops
     from ad_afqmc_prototype_gb300.prop.types import afqmc_params
     from ad_afqmc_prototype_gb300.trial.rhf import get_rdm1, make_rhf_trial_ops, rhf_trial
-    wl = synth.WORKLOADS[wl_name]
+    wl = synth.WORKLOADS[wl_name] if isinstance(wl_name, str) else wl_name
     H = synth.make_workload(wl)
+    if asym:  # an antisymmetric part: V = sum_g x_g L_g is then not symmetric
+        r = np.random.default_rng(wl.seed + 1).normal(size=H["chol"].shape)
+        H["chol"] = H["chol"] + asym * np.abs(H["chol"]).mean() * (r - np.swapaxes(r, 1, 2))
     n, o = wl.nbasis, wl.nocc
     sys_ = system(norb=n, nelec=(o, o), walker_kind="restricted")
     ham = ham_chol(h0=H["h0"], h1=H["h1"], chol=H["chol"])
@@ -68,6 +71,31 @@ def test_mixed_step_close_to_fp64(cuda, wl, W, prec):
     assert relw < 1e-4, relw
     relo = float(((a.overlaps - b.overlaps).abs() / a.overlaps.abs()).max().item())
     assert relo < 1e-3, relo
+
+
+@pytest.mark.parametrize("n,o,G,asym", [(40, 7, 96, 0.0), (120, 20, 240, 0.5), (200, 32, 400, 0.0),
+                                        (256, 32, 300, 0.0), (248, 1, 200, 0.5)])
+def test_tensor_core_taylor_shapes(cuda, n, o, G, asym):
+    """The three-section step at the tensor-core Taylor kernel's edge shapes
+    (norb a multiple of 8 up to 256, not of 16; nocc up to 32 and 1; three and
+    four ring stages, the walker staged through the ring; Cholesky
+    vectors with an antisymmetric part, so that a transposed V would show)
+    against the binary64 step from the same state and fields: walkers within
+    1e-5 of their largest entry after three steps."""
+    from ad_afqmc_prototype_gb300 import engine, synth
+    W = 24
+    wl = synth.Workload(name=f"t_n{n}_o{o}_g{G}", nbasis=n, nocc=o, nchol=G, n_walkers=W, n_steps=3, seed=11)
+    pa, pra, st = _setup(wl, W, "fp64", asym=asym)
+    pb, prb, _ = _setup(wl, W, "mixed_fast", asym=asym)
+    a, b = _dstate(st), _dstate(st)
+    for k in range(3):
+        f = engine.fill_normal((W, G), 5, k)
+        engine.step(pa, pra, a, 0, 0, fields=f)
+        engine.step(pb, prb, b, 0, 0, fields=f)
+    assert engine.workspace_status() == 0
+    rel = float(((a.walkers - b.walkers).abs().max() / a.walkers.abs().max()).item())
+    print(f"n={n} o={o}: max |dW| / max |W| = {rel:.3e}")
+    assert rel < 1e-5, rel
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
