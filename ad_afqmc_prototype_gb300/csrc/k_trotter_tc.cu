@@ -33,10 +33,10 @@
 // of the accumulator belongs to the epilogue thread that holds TMEM lane
 // 4c + 2p + q; the four lanes of an orbital c are in one warp and exchange
 // the piece sums and the Re/Im parts by shuffles.  U(j, c, q) is held by
-// lane (c, j & 1, q).  Between two walkers the walker passes through shared
-// memory in its own element order (coalesced loads and stores), in the B
-// ring's memory: the producer starts the next walker's copies only after the
-// epilogue is done with it.
+// lane (c, j & 1, q).  The walker is read and written by the epilogue lanes
+// themselves: lane (c, p, q) loads part q of W[j][c] (a warp reads 128
+// contiguous bytes of a row j), takes the other part by the xor-1 shuffle,
+// and at the end stores its own entries.
 //
 // Warps: 0 TMA producer, 1 MMA issuer and tensor-memory owner, 2-17 epilogue
 // (warp w reads lanes 32 (w % 4).. of tensor memory, as tcgen05.ld allows;
@@ -55,7 +55,6 @@ constexpr int TT_THREADS = 576;          // 18 warps
 constexpr int TT_EPI = TT_THREADS - 64;  // epilogue threads
 constexpr uint32_t TT_ACOL = 256;        // tensor-memory column of the A operand
 constexpr int TT_SMEM_MAX = 227 * 1024;
-constexpr int TT_MAXCH = 16;             // 4-column chunks of an epilogue thread (N / 16 <= 16)
 
 __host__ __device__ constexpr uint32_t tt_idesc(int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
@@ -77,8 +76,6 @@ static TTGeo tt_geo(int n, int o) {
     const int stage = 2 * g.N * 128;
     g.stg = (TT_SMEM_MAX - 1024 - 256) / stage;
     if (g.stg > 4) g.stg = 4;
-    // the walker staging (N x nocc x 2 floats) reuses the ring between walkers
-    if ((long long)g.N * 2 * o * 4 > (long long)g.stg * stage) g.stg = 0;
     g.smem = 1024 + g.stg * stage + 256;
     return g;
 }
@@ -162,58 +159,9 @@ __device__ __forceinline__ void tmem_ld8_wait(uint32_t a, uint32_t (&v)[8]) {
 }
 #undef TT_O8
 
-// Bounded barrier of the epilogue threads (an mbarrier with their count):
-// false on timeout or abort.
-__device__ __forceinline__ bool tt_epi_sync(uint32_t bar, uint32_t& ph, volatile int* abort_flag) {
-    mbar_arrive(bar);
-    const bool ok = mbar_wait_inl(bar, ph, abort_flag);
-    ph ^= 1u;
-    return ok;
-}
-
-// Staging of a walker through U, coalesced, TT_SPT loads of a thread in
-// flight at once (passes of TT_SPT x 512 entries: three at norb 200 x nocc 30).
-constexpr int TT_SPT = 12;
-
-// U <- W32 of a walker in its own element order (j, c, Re/Im); entries
-// ne..nu-1 (rows n..N-1) zero.
-__device__ __forceinline__ void tt_fill_u(float* Us, const double* __restrict__ W, int ne, int nu, int et) {
-    for (int e0 = et; e0 < nu; e0 += TT_SPT * TT_EPI) {
-        double x[TT_SPT];
-#pragma unroll
-        for (int u = 0; u < TT_SPT; ++u) {
-            const int e = e0 + u * TT_EPI;
-            x[u] = e < ne ? W[e] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < TT_SPT; ++u) {
-            const int e = e0 + u * TT_EPI;
-            if (e < ne) Us[e] = tt_w32(x[u]);
-            else if (e < nu) Us[e] = 0.f;
-        }
-    }
-}
-
-// W' = W + (U - W32): the walker's one binary64 add per entry (win and wout
-// may alias: each entry is read and written by one thread).
-__device__ __forceinline__ void tt_final(const double2* win, double2* wout, const float* Us, int ne, int et) {
-    const double* W = (const double*)win;
-    double* Wo = (double*)wout;
-    for (int e0 = et; e0 < ne; e0 += TT_SPT * TT_EPI) {
-        double x[TT_SPT];
-#pragma unroll
-        for (int u = 0; u < TT_SPT; ++u) {
-            const int e = e0 + u * TT_EPI;
-            x[u] = e < ne ? W[e] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < TT_SPT; ++u) {
-            const int e = e0 + u * TT_EPI;
-            if (e < ne) Wo[e] = x[u] + tt_f2d(Us[e] - tt_w32(x[u]));
-        }
-    }
-}
-
+// MAXCH: the largest count of 4-column chunks an epilogue thread takes
+// (N / 16; the instantiations cover N <= 64, 128, 208 and 256).
+template <int MAXCH>
 __global__ void __launch_bounds__(TT_THREADS, 1)
     k_trotter_tc(const __grid_constant__ CUtensorMap mVh, const __grid_constant__ CUtensorMap mVm,
                  const __grid_constant__ CUtensorMap mEh, const __grid_constant__ CUtensorMap mEm, int wc, int n,
@@ -224,18 +172,13 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
     const int N = g.N, S = g.S, kbh = g.kbh, STG = g.stg;
     const uint32_t TILE = (uint32_t)N * 128u, STAGE = 2u * TILE;
     const int R = n_terms + 2;  // products per walker: E, n_terms V, E
-    const int o2 = 2 * o;
     uint8_t* ring = smem;
-    // walker staging U[j][c][q] (N x o x 2 floats): the ring's memory, used
-    // between two walkers while no copy is in flight
-    float* Us = (float*)ring;
     uint64_t* bars = (uint64_t*)(smem + (size_t)STG * STAGE);
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STG + 5);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STG + 3);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STG);
     const uint32_t dfull = smem_u32(bars + 2 * STG), bready = smem_u32(bars + 2 * STG + 1);
-    const uint32_t drain = smem_u32(bars + 2 * STG + 2), ebar = smem_u32(bars + 2 * STG + 3);
-    const uint32_t sdone = smem_u32(bars + 2 * STG + 4);  // the epilogue is done with the staging
+    const uint32_t drain = smem_u32(bars + 2 * STG + 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
@@ -246,8 +189,6 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         mbar_init(dfull, 1);
         mbar_init(bready, TT_EPI);
         mbar_init(drain, 1);
-        mbar_init(ebar, TT_EPI);
-        mbar_init(sdone, TT_EPI);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -273,10 +214,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
             int issued[4] = {0, 0, 0, 0};
             uint32_t issued_par[4] = {0, 0, 0, 0};
             bool ok = true;
-            uint32_t wit = 0;
-            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x, ++wit) {
-                // the ring's memory holds the walker staging until the epilogue is done with it
-                if (!mbar_wait(sdone, wit & 1u, abort_flag)) { ok = false; break; }
+            for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
                 for (int r = 0; ok && r < R; ++r) {
                     const bool e = (r == 0 || r == R - 1);
                     for (int hf = 0; ok && hf < (e ? 1 : 2); ++hf)
@@ -357,56 +295,60 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         const uint32_t lf = (uint32_t)(32 * q4) << 16;
         const uint32_t tD = tmem + lf + (uint32_t)j0;
         const uint32_t tA = tmem + lf + TT_ACOL + (uint32_t)(j0 >> 1), tAb = tA + (uint32_t)(N >> 1);
-        float* Uc = Us + (size_t)j0 * o2 + 2 * c + q;  // staging: own part of column j0 + jj at Uc[jj * o2]
-        const float* Uo = Uc + (q ? -1 : 1);          // the other part
-        const int ne = n * o2, nu = N * o2;
-        uint32_t rr = 0, eph = 0;
+        uint32_t rr = 0;
         bool ok = true;
         // U in registers: U[2 k + i] = own part q of column j0 + 4 k + 2 i + p
-        float U[2 * TT_MAXCH];
+        float U[2 * MAXCH];
 #pragma unroll
-        for (int m = 0; m < 2 * TT_MAXCH; ++m) U[m] = 0.f;
-        // U <- the first walker's W32, rows past n zero
-        if ((int)blockIdx.x < wc) tt_fill_u(Us, (const double*)(win + (size_t)blockIdx.x * n * o), ne, nu, et);
+        for (int m = 0; m < 2 * MAXCH; ++m) U[m] = 0.f;
         for (int w = blockIdx.x; ok && w < wc; w += gridDim.x) {
-            if (!tt_epi_sync(ebar, eph, abort_flag)) { ok = false; break; }
-            // A <- the split of W32; U <- its own entries
+            // part q of W[j][c] at Wq[2 j o]: a warp reads 128 contiguous bytes a row
+            const double* Wq = (const double*)(win + (size_t)w * n * o + c) + q;
+            // A <- the split of W32 (own part loaded, the other by the xor-1 shuffle); U <- its own entries
 #pragma unroll
-            for (int k = 0; k < TT_MAXCH; ++k) {
-                if (k >= nch) break;
-                float t[4], b[4];
+            for (int kb = 0; kb < (MAXCH + 1) / 2; ++kb) {  // 8 columns, their loads in flight together
+                if (2 * kb >= nch) break;
+                double wv[8];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    t[u] = valid ? Uc[(4 * k + u) * o2] : 0.f;
-                    b[u] = valid ? sg * Uo[(4 * k + u) * o2] : 0.f;
+                for (int u = 0; u < 8; ++u) {
+                    const int j = j0 + 8 * kb + u;
+                    wv[u] = (valid && 2 * kb + (u >> 2) < nch && j < n) ? Wq[(size_t)2 * j * o] : 0.0;
                 }
-                U[2 * k] = p ? t[1] : t[0];
-                U[2 * k + 1] = p ? t[3] : t[2];
-                tmem_st2(tA + 2 * k, tt_piece2(t[0], t[1], p), tt_piece2(t[2], t[3], p));
-                tmem_st2(tAb + 2 * k, tt_piece2(b[0], b[1], p), tt_piece2(b[2], b[3], p));
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc) {
+                    const int k = 2 * kb + cc;
+                    if (k >= nch) break;
+                    float t[4], b[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        t[u] = tt_w32(wv[4 * cc + u]);
+                        b[u] = sg * __shfl_xor_sync(0xffffffffu, t[u], 1);
+                    }
+                    U[2 * k] = p ? t[1] : t[0];
+                    U[2 * k + 1] = p ? t[3] : t[2];
+                    tmem_st2(tA + 2 * k, tt_piece2(t[0], t[1], p), tt_piece2(t[2], t[3], p));
+                    tmem_st2(tAb + 2 * k, tt_piece2(b[0], b[1], p), tt_piece2(b[2], b[3], p));
+                }
             }
-            fence_proxy_async();  // the staging's generic accesses before the ring's next copies
-            mbar_arrive(sdone);
             tmem_wait_st();
             tc_fence_before();
             mbar_arrive(bready);
-            if (w + (int)gridDim.x < wc) {  // the next walker's rows, read after this walker
-                const char* nx = (const char*)(win + (size_t)(w + gridDim.x) * n * o);
-                for (int b = et * 128; b < n * o * 16; b += TT_EPI * 128) prefetch_l2(nx + b);
-            }
             for (int r = 0; r < R; ++r, ++rr) {
                 if (!mbar_wait_inl(dfull, rr & 1, abort_flag)) { ok = false; break; }
                 tc_fence_after();
-                if (r == R - 2) {  // this walker's rows, read again by the final pass
+                if (r == R - 2) {  // this walker's rows (read again at the end) and the next walker's
                     const char* me = (const char*)(win + (size_t)w * n * o);
                     for (int b = et * 128; b < n * o * 16; b += TT_EPI * 128) prefetch_l2(me + b);
+                    if (w + (int)gridDim.x < wc)
+                        for (int b = et * 128; b < n * o * 16; b += TT_EPI * 128)
+                            prefetch_l2(me + (size_t)gridDim.x * n * o * 16 + b);
                 }
                 const float sk = sqrt_dt / (float)(r > 0 ? r : 1), sgsk = sg * sk;
                 const bool last = r == R - 1;
                 const bool x_is_u = !last && (r == 0 || r == R - 2);  // the next operand is U (W1, or out)
                 const bool term_is_y = r == 0 || last;                // the term added to U: Y, else T_r
 #pragma unroll
-                for (int kb = 0; kb < TT_MAXCH / 4; ++kb) {  // 16-column batches of the accumulator
+                for (int kb = 0; kb < (MAXCH + 3) / 4; ++kb) {  // 16-column batches of the accumulator
                     if (4 * kb >= nch) break;
                     uint32_t v[16];
                     if (4 * kb + 4 <= nch) {
@@ -468,18 +410,24 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                 }
             }
             if (!ok) break;
-            // W' = W + ((U - W32) + (E - I) out), U <- the next walker's W32
-            if (valid) {
+            // W' = W + ((U - W32) + (E - I) out), the own entries of this lane
+            double* Wo = (double*)(wout + (size_t)w * n * o + c) + q;
 #pragma unroll
-                for (int k = 0; k < TT_MAXCH; ++k) {
-                    if (k >= nch) break;
-                    Uc[(4 * k + p) * o2] = U[2 * k];
-                    Uc[(4 * k + 2 + p) * o2] = U[2 * k + 1];
+            for (int kb = 0; kb < (MAXCH + 3) / 4; ++kb) {
+                if (4 * kb >= nch) break;
+                double wv[8];
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {  // own columns j0 + 16 kb + 2 m + p
+                    const int j = j0 + 16 * kb + 2 * m + p;
+                    wv[m] = (valid && 4 * kb + (m >> 1) < nch && j < n) ? Wq[(size_t)2 * j * o] : 0.0;
+                }
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    const int j = j0 + 16 * kb + 2 * m + p;
+                    if (valid && 4 * kb + (m >> 1) < nch && j < n)
+                        Wo[(size_t)2 * j * o] = wv[m] + tt_f2d(U[8 * kb + m] - tt_w32(wv[m]));
                 }
             }
-            if (!tt_epi_sync(ebar, eph, abort_flag)) { ok = false; break; }
-            tt_final(win + (size_t)w * n * o, wout + (size_t)w * n * o, Us, ne, et);
-            if (w + (int)gridDim.x < wc) tt_fill_u(Us, (const double*)(win + (size_t)(w + gridDim.x) * n * o), ne, nu, et);
         }
         if (!ok) {
             atomicExch(err, 1);
@@ -512,19 +460,34 @@ int launch_trotter_tc(int wc, int n, int o, int n_terms, double sqrt_dt, const _
                     n, o);
     if (n_terms < 0) return fail(AFQ_E_INVALID_ARGUMENT, "n_exp_terms=%d must be >= 0", n_terms);
     const TTGeo g = tt_geo(n, o);
-    static DeviceOnce smem_once;
+    static DeviceOnce smem_once[4];
     AFQ_TRY(get_encode());
     int nsm = 0;
     AFQ_TRY(device_sms(&nsm));
-    AFQ_TRY(raise_smem_once(smem_once, k_trotter_tc, TT_SMEM_MAX));
+    const int nch = g.N / 16;
+    const int inst = nch <= 4 ? 0 : nch <= 8 ? 1 : nch <= 13 ? 2 : 3;
+    switch (inst) {
+        case 0: AFQ_TRY(raise_smem_once(smem_once[0], k_trotter_tc<4>, TT_SMEM_MAX)); break;
+        case 1: AFQ_TRY(raise_smem_once(smem_once[1], k_trotter_tc<8>, TT_SMEM_MAX)); break;
+        case 2: AFQ_TRY(raise_smem_once(smem_once[2], k_trotter_tc<13>, TT_SMEM_MAX)); break;
+        default: AFQ_TRY(raise_smem_once(smem_once[3], k_trotter_tc<16>, TT_SMEM_MAX)); break;
+    }
     CUtensorMap mvh, mvm, meh, mem;
     AFQ_TRY(make_map3(&mvh, vh, 2LL * wc, n, n, n, g.N));
     AFQ_TRY(make_map3(&mvm, vm, 2LL * wc, n, n, n, g.N));
     AFQ_TRY(make_map(&meh, eh, n, n, n, g.N));
     AFQ_TRY(make_map(&mem, em, n, n, n, g.N));
     const int grid = wc < nsm ? wc : nsm;
-    k_trotter_tc<<<grid, TT_THREADS, g.smem, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, g, win, wout,
-                                                err);
+#define AFQ_TT(MC)                                                                                         \
+    k_trotter_tc<MC><<<grid, TT_THREADS, g.smem, s>>>(mvh, mvm, meh, mem, wc, n, o, n_terms, (float)sqrt_dt, g, win, \
+                                                    wout, err)
+    switch (inst) {
+        case 0: AFQ_TT(4); break;
+        case 1: AFQ_TT(8); break;
+        case 2: AFQ_TT(13); break;
+        default: AFQ_TT(16); break;
+    }
+#undef AFQ_TT
     AFQ_LAUNCHED("k_trotter_tc");
     return AFQ_OK;
 }
