@@ -102,23 +102,41 @@ __device__ __forceinline__ void rfma(double2& acc, double r, double2 b) {
 __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
 
 // x = hi + lo as an fp32 pair from the binary64 fields with integer
-// operations (binary64 conversions run at the binary64 rate): hi is x cut
-// to 24 significant bits, lo the remaining 29 bits rounded to 24, so
-// |x - hi - lo| <= 2^-48 |x|.  Exponents outside [2^-74, 2^128) (zero,
-// tiny, huge, inf, nan) take the binary64 conversions.
+// operations only, on every path (the binary64 pipe runs at 1/64 of the fp32
+// rate here, and a branch to binary64 conversions would be if-converted and
+// paid for every element): hi is x cut to 24 significant bits, lo the
+// remaining 29 bits rounded to 24, so |x - hi - lo| <= 2^-48 |x| for
+// 2^-74 <= |x| < 2^128.  Below 2^-74 lo is a signed zero, below the fp32
+// normal range hi too; beyond it hi is infinity (nan for a nan).
 __device__ __forceinline__ float2 split_d2f(double x) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(x);
     const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
-    const unsigned e = (h >> 20) & 0x7ffu;
-    if (e < 949u || e > 1150u) {
-        const float hi = (float)x;
-        return make_float2(hi, (float)(x - (double)hi));
-    }
-    const unsigned sign = h & 0x80000000u;
-    const float hi = __uint_as_float(sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29)));
-    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075), the weight of bit 0 of l
-    const float lo = __uint_as_float(sign | __float_as_uint(__uint2float_rn(l & 0x1fffffffu) * scale));
+    const unsigned e = (h >> 20) & 0x7ffu, sign = h & 0x80000000u;
+    const unsigned nrm = sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29));
+    const unsigned big = ((e == 0x7ffu) && ((h & 0xfffffu) | l)) ? 0x7fc00000u : (sign | 0x7f800000u);
+    const float hi = __uint_as_float(e < 897u ? sign : (e > 1150u ? big : nrm));
+    const float scale = __uint_as_float(((e - 948u) & 0xffu) << 23);  // 2^(e - 1075), the weight of bit 0 of l
+    const float lo_n = __uint_as_float(sign | __float_as_uint(__uint2float_rn(l & 0x1fffffffu) * scale));
+    const float lo = (e >= 949u && e <= 1150u) ? lo_n : __uint_as_float(sign);
     return make_float2(hi, lo);
+}
+// x cut to fp32 (the hi part of split_d2f).
+__device__ __forceinline__ float d2f_trunc(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
+    const unsigned e = (h >> 20) & 0x7ffu, sign = h & 0x80000000u;
+    const unsigned nrm = sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29));
+    const unsigned big = ((e == 0x7ffu) && ((h & 0xfffffu) | l)) ? 0x7fc00000u : (sign | 0x7f800000u);
+    return __uint_as_float(e < 897u ? sign : (e > 1150u ? big : nrm));
+}
+// Exact fp32 -> binary64 by integer operations only (fp32 subnormals give a
+// signed zero; inf and nan keep their class).
+__device__ __forceinline__ double f2d_exact(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    const unsigned long long ex = e == 0u ? 0ull : (e == 0xffu ? 2047ull : (unsigned long long)(e + 896u));
+    const unsigned long long m = e == 0u ? 0ull : (unsigned long long)(u & 0x7fffffu) << 29;
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (ex << 52) | m));
 }
 // complex division a / b (Smith's method)
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {

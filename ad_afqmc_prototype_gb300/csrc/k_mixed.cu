@@ -566,11 +566,6 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     float2* invf = mf + o * o;                     // o x o fp32 inverse
     float2* wf = invf + o * o;                     // n x o fp32 copy of W (its hi part)
     float2* wl = wf + (size_t)OS_CH * o;           // DF: lo part of a chunk of OS_CH rows
-    __shared__ int s_piv;
-    __shared__ double2 s_rp;
-    __shared__ float4 s_rpd;
-    __shared__ double2 s_det;
-    __shared__ int s_zero;
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
@@ -645,71 +640,93 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
         for (int e = tid; e < o * o; e += blockDim.x)
             invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
     }
-    if (tid == 0) {
-        s_det = make_double2(1.0, 0.0);
-        s_zero = 0;
-    }
     __syncthreads();
 
-    // One pivot loop for both factorisations of m, three barriers a step:
-    //   LU with partial pivoting (det(m) only; double-float with DF, else
-    //   binary64), pivots by warp 0;
-    //   fp32 Gauss-Jordan inverse of the copy, pivots by warp 1; its pivot
-    //   row k is scaled by 1/pivot in the next step's first phase (rows
-    //   r != k eliminate with the unscaled row times 1/pivot meanwhile).
-    //   The row multipliers (LU: m[r][k] / pivot for r > k; Gauss-Jordan:
-    //   mf[r][k] / pivot for r != k) are formed once a step, during the row
-    //   swaps, which leave column k alone: the multipliers read it with the
-    //   swap applied (it is not read again).  Element loops advance (row,
-    //   column) incrementally instead of dividing per element.
-    __shared__ int s_piv2;
-    __shared__ float2 s_rpf2[2];
+    // The two factorisations of m, each by one warp with no block barrier
+    // inside (the other warps go on to the barrier below):
+    //   warp 0: LU with partial pivoting for det(m) only (double-float with
+    //     DF, else binary64): rows are swapped and eliminated from column k
+    //     on, the multipliers of step k are formed by their rows' lanes;
+    //   warp 1: fp32 Gauss-Jordan with partial pivoting on [mf | I], giving
+    //     invf = m^-1 for G_half.
+    // Pivots: the largest |Re| + |Im| of the column (ties to the lower row).
     constexpr int OMAX = MA <= 4 ? 32 : 64;   // nocc bound of this instantiation (AG = 256 / o >= o / MA)
     __shared__ float4 s_lmul[OMAX];           // LU multipliers (double-float, or binary64 as double2)
     __shared__ float2 s_fmul[OMAX];           // Gauss-Jordan multipliers
-    const int o2 = 2 * o;
-    const int gj_sr = blockDim.x / o2, gj_sj = blockDim.x % o2, gj_r0 = tid / o2, gj_j0 = tid % o2;
-    for (int k = 0; k <= o; ++k) {
-        if (k < o && wid == 0) {
-            double best = -1.0;
+    if (wid == 0) {
+        double2 det = make_double2(1.0, 0.0);
+        bool zero = false;
+        for (int k = 0; k < o && !zero; ++k) {
+            float best = -1.f;
             int bi = k;
             for (int r = k + lane; r < o; r += 32) {
-                double v;
+                float v;
                 if (DF) {
                     const float4 x = md[r * o + k];
-                    v = (double)x.x * x.x + (double)x.z * x.z;
+                    v = fabsf(x.x) + fabsf(x.z);
                 } else {
-                    v = cabs2(m[r * o + k]);
+                    const double2 x = m[r * o + k];
+                    v = (float)(fabs(x.x) + fabs(x.y));
                 }
                 if (v > best) { best = v; bi = r; }
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const float ob = __shfl_xor_sync(0xffffffffu, best, off);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
-            if (lane == 0) {
-                s_piv = bi;
-                double2 piv;
-                if (DF) {
-                    const float4 p = md[bi * o + k];
-                    piv = make_double2((double)p.x + (double)p.y, (double)p.z + (double)p.w);
-                    s_rpd = zdf_rcp(p);
-                } else {
-                    piv = m[bi * o + k];
-                    s_rp = cdiv(make_double2(1.0, 0.0), piv);
+            if (bi != k)  // 16-byte entries: binary64 complex, or double-float
+                for (int j = k + lane; j < o; j += 32) {
+                    const double2 t = m[k * o + j];
+                    m[k * o + j] = m[bi * o + j];
+                    m[bi * o + j] = t;
                 }
-                const double2 d = cmul(s_det, piv);
-                s_det = (bi != k) ? make_double2(-d.x, -d.y) : d;
-                if (piv.x == 0.0 && piv.y == 0.0) s_zero = 1;
+            __syncwarp();
+            double2 piv;
+            float4 rpd = make_float4(0.f, 0.f, 0.f, 0.f);
+            double2 rp = make_double2(0.0, 0.0);
+            if (DF) {
+                const float4 pk = md[k * o + k];
+                piv = make_double2((double)pk.x + (double)pk.y, (double)pk.z + (double)pk.w);
+                if (pk.x == 0.f && pk.y == 0.f && pk.z == 0.f && pk.w == 0.f) zero = true;
+                else rpd = zdf_rcp(pk);
+            } else {
+                piv = m[k * o + k];
+                if (piv.x == 0.0 && piv.y == 0.0) zero = true;
+                else rp = cdiv(make_double2(1.0, 0.0), piv);
             }
-        } else if (k < o && wid == 1) {
+            if (lane == 0) {
+                const double2 d = cmul(det, piv);
+                det = (bi != k) ? make_double2(-d.x, -d.y) : d;
+            }
+            if (zero) break;
+            for (int r = k + 1 + lane; r < o; r += 32) {  // multipliers, by their rows' lanes
+                if (DF) s_lmul[r] = zdf_mul(md[r * o + k], rpd);
+                else ((double2*)s_lmul)[r] = cmul(m[r * o + k], rp);
+            }
+            __syncwarp();
+            for (int j = k + 1 + lane; j < o; j += 32) {  // columns by lanes, rows in turn
+                if (DF) {
+                    const float4 ukj = md[k * o + j];
+                    for (int r = k + 1; r < o; ++r) md[r * o + j] = zdf_sub(md[r * o + j], zdf_mul(s_lmul[r], ukj));
+                } else {
+                    const double2 ukj = m[k * o + j];
+                    for (int r = k + 1; r < o; ++r)
+                        m[r * o + j] = csub(m[r * o + j], cmul(((const double2*)s_lmul)[r], ukj));
+                }
+            }
+            __syncwarp();
+        }
+        // an exactly zero pivot: m is singular and det(m) is exactly 0 (as LAPACK's LU gives it)
+        if (lane == 0 && ovlp_out) ovlp_out[w] = zero ? make_double2(0.0, 0.0) : cmul(det, det);
+    } else if (wid == 1) {
+        for (int k = 0; k < o; ++k) {
             float best = -1.f;
             int bi = k;
             for (int r = k + lane; r < o; r += 32) {
                 const float2 v = mf[r * o + k];
-                const float a = v.x * v.x + v.y * v.y;
+                const float a = fabsf(v.x) + fabsf(v.y);
                 if (a > best) { best = a; bi = r; }
             }
 #pragma unroll
@@ -718,88 +735,37 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
-            if (lane == 0) {
-                s_piv2 = bi;
-                const float2 v = mf[bi * o + k];
-                const float den = v.x * v.x + v.y * v.y;
-                s_rpf2[k & 1] = make_float2(v.x / den, -v.y / den);
-            }
-        } else if (k > 0 && tid >= 64) {
-            // scale the previous Gauss-Jordan pivot row (columns > k-1 of the copy, all of the inverse)
-            const float2 rp = s_rpf2[(k - 1) & 1];
-            for (int j = tid - 64; j < 2 * o; j += blockDim.x - 64) {
+            // swap rows k and bi (columns k.. of the copy, all of the inverse), then scale row k by 1 / pivot
+            const float2 pv = mf[bi * o + k];
+            const float den = pv.x * pv.x + pv.y * pv.y;
+            const float2 rp = make_float2(pv.x / den, -pv.y / den);
+            __syncwarp();  // every lane has read the pivot before row k is rewritten
+            for (int j = lane; j < 2 * o; j += 32) {
                 float2* X = j < o ? mf : invf;
                 const int jj = j < o ? j : j - o;
-                if (j < o && jj <= k - 1) continue;
-                const float2 v = X[(k - 1) * o + jj];
-                X[(k - 1) * o + jj] = make_float2(v.x * rp.x - v.y * rp.y, v.x * rp.y + v.y * rp.x);
+                if (j < o && jj < k) continue;
+                const float2 a = X[k * o + jj], b = X[bi * o + jj];
+                if (bi != k) X[bi * o + jj] = a;
+                X[k * o + jj] = make_float2(b.x * rp.x - b.y * rp.y, b.x * rp.y + b.y * rp.x);
             }
-        }
-        __syncthreads();
-        if (k == o) break;
-        const int p = s_piv, p2 = s_piv2;
-        const float2 rpf = s_rpf2[k & 1];
-        for (int j = tid; j < 3 * o; j += blockDim.x) {  // row swaps outside column k
-            if (j < o) {
-                if (p != k && j != k) {  // 16-byte entries: binary64 complex, or double-float
-                    const double2 t = m[k * o + j];
-                    m[k * o + j] = m[p * o + j];
-                    m[p * o + j] = t;
-                }
-            } else if (p2 != k && j != o + k) {
-                float2* X = j < 2 * o ? mf : invf;
-                const int jj = j < 2 * o ? j - o : j - 2 * o;
-                const float2 t = X[k * o + jj];
-                X[k * o + jj] = X[p2 * o + jj];
-                X[p2 * o + jj] = t;
-            }
-        }
-        for (int r = tid; r < 2 * o; r += blockDim.x) {  // multipliers from column k, rows swapped
-            if (r < o) {
-                if (r > k) {
-                    const int src = r == p ? k : r;
-                    if (DF) s_lmul[r] = zdf_mul(md[src * o + k], s_rpd);
-                    else ((double2*)s_lmul)[r] = cmul(m[src * o + k], s_rp);
-                }
-            } else if (r - o != k) {
-                const int src = r - o == p2 ? k : r - o;
-                const float2 f0 = mf[src * o + k];
-                s_fmul[r - o] = make_float2(f0.x * rpf.x - f0.y * rpf.y, f0.x * rpf.y + f0.y * rpf.x);
-            }
-        }
-        __syncthreads();
-        const int rem = o - k - 1;
-        if (rem > 0 && tid < rem * rem) {
-            const int sr = blockDim.x / rem, sj = blockDim.x % rem;
-            int rr = tid / rem, jj = tid % rem;
-            for (int e = tid; e < rem * rem; e += blockDim.x) {
-                const int r = k + 1 + rr, j = k + 1 + jj;
-                if (DF) md[r * o + j] = zdf_sub(md[r * o + j], zdf_mul(s_lmul[r], md[k * o + j]));
-                else m[r * o + j] = csub(m[r * o + j], cmul(((const double2*)s_lmul)[r], m[k * o + j]));
-                rr += sr;
-                jj += sj;
-                if (jj >= rem) { jj -= rem; ++rr; }
-            }
-        }
-        {
-            int r = gj_r0, j = gj_j0;
-            for (int e = tid; e < o * o2; e += blockDim.x) {
-                if (r != k && !(j < o && j <= k)) {
-                    float2* X = j < o ? mf : invf;
-                    const int jj = j < o ? j : j - o;
-                    const float2 f = s_fmul[r];
-                    const float2 v = X[k * o + jj], x = X[r * o + jj];
+            __syncwarp();
+            for (int r = lane; r < o; r += 32) s_fmul[r] = mf[r * o + k];  // multipliers (row k's is 1)
+            __syncwarp();
+            for (int j = lane; j < 2 * o; j += 32) {  // eliminate column k from every other row
+                float2* X = j < o ? mf : invf;
+                const int jj = j < o ? j : j - o;
+                if (j < o && jj <= k) continue;
+                const float2 v = X[k * o + jj];
+                for (int r = 0; r < o; ++r) {
+                    if (r == k) continue;
+                    const float2 f = s_fmul[r], x = X[r * o + jj];
                     X[r * o + jj] = make_float2(x.x - (f.x * v.x - f.y * v.y), x.y - (f.x * v.y + f.y * v.x));
                 }
-                r += gj_sr;
-                j += gj_sj;
-                if (j >= o2) { j -= o2; ++r; }
             }
+            __syncwarp();
         }
-        __syncthreads();
     }
-    // an exactly zero pivot: m is singular and det(m) is exactly 0 (as LAPACK's LU gives it)
-    if (tid == 0 && ovlp_out) ovlp_out[w] = s_zero ? make_double2(0.0, 0.0) : cmul(s_det, s_det);
+    __syncthreads();
 
     // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
     __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
@@ -814,7 +780,7 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
         __syncthreads();
         for (int e = tid; e < rows * o; e += blockDim.x) {
             const double2 x = Wp[(size_t)i0 * o + e];
-            wf[e] = make_float2((float)x.x, (float)x.y);
+            wf[e] = make_float2(d2f_trunc(x.x), d2f_trunc(x.y));
         }
         __syncthreads();
     }
@@ -1130,7 +1096,7 @@ __global__ void __launch_bounds__(256, 2) k_cholqr2(int n, int o, const double2*
     for (int e = threadIdx.x; e < n * o; e += blockDim.x) {
         const size_t d = (size_t)(e % o) * ld + e / o;
         const float2 h = Ah[d], l = Al[d];
-        Wo[e] = make_double2((double)h.x + (double)l.x, (double)h.y + (double)l.y);
+        Wo[e] = make_double2(f2d_exact(h.x) + f2d_exact(l.x), f2d_exact(h.y) + f2d_exact(l.y));
     }
     if (det_out && threadIdx.x == 0) det_out[w] = make_double2(s_det, 0.0);
 }

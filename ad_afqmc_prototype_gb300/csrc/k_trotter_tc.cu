@@ -29,7 +29,7 @@
 // The running sum U = W + (E - I) W + sum_k T_k (= out after the last V
 // product) is kept in fp32 registers; W' = W + ((U - W32) + (E - I) out) is
 // formed with one binary64 add per entry, W32 being W cut to fp32 by integer
-// operations (the same bits in the first and the last use).  Lane (c, p, q)
+// operations (d2f_trunc: the same bits in the first and the last use).  Lane (c, p, q)
 // of the accumulator belongs to the epilogue thread that holds TMEM lane
 // 4c + 2p + q; the four lanes of an orbital c are in one warp and exchange
 // the piece sums and the Re/Im parts by shuffles.  U(j, c, q) is held by
@@ -113,26 +113,6 @@ __device__ __forceinline__ uint32_t tt_piece2(float a, float b, int p) {
     const __nv_bfloat162 m = __floats2bfloat162_rn(a - hf.x, b - hf.y);
     const __nv_bfloat162 x = p ? m : h;
     return *(const uint32_t*)&x;
-}
-// W entry cut to fp32 (24 significant bits, toward zero) by integer
-// operations only (no binary64 instruction on any path): magnitudes below
-// the fp32 normal range give a signed zero, above it infinity, nan a nan.
-__device__ __forceinline__ float tt_w32(double x) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
-    const unsigned e = (h >> 20) & 0x7ffu, sign = h & 0x80000000u;
-    const unsigned nrm = sign | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29));
-    const unsigned big = ((e == 0x7ffu) && ((h & 0xfffffu) | l)) ? 0x7fc00000u : (sign | 0x7f800000u);
-    return __uint_as_float(e < 897u ? sign : (e > 1150u ? big : nrm));
-}
-// Exact fp32 -> binary64 by integer operations only (fp32 subnormals give a
-// signed zero; inf and nan keep their class).
-__device__ __forceinline__ double tt_f2d(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xffu;
-    const unsigned long long ex = e == 0u ? 0ull : (e == 0xffu ? 2047ull : (unsigned long long)(e + 896u));
-    const unsigned long long m = e == 0u ? 0ull : (unsigned long long)(u & 0x7fffffu) << 29;
-    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (ex << 52) | m));
 }
 
 // 16 and 8 consecutive fp32 columns of this warp's lanes; the wait is part
@@ -321,7 +301,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                     float t[4], b[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        t[u] = tt_w32(wv[4 * cc + u]);
+                        t[u] = d2f_trunc(wv[4 * cc + u]);
                         b[u] = sg * __shfl_xor_sync(0xffffffffu, t[u], 1);
                     }
                     U[2 * k] = p ? t[1] : t[0];
@@ -425,7 +405,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                 for (int m = 0; m < 8; ++m) {
                     const int j = j0 + 16 * kb + 2 * m + p;
                     if (valid && 4 * kb + (m >> 1) < nch && j < n)
-                        Wo[(size_t)2 * j * o] = wv[m] + tt_f2d(U[8 * kb + m] - tt_w32(wv[m]));
+                        Wo[(size_t)2 * j * o] = wv[m] + f2d_exact(U[8 * kb + m] - d2f_trunc(wv[m]));
                 }
             }
         }
