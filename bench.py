@@ -130,9 +130,10 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64", n_terms=6):
     """(work per launch, pipe) of each timed phase.  FP64 form: algorithmic
     real flops.  Mixed forms: the tensor-core phases count the flops of the
     bf16 split operands (2 M N K with K the split row length; the energy GEMM
-    without the padding of its exchange-fused layout; the three-section Taylor
-    products 3 x 2 n (2 nocc) (2 n) per V product and 3 x 2 n (2 nocc) n per
-    E - I product), the exchange step the bytes it must read.  The overlap,
+    without the padding of its exchange-fused layout; the Taylor kernel's
+    128 x N x 16 MMAs, N = norb rounded up to 16, two a K step (V's hi and mid
+    pieces) over K = 2 N per V product and N per E - I product: 256 (4
+    n_terms + 4) N^2 per walker), the exchange step the bytes it must read.  The overlap,
     Green's function and QR phases of the mixed forms run double-float
     arithmetic on the fp32 pipe ("df32"): no algorithmic-flop roofline."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
@@ -157,7 +158,8 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64", n_terms=6):
             work["e_exchange"] = (4.0 * (2 * o * W) * (G * o), "hbm")
         work["trotter"] = ((48.0 + 8.0) * n * n * o * W, "fp32")
         if precision == "mixed_fast" and n % 8 == 0 and n <= 256 and o <= 32:  # tensor-core Taylor products
-            work["trotter"] = (3.0 * (8.0 * n_terms + 8.0) * n * n * o * W, "tensor")
+            nn = (n + 15) // 16 * 16
+            work["trotter"] = (256.0 * (4 * n_terms + 4) * nn * nn * W, "tensor")
         for k in ("overlap", "green", "qr"):
             work[k] = (work[k][0], "df32")
     return work

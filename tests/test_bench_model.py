@@ -16,7 +16,8 @@ def test_phase_work_pipes_per_precision():
     fast = bench.phase_work(200, 30, 1000, 4096, precision="mixed_fast")
     assert fast["trotter"][1] == "tensor"
     # three bf16 sections of 6 V products (2n x 2o x 2n) and 2 E - I products (2n x 2o x n) per walker
-    assert fast["trotter"][0] == pytest.approx(3 * (6 * 2 * 200 * 60 * 400 + 2 * 2 * 200 * 60 * 200) * 4096)
+    # 128 x 208 x 16 MMAs, two a K step: 6 V products of 26 K steps, 2 E - I products of 13
+    assert fast["trotter"][0] == pytest.approx((6 * 26 + 2 * 13) * 2 * (2 * 128 * 208 * 16) * 4096)
     for k in ("overlap", "green", "qr"):
         assert fast[k][1] == "df32"
     for k in ("vbuild_gemm", "fb_gemm", "e_gemm"):
@@ -39,7 +40,9 @@ def test_roofline_is_algorithmic_with_executed_beside(monkeypatch):
     flops_block = (8 * 6 + 8) * 200 ** 2 * 30 * 4096 * bench.STEPS_PER_BLOCK
     assert r["achieved"] == pytest.approx(flops_block / (49.0 / 2 / 1000.0) / 1e12, rel=1e-4)
     assert math.isclose(r["frac"], r["achieved"] / r["peak"], rel_tol=1e-3)
-    assert r["executed_achieved"] == pytest.approx(3 * r["achieved"], rel=1e-3)
+    # executed: the Taylor kernel's MMAs (128 rows, N = 208, hi and mid pieces of V)
+    assert r["executed_achieved"] == pytest.approx(r["achieved"] * work["trotter"][0] / alg["trotter"], rel=1e-3)
+    assert work["trotter"][0] / alg["trotter"] == pytest.approx(7168 * 208 ** 2 / (56 * 200 ** 2 * 30), rel=1e-9)
     # the share excludes the composite energy phase that encloses e_gemm
     assert r["share_of_step"] == pytest.approx(49.0 / (30 + 49 + 44 + 20 + 17), rel=1e-3)
     # the double-float phases are measured against the fp32 pipe they run on
