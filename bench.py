@@ -598,6 +598,12 @@ def run_cv(args, env, st, W, world, seed, ctr, chain_blocks=40, run_steps=400):
         engine.block(prob, params, st, seed, ctr, cv=cv.block_args(W))
         cv.after_block()
         ctr += STEPS_PER_BLOCK + 1
+    # one throwaway epoch on a second network first: the torch operations the
+    # training uses (randperm on the device, gathers) are compiled for this GPU
+    # on first use, a one-time cost that is not part of the training
+    warm = ExchangeControlVariate(hidden=256, sample_fraction=1 / 8, seed=seed + 1)
+    warm.data_x, warm.data_y = cv.data_x, cv.data_y
+    warm.fit(epochs=1, batch=1024, lr=1e-3)
     torch.cuda.synchronize()
     t0 = time.time()
     losses = cv.fit(epochs=20, batch=1024, lr=1e-3)
