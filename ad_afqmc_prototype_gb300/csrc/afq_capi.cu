@@ -127,7 +127,17 @@ struct StepWS {
     float2* tsum;       // Wc*n*o: fp32 sum of the Taylor terms of a chunk
     __nv_bfloat16* esplit;  // 2 n*n: E - I as bf16 hi, mid (tensor-core Taylor products)
     float2* csplit;     // n*o: trial orbitals as (hi, lo) fp32 pairs (double-float overlap)
+    // m = C^T W on the tensor cores from integer digit slices (k_ozaki.cu), nocc <= 32
+    __nv_bfloat16* ozA;  // 2 o W x Kt: the walkers' digit rows
+    __nv_bfloat16* ozB;  // 8 o x Kt: the trial's digit rows
+    int* ozE;            // 2 o W: row exponents
+    int* ozF;            // o: column exponents
+    float2* ozM;         // W o o x 2: m as double-float pairs
 };
+
+// The tensor-core m of the mixed forms: nocc <= 32 and the digit sums exact
+// (7 norb 2^12 < 2^24).
+static bool oz_supported(const afq_dims* d) { return d->nocc <= 32 && d->norb <= 584; }
 
 static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
     const size_t W = d->n_walkers, n = d->norb, o = d->nocc, G = d->nchol;
@@ -148,6 +158,14 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         s.tsum = a.take<float2>(Wc * n * o);
         s.esplit = a.take<__nv_bfloat16>(2 * n * n);
         s.csplit = a.take<float2>(n * o);
+        if (oz_supported(d)) {
+            const OzDims z = oz_dims((int)n, (int)o);
+            s.ozA = a.take<__nv_bfloat16>((size_t)z.rows * W * z.Kt);
+            s.ozB = a.take<__nv_bfloat16>((size_t)z.Nb * z.Kt);
+            s.ozE = a.take<int>((size_t)z.rows * W);
+            s.ozF = a.take<int>(64);
+            s.ozM = a.take<float2>(W * o * o * 2);
+        }
     } else {
         s.green = a.take<double2>(W * o * n);
         s.fb = a.take<double2>(W * G);
@@ -283,6 +301,23 @@ static SplitOut fb_split(const afq_dims* d, const StepWS& ws) {
     return so;
 }
 
+// The mixed forms' overlap pass: m = C^T W on the tensor cores when the
+// workspace holds the digit buffers (else in double-float inside the
+// overlap kernel), then the LU, the inverse and G_half per walker.
+static int overlap_mixed(const afq_problem* pb, double2* walk, double2* ovl, SplitOut split, double2* green_out,
+                         const StepWS& ws, cudaStream_t s) {
+    const afq_dims* d = &pb->dims;
+    const int W = d->n_walkers, n = d->norb, o = d->nocc;
+    const double2* mo = (const double2*)pb->mo_coeff;
+    if (ws.ozA) {
+        AFQ_TRY(launch_oz_split_c(n, o, mo, ws.ozB, ws.ozF, s));
+        AFQ_TRY(launch_oz_split_w(W, n, o, walk, ws.ozA, ws.ozE, s));
+        AFQ_TRY(launch_tc_gemm_oz(W, n, o, ws.ozA, ws.ozB, ws.ozE, ws.ozF, ws.ozM, ws.status, s));
+        return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit, (const float4*)ws.ozM);
+    }
+    return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit);
+}
+
 // green_ready: ws.Ag already holds the split G_half of the current walkers
 // (written by the previous step's overlap kernel or by the overlap refresh
 // after a QR inside the same block).
@@ -301,7 +336,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     // force bias: G_half split straight from the Green's function kernel
     if (!green_ready) {
         AFQ_PHASE("green", s);
-        AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, nullptr, fb_split(d, ws), s, nullptr, ws.csplit));
+        AFQ_TRY(overlap_mixed(pb, walk, nullptr, fb_split(d, ws), nullptr, ws, s));
     }
     { AFQ_PHASE("fb_gemm", s);
       AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.fbm, G, ws.status, s,
@@ -340,7 +375,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     }
     // overlaps, and the next step's force-bias operand from the same factorisation
     { AFQ_PHASE("overlap", s);
-      AFQ_TRY(launch_overlap_split(W, n, o, mo, walk, ws.ovl_new, fb_split(d, ws), s, green_out, ws.csplit)); }
+      AFQ_TRY(overlap_mixed(pb, walk, ws.ovl_new, fb_split(d, ws), green_out, ws, s)); }
     AFQ_PHASE("weight_update", s);
     return launch_weight_update(W, p, pb->sqrt_dt, pb->dt, make_double2(pb->h0_prop_re, pb->h0_prop_im),
                                 ws.shift_term, ws.fb_term, ws.ovl_new, st->weights, (double2*)st->overlaps,
@@ -456,7 +491,8 @@ static int step_impl(const afq_problem* pb, const afq_params* p, const afq_state
 // does (prop/blocks.py:53-57).
 static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cudaStream_t s,
                                   const StepWS* ws = nullptr, double2* green_out = nullptr,
-                                  const float2* cs = nullptr, double2* det_buf = nullptr, bool green_kept = false) {
+                                  const float2* cs = nullptr, double2* det_buf = nullptr, bool green_kept = false,
+                                  const StepWS* green_ws = nullptr) {
     const afq_dims* d = &pb->dims;
     double2* walk = (double2*)st->walkers;
     const bool keep = is_mixed(d->precision) && det_buf && (ws || green_kept);
@@ -472,9 +508,11 @@ static int orthonormalize_refresh(const afq_problem* pb, const afq_state* st, cu
     }
     AFQ_PHASE(green_out ? "green" : "overlap", s);
     if (ws && is_mixed(d->precision))
-        return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
-                                    (double2*)st->overlaps, fb_split(d, *ws), s, nullptr, ws->csplit);
+        return overlap_mixed(pb, walk, (double2*)st->overlaps, fb_split(d, *ws), nullptr, *ws, s);
     // the three-section energy resolves less than fp32: its Green's function in fp32
+    // (with m from the same tensor-core pass as every other overlap of the block)
+    if (green_out && d->precision == AFQ_PREC_MIXED_FAST && green_ws)
+        return overlap_mixed(pb, walk, (double2*)st->overlaps, SplitOut{}, green_out, *green_ws, s);
     if (green_out && d->precision == AFQ_PREC_MIXED_FAST)
         return launch_overlap_split(d->n_walkers, d->norb, d->nocc, (const double2*)pb->mo_coeff, walk,
                                     (double2*)st->overlaps, SplitOut{}, s, green_out, cs);
@@ -917,7 +955,7 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
     if (cvmode == AFQ_CV_OFF) {
         AFQ_TRY(orthonormalize_refresh(pb, st, s, nullptr, ws.green,
                                        is_mixed(d->precision) ? ws.step.csplit : nullptr, ws.step.ovl_new,
-                                       green_kept));
+                                       green_kept, &ws.step));
         // prop/blocks.py:59-79
         AFQ_TRY(energy_impl(pb, st, ws, s, true));
         AFQ_PHASE("block_measure", s);
@@ -934,8 +972,7 @@ int afq_block_cv(const afq_problem* pb, const afq_params* p, const afq_state* st
             { AFQ_PHASE("qr", s); AFQ_TRY(launch_cholqr2(W, n, o, walk, walk, nullptr, s)); }
             // overlaps, the Green's function and its force-bias operand in one pass; the GEMM gives c_g
             { AFQ_PHASE("green", s);
-              AFQ_TRY(launch_overlap_split(W, n, o, (const double2*)pb->mo_coeff, walk, (double2*)st->overlaps,
-                                           fb_split(d, ws.step), s, ws.green, ws.step.csplit)); }
+              AFQ_TRY(overlap_mixed(pb, walk, (double2*)st->overlaps, fb_split(d, ws.step), ws.green, ws.step, s)); }
         }
         { AFQ_PHASE("fb_gemm", s);
           AFQ_TRY(launch_tc_gemm_tn_drain(2 * W, G, L.Kt_F, ws.step.Ag, L.Kt_F, lb.Bf, L.Kt_F, ws.step.fbm, G,

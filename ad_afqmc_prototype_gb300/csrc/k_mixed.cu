@@ -553,12 +553,15 @@ __device__ __forceinline__ float4 zdf_rcp(float4 p) {  // 1 / (a + i b) = (a - i
     return make_float4(re.x, re.y, im.x, im.y);
 }
 
-template <int MA, bool STAGE_W, bool DF>
+// MIN: m (double-float) is given in m_in[(w o + a) o + b] (k_ozaki.cu) instead
+// of formed here.
+template <int MA, bool STAGE_W, bool DF, bool MIN = false>
 __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
                                                        double2* __restrict__ ovlp_out, SplitOut split,
                                                        double2* __restrict__ green_out,
-                                                       const float2* __restrict__ cs) {
+                                                       const float2* __restrict__ cs,
+                                                       const float4* __restrict__ m_in) {
     extern __shared__ double2 smd[];
     double2* m = smd;                              // o x o binary64 (LU in place)
     float4* md = (float4*)smd;                     // DF: the same storage as double-float pairs
@@ -569,7 +572,15 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
-    if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
+    if (MIN) {  // m given
+        const float4* mw = m_in + (size_t)w * o * o;
+        for (int e = tid; e < o * o; e += blockDim.x) {
+            const float4 x = mw[e];
+            md[e] = x;
+            mf[e] = make_float2(x.x, x.z);
+            invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
+        }
+    } else if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
         const int AG = blockDim.x / o;
         const int b = tid % o, ag = tid / o;
         float2 s2[MA], e2[MA];  // (Re, Im) sums and their error terms
@@ -832,28 +843,33 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
 }
 
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
-                         SplitOut split, cudaStream_t s, double2* green_out, const float2* cs) {
+                         SplitOut split, cudaStream_t s, double2* green_out, const float2* cs, const float4* m_in) {
     if (W <= 0) return AFQ_OK;
     const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
     const size_t wbytes = (size_t)n * o * sizeof(float2);
     const size_t dfbytes = 2 * (size_t)OS_CH * o * sizeof(float2);
-    const bool df = cs != nullptr;                          // double-float m, W staged in chunks
+    const bool df = cs != nullptr || m_in != nullptr;        // double-float m, W staged in chunks
     const bool stage = df || base + wbytes <= 160 * 1024;  // else read W from global in the last loop
     const size_t smem = base + (df ? dfbytes : stage ? wbytes : 0);
     const int ag = 256 / o, ma = (o + ag - 1) / ag;
 #define AFQ_OS(MAV)                                                                                              \
     do {                                                                                                         \
-        if (df) {                                                                                                \
+        if (m_in) {                                                                                              \
+            AFQ_TRY(smem_attr(k_overlap_split<MAV, true, true, true>, smem));                                    \
+            k_overlap_split<MAV, true, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split,       \
+                                                                       green_out, cs, m_in);                     \
+        } else if (df) {                                                                                         \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, true, true>, smem));                                          \
-            k_overlap_split<MAV, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, cs); \
+            k_overlap_split<MAV, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, cs, \
+                                                                 nullptr);                                       \
         } else if (stage) {                                                                                      \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, true, false>, smem));                                         \
             k_overlap_split<MAV, true, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out,  \
-                                                                  nullptr);                                      \
+                                                                  nullptr, nullptr);                             \
         } else {                                                                                                 \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, false, false>, smem));                                        \
             k_overlap_split<MAV, false, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, \
-                                                                   nullptr);                                     \
+                                                                   nullptr, nullptr);                            \
         }                                                                                                        \
     } while (0)
     if (ma <= 1) AFQ_OS(1);
