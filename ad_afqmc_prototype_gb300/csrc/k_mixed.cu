@@ -553,15 +553,12 @@ __device__ __forceinline__ float4 zdf_rcp(float4 p) {  // 1 / (a + i b) = (a - i
     return make_float4(re.x, re.y, im.x, im.y);
 }
 
-// MIN: m (double-float) is given in m_in[(w o + a) o + b] (k_ozaki.cu) instead
-// of formed here.
-template <int MA, bool STAGE_W, bool DF, bool MIN = false>
+template <int MA, bool STAGE_W, bool DF>
 __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
                                                        double2* __restrict__ ovlp_out, SplitOut split,
                                                        double2* __restrict__ green_out,
-                                                       const float2* __restrict__ cs,
-                                                       const float4* __restrict__ m_in) {
+                                                       const float2* __restrict__ cs) {
     extern __shared__ double2 smd[];
     double2* m = smd;                              // o x o binary64 (LU in place)
     float4* md = (float4*)smd;                     // DF: the same storage as double-float pairs
@@ -572,15 +569,7 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double2* Wp = walkers + (size_t)w * n * o;
 
-    if (MIN) {  // m given
-        const float4* mw = m_in + (size_t)w * o * o;
-        for (int e = tid; e < o * o; e += blockDim.x) {
-            const float4 x = mw[e];
-            md[e] = x;
-            mf[e] = make_float2(x.x, x.z);
-            invf[e] = make_float2((e / o) == (e % o) ? 1.f : 0.f, 0.f);
-        }
-    } else if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
+    if (DF) {  // m in double-float from the split of W, staged OS_CH rows at a time
         const int AG = blockDim.x / o;
         const int b = tid % o, ag = tid / o;
         float2 s2[MA], e2[MA];  // (Re, Im) sums and their error terms
@@ -842,34 +831,249 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
     }
 }
 
+// The overlap, its Green's function and the force-bias operand of the mixed
+// forms from a given double-float m = C^T W (k_ozaki.cu; meas/rhf.py:15-33),
+// one CTA of 256 threads per walker:
+//   warps 0-3: LU of m with partial pivoting in double-float, for det(m)
+//     (overlap = det(m)^2 for the restricted walker);
+//   warps 4-7: fp32 Gauss-Jordan on [m | I], for m^-1 (G_half's factor).
+// Each step of both runs four threads a row with one barrier of the group:
+// rows are addressed through a permutation (no row swaps), the pivot of step
+// k + 1 (the largest |Re| + |Im| of the column, ties to the lower row) is
+// found while step k updates column k + 1 (a shared-memory atomicMax over
+// (value, -row) keys, three in rotation), and Gauss-Jordan leaves each pivot
+// row unscaled (row k of the inverse is scaled by 1 / pivot_k at the end,
+// the multipliers carry the factor meanwhile).  Then G_half = W m^-1 in fp32
+// by all warps, W staged OG_CH rows a time, two rows by four columns a thread.
+constexpr int OG_CH = 64;  // rows of W per G_half staging chunk
+
+__device__ __forceinline__ unsigned long long piv_key(float v, int r) {  // v >= 0: its bits order as values
+    return ((unsigned long long)__float_as_uint(v) << 32) | (unsigned)(0xffff - r);
+}
+__device__ __forceinline__ int piv_row(unsigned long long key) { return 0xffff - (int)(key & 0xffffu); }
+__host__ __device__ constexpr int og_xs(int o) {  // float2 entries of [m | I], and of the packed inverse
+    return 2 * o * o > o * ((o + 3) & ~3) ? 2 * o * o : o * ((o + 3) & ~3);
+}
+__host__ __device__ constexpr int og_a16(int o) {  // 16-byte units of the region of m, later of staged W
+    return o * o > (OG_CH * (o | 1) + 1) / 2 ? o * o : (OG_CH * (o | 1) + 1) / 2;
+}
+__device__ __forceinline__ void group_bar(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+__global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float4* __restrict__ m_in,
+                                                       const double2* __restrict__ walkers,
+                                                       double2* __restrict__ ovlp_out, SplitOut split,
+                                                       double2* __restrict__ green_out) {
+    extern __shared__ float4 smf[];
+    const int o2 = 2 * o, ws = o | 1, IS = (o + 3) & ~3;
+    float4* md = smf;                       // o x o double-float m, LU in place
+    float2* wf = (float2*)smf;              // then OG_CH x ws staged fp32 rows of W
+    float2* X = (float2*)(smf + og_a16(o)); // o x 2o fp32 [m | I], Gauss-Jordan in place
+    float2* inv = X;                        // then o x IS: row a of m^-1
+    __shared__ unsigned long long s_key[2][3];
+    __shared__ int s_perm[2][2][32];        // [LU, GJ][ping-pong][logical row] -> physical row
+    __shared__ int s_pf[32];                // GJ: physical row of logical row k from step k on
+    __shared__ float2 s_rp[32];             // GJ: 1 / pivot_k
+    const int w = blockIdx.x, tid = threadIdx.x;
+
+    const float4* mw = m_in + (size_t)w * o * o;
+    for (int e = tid; e < o * o; e += blockDim.x) {
+        const float4 x = mw[e];
+        const int r = e / o, c = e - r * o;
+        md[e] = x;
+        X[r * o2 + c] = make_float2(x.x, x.z);
+        X[r * o2 + o + c] = make_float2(r == c ? 1.f : 0.f, 0.f);
+    }
+    if (tid < 32) s_perm[0][0][tid] = s_perm[1][0][tid] = tid;
+    if (tid < 6) (&s_key[0][0])[tid] = 0ull;
+    __syncthreads();
+    if (tid < o) {  // the pivot keys of step 0 (column 0; the same fp32 heads for both)
+        const float4 x = md[tid * o];
+        const unsigned long long key = piv_key(fabsf(x.x) + fabsf(x.z), tid);
+        atomicMax(&s_key[0][0], key);
+        atomicMax(&s_key[1][0], key);
+    }
+    __syncthreads();
+
+    if (tid < 128) {  // LU (double-float)
+        const int rr = tid >> 2, q = tid & 3;
+        double2 det = make_double2(1.0, 0.0);
+        bool zero = false;
+        for (int k = 0; k < o; ++k) {
+            const int* pc = s_perm[0][k & 1];
+            int* pn = s_perm[0][(k + 1) & 1];
+            const int bi = piv_row(s_key[0][k % 3]);
+            const int pr = pc[bi];
+            const float4 pk = md[pr * o + k];
+            // an exactly zero pivot: m is singular and det(m) is exactly 0 (as LAPACK's LU gives it)
+            if (pk.x == 0.f && pk.y == 0.f && pk.z == 0.f && pk.w == 0.f) { zero = true; break; }
+            if (tid == 0) {
+                const double2 d = cmul(det, make_double2((double)pk.x + (double)pk.y, (double)pk.z + (double)pk.w));
+                det = bi != k ? make_double2(-d.x, -d.y) : d;
+                s_key[0][(k + 2) % 3] = 0ull;
+            }
+            const float4 rpd = zdf_rcp(pk);
+            const int r = k + 1 + rr;
+            if (r < o) {
+                const int p = r == bi ? pc[k] : pc[r];
+                if (q == 0) pn[r] = p;
+                const float4 l = zdf_mul(md[p * o + k], rpd);
+                for (int j = k + 1 + q; j < o; j += 4) {
+                    const float4 v = zdf_sub(md[p * o + j], zdf_mul(l, md[pr * o + j]));
+                    md[p * o + j] = v;
+                    if (j == k + 1) atomicMax(&s_key[0][(k + 1) % 3], piv_key(fabsf(v.x) + fabsf(v.z), r));
+                }
+            }
+            group_bar(1);
+        }
+        if (tid == 0 && ovlp_out) ovlp_out[w] = zero ? make_double2(0.0, 0.0) : cmul(det, det);
+    } else {  // Gauss-Jordan (fp32)
+        const int t = tid - 128, rr = t >> 2, q = t & 3;
+        for (int k = 0; k < o; ++k) {
+            const int* pc = s_perm[1][k & 1];
+            int* pn = s_perm[1][(k + 1) & 1];
+            const int bi = piv_row(s_key[1][k % 3]);
+            const int pr = pc[bi];
+            const float2 pv = X[pr * o2 + k];
+            const float den = pv.x * pv.x + pv.y * pv.y;
+            const float2 rp = make_float2(pv.x / den, -pv.y / den);
+            if (t == 0) {
+                s_key[1][(k + 2) % 3] = 0ull;
+                s_pf[k] = pr;
+                s_rp[k] = rp;
+            }
+            if (rr < o - 1) {
+                const int r = rr < k ? rr : rr + 1;  // every logical row but k
+                const int p = r < k ? s_pf[r] : (r == bi ? pc[k] : pc[r]);
+                if (q == 0 && r > k) pn[r] = p;
+                const float2 x = X[p * o2 + k];
+                const float2 f = make_float2(x.x * rp.x - x.y * rp.y, x.x * rp.y + x.y * rp.x);
+                for (int c = k + 1 + q; c < o2; c += 4) {
+                    const float2 u = X[pr * o2 + c], y = X[p * o2 + c];
+                    const float2 v = make_float2(y.x - (f.x * u.x - f.y * u.y), y.y - (f.x * u.y + f.y * u.x));
+                    X[p * o2 + c] = v;
+                    if (c == k + 1 && r > k && c < o)
+                        atomicMax(&s_key[1][(k + 1) % 3], piv_key(fabsf(v.x) + fabsf(v.y), r));
+                }
+            }
+            group_bar(2);
+        }
+    }
+    __syncthreads();
+    {  // row a of m^-1 = (physical row pf[a] of the right half) / pivot_a, packed at stride IS
+        float2 t4[4];  // o * o <= 4 x 256
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = tid + 256 * u;
+            if (e < o * o) {
+                const int a = e / o, b = e - a * o;
+                const float2 x = X[s_pf[a] * o2 + o + b], rp = s_rp[a];
+                t4[u] = make_float2(x.x * rp.x - x.y * rp.y, x.x * rp.y + x.y * rp.x);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = tid + 256 * u;
+            if (e < o * o) inv[(e / o) * IS + e % o] = t4[u];
+        }
+        for (int e = tid; e < o * (IS - o); e += blockDim.x) inv[(e / (IS - o)) * IS + o + e % (IS - o)] = make_float2(0.f, 0.f);
+    }
+
+    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
+    const double2* Wp = walkers + (size_t)w * n * o;
+    __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
+    __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
+    double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
+    const int il = tid & 31, b0 = 4 * (tid >> 5);  // rows il and il + 32 of a chunk, columns b0..b0+3
+    for (int i0 = 0; i0 < n; i0 += OG_CH) {
+        const int rows = min(OG_CH, n - i0);
+        __syncthreads();
+        for (int e = tid; e < rows * o; e += blockDim.x) {
+            const double2 x = Wp[(size_t)i0 * o + e];
+            wf[(e / o) * ws + e % o] = make_float2(d2f_trunc(x.x), d2f_trunc(x.y));
+        }
+        __syncthreads();
+        if (b0 >= o || il >= rows) continue;
+        const bool two = il + 32 < rows;
+        float2 a0[4], a1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) a0[j] = a1[j] = make_float2(0.f, 0.f);
+        const float2* x0p = wf + il * ws;
+        const float2* x1p = wf + (two ? il + 32 : il) * ws;
+#pragma unroll 1
+        for (int a = 0; a < o; ++a) {
+            const float2 x0 = x0p[a], x1 = x1p[a];
+            const float4 va = *(const float4*)(inv + a * IS + b0), vb = *(const float4*)(inv + a * IS + b0 + 2);
+            const float2 v[4] = {make_float2(va.x, va.y), make_float2(va.z, va.w), make_float2(vb.x, vb.y),
+                                 make_float2(vb.z, vb.w)};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                a0[j].x = fmaf(x0.x, v[j].x, a0[j].x); a0[j].x = fmaf(-x0.y, v[j].y, a0[j].x);
+                a0[j].y = fmaf(x0.x, v[j].y, a0[j].y); a0[j].y = fmaf(x0.y, v[j].x, a0[j].y);
+                a1[j].x = fmaf(x1.x, v[j].x, a1[j].x); a1[j].x = fmaf(-x1.y, v[j].y, a1[j].x);
+                a1[j].y = fmaf(x1.x, v[j].y, a1[j].y); a1[j].y = fmaf(x1.y, v[j].x, a1[j].y);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = b0 + j;
+            if (b >= o) break;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && !two) break;
+                const int i = i0 + il + 32 * h;
+                const float2 g = h ? a1[j] : a0[j];
+                if (re_row) {
+                    split_storef(re_row, split.S, b * n + i, g.x, true, split.sec);
+                    split_storef(im_row, split.S, b * n + i, g.y, true, split.sec);
+                }
+                if (Gp) Gp[(size_t)b * n + i] = make_double2(g.x, g.y);
+            }
+        }
+    }
+    if (!re_row) return;
+    for (int e = n * o + tid; e < split.S; e += blockDim.x) {
+        split_storef(re_row, split.S, e, 0.f, true, split.sec);
+        split_storef(im_row, split.S, e, 0.f, true, split.sec);
+    }
+    for (long long e = (long long)split.sec * split.S + tid; e < split.ld; e += blockDim.x) {
+        re_row[e] = __float2bfloat16(0.f);
+        im_row[e] = __float2bfloat16(0.f);
+    }
+}
+
 int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* walkers, double2* ovlp_out,
                          SplitOut split, cudaStream_t s, double2* green_out, const float2* cs, const float4* m_in) {
     if (W <= 0) return AFQ_OK;
     const size_t base = (size_t)o * o * sizeof(double2) + 2 * (size_t)o * o * sizeof(float2);
     const size_t wbytes = (size_t)n * o * sizeof(float2);
     const size_t dfbytes = 2 * (size_t)OS_CH * o * sizeof(float2);
-    const bool df = cs != nullptr || m_in != nullptr;        // double-float m, W staged in chunks
+    if (m_in) {  // m given (double-float)
+        if (o > 32) return fail(AFQ_E_UNSUPPORTED, "overlap from a given m: nocc=%d > 32", o);
+        const size_t sm = (size_t)og_a16(o) * sizeof(float4) + (size_t)og_xs(o) * sizeof(float2);
+        AFQ_TRY(smem_attr(k_overlap_oz, sm));
+        k_overlap_oz<<<W, 256, sm, s>>>(n, o, m_in, walkers, ovlp_out, split, green_out);
+        AFQ_LAUNCHED("k_overlap_oz");
+        return AFQ_OK;
+    }
+    const bool df = cs != nullptr;        // double-float m, W staged in chunks
     const bool stage = df || base + wbytes <= 160 * 1024;  // else read W from global in the last loop
     const size_t smem = base + (df ? dfbytes : stage ? wbytes : 0);
     const int ag = 256 / o, ma = (o + ag - 1) / ag;
 #define AFQ_OS(MAV)                                                                                              \
     do {                                                                                                         \
-        if (m_in) {                                                                                              \
-            AFQ_TRY(smem_attr(k_overlap_split<MAV, true, true, true>, smem));                                    \
-            k_overlap_split<MAV, true, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split,       \
-                                                                       green_out, cs, m_in);                     \
-        } else if (df) {                                                                                         \
+        if (df) {                                                                                                \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, true, true>, smem));                                          \
-            k_overlap_split<MAV, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, cs, \
-                                                                 nullptr);                                       \
+            k_overlap_split<MAV, true, true><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out,   \
+                                                                 cs);                                            \
         } else if (stage) {                                                                                      \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, true, false>, smem));                                         \
             k_overlap_split<MAV, true, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out,  \
-                                                                  nullptr, nullptr);                             \
+                                                                  nullptr);                                      \
         } else {                                                                                                 \
             AFQ_TRY(smem_attr(k_overlap_split<MAV, false, false>, smem));                                        \
             k_overlap_split<MAV, false, false><<<W, 256, smem, s>>>(n, o, mo, walkers, ovlp_out, split, green_out, \
-                                                                   nullptr, nullptr);                            \
+                                                                   nullptr);                                     \
         }                                                                                                        \
     } while (0)
     if (ma <= 1) AFQ_OS(1);
