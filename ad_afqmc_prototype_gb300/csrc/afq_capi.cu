@@ -128,9 +128,8 @@ struct StepWS {
     __nv_bfloat16* esplit;  // 2 n*n: E - I as bf16 hi, mid (tensor-core Taylor products)
     float2* csplit;     // n*o: trial orbitals as (hi, lo) fp32 pairs (double-float overlap)
     // m = C^T W on the tensor cores from integer digit slices (k_ozaki.cu), nocc <= 32
-    __nv_bfloat16* ozA;  // 2 o W x Kt: the walkers' digit rows
-    __nv_bfloat16* ozB;  // 8 o x Kt: the trial's digit rows
-    int* ozE;            // 2 o W: row exponents
+    __nv_bfloat16* ozB;  // NB x K: the trial's digit rows
+    int* ozE;            // W x 64: row exponents
     int* ozF;            // o: column exponents
     float2* ozM;         // W o o x 2: m as double-float pairs
 };
@@ -160,9 +159,8 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         s.csplit = a.take<float2>(n * o);
         if (oz_supported(d)) {
             const OzDims z = oz_dims((int)n, (int)o);
-            s.ozA = a.take<__nv_bfloat16>((size_t)z.rows * W * z.Kt);
-            s.ozB = a.take<__nv_bfloat16>((size_t)z.Nb * z.Kt);
-            s.ozE = a.take<int>((size_t)z.rows * W);
+            s.ozB = a.take<__nv_bfloat16>((size_t)z.NB * z.K);
+            s.ozE = a.take<int>(64 * W);
             s.ozF = a.take<int>(64);
             s.ozM = a.take<float2>(W * o * o * 2);
         }
@@ -309,10 +307,9 @@ static int overlap_mixed(const afq_problem* pb, double2* walk, double2* ovl, Spl
     const afq_dims* d = &pb->dims;
     const int W = d->n_walkers, n = d->norb, o = d->nocc;
     const double2* mo = (const double2*)pb->mo_coeff;
-    if (ws.ozA) {
+    if (ws.ozB) {
         AFQ_TRY(launch_oz_split_c(n, o, mo, ws.ozB, ws.ozF, s));
-        AFQ_TRY(launch_oz_split_w(W, n, o, walk, ws.ozA, ws.ozE, s));
-        AFQ_TRY(launch_tc_gemm_oz(W, n, o, ws.ozA, ws.ozB, ws.ozE, ws.ozF, ws.ozM, ws.status, s));
+        AFQ_TRY(launch_oz_m(W, n, o, walk, ws.ozB, ws.ozF, ws.ozE, ws.ozM, ws.status, s));
         return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit, (const float4*)ws.ozM);
     }
     return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit);

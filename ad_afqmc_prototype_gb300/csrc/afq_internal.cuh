@@ -371,19 +371,19 @@ int launch_overlap_split(int W, int n, int o, const double2* mo, const double2* 
                          const float4* m_in = nullptr);
 
 // k_ozaki.cu: m = C^T W of every walker from integer digit slices on the
-// tensor cores (the GEMM and its recombination: launch_tc_gemm_oz).
+// tensor cores, nocc <= 32, norb <= 584.
 struct OzDims {
-    int rows;  // product rows per walker: 2 nocc (orbital b, Re / Im)
-    int nK;    // norb rounded up to 8: the K stride of a digit slice
-    int Kt;    // 7 nK rounded up to 64
-    int Nb;    // B rows: 8 per trial orbital
+    int nks;  // K steps: eight orbitals each
+    int K;    // 64 nks: eight K slots per orbital
+    int NB;   // B rows: 8 per trial orbital, nocc rounded up to even
 };
 constexpr int OZ_NONFINITE = 0x7fffffff;  // E_r of a row holding inf or nan
 OzDims oz_dims(int n, int o);
+// B (NB x K) and F_a (o) from the trial orbitals
 int launch_oz_split_c(int n, int o, const double2* mo, __nv_bfloat16* B, int* fa, cudaStream_t s);
-int launch_oz_split_w(int W, int n, int o, const double2* walkers, __nv_bfloat16* A, int* er, cudaStream_t s);
-int launch_tc_gemm_oz(int W, int n, int o, const __nv_bfloat16* A, const __nv_bfloat16* B, const int* er,
-                      const int* fa, float2* m, int* err, cudaStream_t s);
+// m[((w o + a) o + b) 2 + part] (double-float pairs) from the walkers; er: W x 64 row exponents (scratch)
+int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, int* er,
+                float2* m, int* err, cudaStream_t s);
 int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
 // k_cv.cu, k_mlp.cu

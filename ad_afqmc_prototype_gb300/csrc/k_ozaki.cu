@@ -9,156 +9,404 @@
 // with E_r two above the exponent of the largest entry of the row r =
 // (walker, b, part), F_a the same for column a of C (so the scaled entries
 // are below 1/4 and the top digit stays in range), each digit an integer
-// bf16 holds exactly.  The GEMM D = A B^T takes A row r = [w_1 | ... | w_7]
-// (K = 7 nK, nK = norb rounded up to 8) and B row (a, d) = [c_{d-1} | c_{d-2}
-// | ... ] (the digits of C whose index pairs with the slice to d = s + t,
-// zero elsewhere), d = 2..9:
+// bf16 holds exactly.  The product D = A B^T takes A row r with orbital i's
+// digits in the eight K slots 8 i .. 8 i + 7 (w_1 .. w_7, then a zero), and B
+// row (a, d), d = 2..9, with c_{d-s} in the slot of w_s (zero where d - s is
+// not a digit index):
 //   D[r][(a, d)] = sum_{s + t = d} sum_i w_s[i] c_t[i],
-// an integer of magnitude <= 7 x norb x 2^12 < 2^24 for norb <= 585, so the
+// an integer of magnitude <= 7 x norb x 2^12 < 2^24 for norb <= 584, so the
 // tensor cores' fp32 sums are exact.  Then
 //   m = 2^(E_r + F_a) sum_{d=2..9} D_d 2^(-7 d)
 // with the terms s + t > 9 left out (each below 2^-51 of 2^(E_r + F_a) an
 // orbital) and the digits cut toward zero at 2^-49: m to ~2^-45 of the
 // product of the row's and the column's largest entries, the accuracy of the
-// double-float m it replaces.  The recombination runs in the GEMM's epilogue
-// (k_tc_gemm.cu, MODE 3) with integer and fp32 operations, and gives m as a
-// double-float pair.
+// double-float m it replaces, given as a double-float pair.
+//
+// k_oz_m builds A itself: the walkers' rows are bulk-copied into shared
+// memory beside each B tile, eight producer warps cut them into digits and
+// write the 128-byte-swizzled A tile, one thread issues the MMAs, and eight
+// epilogue warps recombine the digit sums from tensor memory.  A never goes
+// through HBM.
 #include "afq_internal.cuh"
+#include "tc_common.cuh"
 
 namespace afq {
 
 OzDims oz_dims(int n, int o) {
     OzDims z;
-    z.rows = 2 * o;
-    z.nK = (n + 7) / 8 * 8;
-    z.Kt = (7 * z.nK + 63) / 64 * 64;
-    z.Nb = 8 * o;
+    z.nks = (n + 7) / 8;
+    z.K = 64 * z.nks;
+    z.NB = 8 * (o + (o & 1));
     return z;
 }
 
-// The 7 signed base-128 digits of x 2^-E (|x| 2^-E < 1/4) cut toward zero at
-// 2^-49, by integer operations: x = +-mant 2^(eb - 1075), so the 49-bit
-// fixed-point value (|X| < 2^47) is mant shifted by eb - 1026 - E (<= -6).
-__device__ __forceinline__ void oz_digits(double x, int E, int (&d)[7]) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    const int eb = (int)((u >> 52) & 0x7ffu);
-    long long X = 0;
-    if (eb != 0 && eb != 0x7ff) {
-        const unsigned long long mant = (u & 0xfffffffffffffull) | (1ull << 52);
-        const int sh = eb - 1026 - E;
-        if (sh > -64) X = (long long)(sh >= 0 ? mant << sh : mant >> (-sh));
-        if (u >> 63) X = -X;
-    }
-#pragma unroll
-    for (int t = 6; t >= 0; --t) {  // balanced digits in [-64, 64), least significant first
-        const long long dt = ((X + 64) & 127) - 64;
-        d[t] = (int)dt;
-        X = (X - dt) >> 7;
-    }
-}
+namespace {
 
-// Largest biased binary64 exponent of |x| (2047 for inf / nan).
-__device__ __forceinline__ int oz_ebits(double x) {
+// Balanced base-128 digits d_t in [-64, 64) of X (|X| < 2^47), X = sum d_t
+// 128^t, are the plain base-128 digits of X + OZ_OFF minus 64.
+constexpr long long OZ_OFF = 64LL * ((1LL << 49) - 1) / 127;
+
+// The 7 signed base-128 digits of x 2^-E (|x| 2^-E < 1/4) cut toward zero at
+// 2^-49, most significant first, by integer operations: x = +-mant 2^(eb -
+// 1075), so the 49-bit fixed-point value (|X| < 2^47) is mant shifted right by
+// E + 1026 - eb (>= 6).  Zero for zero, subnormal and non-finite x.
+__device__ __forceinline__ unsigned long long oz_fixed(double x, int E) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int eb = (int)((u >> 52) & 0x7ffu), rs = E + 1026 - eb;
+    long long X = 0;
+    if (eb != 0 && eb != 0x7ff && rs < 64) {
+        X = (long long)(((u & 0xfffffffffffffull) | (1ull << 52)) >> rs);
+        if ((long long)u < 0) X = -X;
+    }
+    return (unsigned long long)(X + OZ_OFF);
+}
+// digit s (1..7) of the offset value Y, as an exact fp32 integer
+__device__ __forceinline__ float oz_field(uint32_t v, int sh) {
+    return __int_as_float(0x4B000000 | ((v >> sh) & 127u)) - 8388672.f;  // (2^23 + field) - (2^23 + 64)
+}
+__device__ __forceinline__ uint32_t oz_bf2(float lo, float hi) {  // two small integers as a bf16 pair (exact)
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *(const uint32_t*)&v;
+}
+// Orbital i's eight K slots of an A row: w_1 .. w_7 and a zero.
+__device__ __forceinline__ uint4 oz_chunk(double x, int E) {
+    const unsigned long long Y = oz_fixed(x, E);
+    const uint32_t lo = (uint32_t)Y, hi = (uint32_t)(Y >> 28);
+    return make_uint4(oz_bf2(oz_field(hi, 14), oz_field(hi, 7)), oz_bf2(oz_field(hi, 0), oz_field(lo, 21)),
+                      oz_bf2(oz_field(lo, 14), oz_field(lo, 7)), oz_bf2(oz_field(lo, 0), 0.f));
+}
+__device__ __forceinline__ int oz_digit(double x, int E, int s) {  // w_s, s = 1..7
+    const unsigned long long Y = oz_fixed(x, E);
+    return (int)((Y >> (7 * (7 - s))) & 127u) - 64;
+}
+__device__ __forceinline__ int oz_ebits(double x) {  // biased binary64 exponent (2047 for inf / nan)
     return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu);
 }
 
-__device__ __forceinline__ uint32_t oz_bf2(int lo, int hi) {  // two small integers as a bf16 pair (exact)
-    const __nv_bfloat162 v = __floats2bfloat162_rn((float)lo, (float)hi);
-    return *(const uint32_t*)&v;
-}
-
-// B (Nb x Kt, K-major) and F_a from the trial C (n x o, real part used): one
+// B (NB x K, K-major) and F_a from the trial C (n x o, real part used): one
 // CTA per B row (a, d), each finding its column's scale.
 __global__ void __launch_bounds__(256) k_oz_split_c(int n, int o, const double2* __restrict__ mo,
-                                                    __nv_bfloat16* __restrict__ B, int* __restrict__ fa, int nK,
-                                                    int Kt) {
+                                                    __nv_bfloat16* __restrict__ B, int* __restrict__ fa, int K) {
     __shared__ int s_e;
-    const int row = blockIdx.x, a = row >> 3, dd = (row & 7) + 2;
+    const int row = blockIdx.x, a = row >> 3, d = (row & 7) + 2;
     if (threadIdx.x == 0) s_e = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) atomicMax(&s_e, oz_ebits(mo[(size_t)i * o + a].x));
+    if (a < o)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) atomicMax(&s_e, oz_ebits(mo[(size_t)i * o + a].x));
     __syncthreads();
     const int F = s_e - 1020;
-    if (threadIdx.x == 0 && (row & 7) == 0) fa[a] = F;
-    // B[(a, d)][(s - 1) nK + i] = c_{d - s}[i][a] where 1 <= d - s <= 7
-    for (int k = threadIdx.x; k < Kt; k += blockDim.x) {
-        const int s = k / nK + 1, i = k % nK, t = dd - s;
+    if (threadIdx.x == 0 && (row & 7) == 0 && a < o) fa[a] = F;
+    // B[(a, d)][8 i + s - 1] = c_{d - s}[i][a] for 1 <= d - s <= 7
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const int i = k >> 3, s = (k & 7) + 1, t = d - s;
         int v = 0;
-        if (s <= 7 && i < n && t >= 1 && t <= 7) {
-            int dg[7];
-            oz_digits(mo[(size_t)i * o + a].x, F, dg);
-            v = dg[t - 1];
-        }
-        B[(size_t)row * Kt + k] = __float2bfloat16((float)v);
+        if (a < o && i < n && s <= 7 && t >= 1 && t <= 7) v = oz_digit(mo[(size_t)i * o + a].x, F, t);
+        B[(size_t)row * K + k] = __float2bfloat16((float)v);
     }
 }
 
-// A rows (walker, b, part) over K = (s - 1) nK + i, and E_r; one CTA per walker.
-constexpr int OZ_CH = 32;  // orbital rows staged a chunk
-__global__ void __launch_bounds__(256) k_oz_split_w(int n, int o, const double2* __restrict__ walkers,
-                                                    __nv_bfloat16* __restrict__ A, int* __restrict__ er, int nK,
-                                                    int Kt) {
-    extern __shared__ double2 s_w[];  // OZ_CH x o staged rows
-    __shared__ int s_e[64];
-    const int w = blockIdx.x, R = 2 * o;
-    const double2* Wp = walkers + (size_t)w * n * o;
-    for (int r = threadIdx.x; r < R; r += blockDim.x) s_e[r] = 0;
+// E_r of every row (walker, b, part) of A: er[w 64 + 2 b + part]; one CTA per
+// walker, four threads a row.
+__global__ void __launch_bounds__(256) k_oz_rowexp(int n, int o, const double2* __restrict__ walkers,
+                                                   int* __restrict__ er) {
+    __shared__ int s_e[4][64];
+    const int w = blockIdx.x, r = threadIdx.x & 63, ph = threadIdx.x >> 6, b = r >> 1;
+    const double* Wp = (const double*)(walkers + (size_t)w * n * o) + (r & 1);
+    int e = 0;
+    if (b < o)
+        for (int i = ph; i < n; i += 4) e = max(e, oz_ebits(Wp[2 * ((size_t)i * o + b)]));
+    s_e[ph][r] = e;
     __syncthreads();
-    for (int e = threadIdx.x; e < n * o; e += blockDim.x) {
-        const double2 x = Wp[e];
-        const int b = e % o;
-        atomicMax(&s_e[2 * b], oz_ebits(x.x));
-        atomicMax(&s_e[2 * b + 1], oz_ebits(x.y));
-    }
-    __syncthreads();
-    for (int r = threadIdx.x; r < R; r += blockDim.x)
-        er[(size_t)w * R + r] = s_e[r] == 0x7ff ? OZ_NONFINITE : s_e[r] - 1020;
-    __nv_bfloat16* Aw = A + (size_t)w * R * Kt;
-    // digits, two orbital rows a thread: 4-byte stores along K, a warp's 32 lanes on consecutive pairs
-    for (int i0 = 0; i0 < nK; i0 += OZ_CH) {
-        const int rows = min(OZ_CH, nK - i0);
-        __syncthreads();
-        for (int e = threadIdx.x; e < rows * o; e += blockDim.x) {
-            const int i = i0 + e / o;
-            s_w[e] = i < n ? Wp[(size_t)i * o + e % o] : make_double2(0.0, 0.0);
-        }
-        __syncthreads();
-        const int pairs = rows >> 1;
-        for (int t = threadIdx.x; t < R * pairs; t += blockDim.x) {
-            const int r = t / pairs, ip = t % pairs, b = r >> 1, part = r & 1;
-            const int il = 2 * ip;
-            const double2 x0 = s_w[il * o + b], x1 = s_w[(il + 1) * o + b];
-            const int E = s_e[r] == 0x7ff ? 0 : s_e[r] - 1020;
-            int d0[7], d1[7];
-            oz_digits(part ? x0.y : x0.x, E, d0);
-            oz_digits(part ? x1.y : x1.x, E, d1);
-            uint32_t* row = (uint32_t*)(Aw + (size_t)r * Kt);
-#pragma unroll
-            for (int s = 0; s < 7; ++s) row[(s * nK + i0 + il) >> 1] = oz_bf2(d0[s], d1[s]);
-        }
-    }
-    // the K padding past 7 nK
-    for (int t = threadIdx.x; t < R * ((Kt - 7 * nK) >> 1); t += blockDim.x) {
-        const int pk = (Kt - 7 * nK) >> 1, r = t / pk, k = 7 * nK + 2 * (t % pk);
-        *(uint32_t*)(Aw + (size_t)r * Kt + k) = 0u;
+    if (threadIdx.x < 64) {
+        const int m = max(max(s_e[0][r], s_e[1][r]), max(s_e[2][r], s_e[3][r]));
+        er[(size_t)w * 64 + r] = b >= o ? 0 : m == 0x7ff ? OZ_NONFINITE : m - 1020;
     }
 }
+
+constexpr int OZ_BM = 128;               // A rows a tile: two walkers of 64 rows (2 b + part, b < 32)
+constexpr int OZ_THREADS = 18 * 32;      // warp 0: copies, 1: MMA, 2-9: digits, 10-17: epilogue
+constexpr int OZ_PW0 = 2, OZ_EW0 = 10;   // first producer / epilogue warp
+constexpr int OZ_STG = 4;
+constexpr int OZ_A_BYTES = OZ_BM * 64 * 2;
+constexpr int OZ_SLOT_COLS = 256;        // tensor-memory columns between the two accumulators
+constexpr int OZ_SMEM_MAX = 227 * 1024;
+
+struct OzGeo {
+    int b_bytes, w_bytes, stage, smem;
+};
+__host__ __device__ inline OzGeo oz_geo(int o) {
+    OzGeo g;
+    g.b_bytes = 8 * (o + (o & 1)) * 128;             // NB rows of 64 bf16
+    g.w_bytes = (2 * 8 * o * 16 + 1023) / 1024 * 1024;  // two walkers' eight orbital rows
+    g.stage = OZ_A_BYTES + g.b_bytes + g.w_bytes;
+    g.smem = OZ_STG * g.stage + 1024 + 256;
+    return g;
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"((unsigned long long)src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+}
+
+// m of walkers 2 t, 2 t + 1 for the tiles t of this CTA (persistent).
+// Barriers a stage: ld_full (B tile and the walkers' rows landed), a_full
+// (the eight producer warps wrote the A tile), empty (the MMAs that read
+// the stage finished).  Every wait is bounded; on a timeout the CTA raises
+// *err and every role unwinds (the copy thread waits, bounded, for its
+// copies, the MMA thread for its MMAs before the tensor memory is freed).
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_oz_m(const __grid_constant__ CUtensorMap tmB, int W, int n, int o, const double2* __restrict__ walkers,
+           const int* __restrict__ er, const int* __restrict__ fa, float2* __restrict__ mout, int* __restrict__ err) {
+    using namespace tc;
+    const OzGeo geo = oz_geo(o);
+    const int NB = 8 * (o + (o & 1)), nks = (n + 7) / 8, ntiles = (W + 1) / 2;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + OZ_STG * geo.stage);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 3 * OZ_STG + 4 + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    const uint32_t ldf0 = smem_u32(bars), af0 = smem_u32(bars + OZ_STG), emp0 = smem_u32(bars + 2 * OZ_STG);
+    const uint32_t tfull0 = smem_u32(bars + 3 * OZ_STG), tempty0 = smem_u32(bars + 3 * OZ_STG + 2);
+    const uint32_t drain = smem_u32(bars + 3 * OZ_STG + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < OZ_STG; ++s) {
+            mbar_init(ldf0 + 8 * s, 1);
+            mbar_init(af0 + 8 * s, 8);  // one arrival per producer warp
+            mbar_init(emp0 + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 256);  // every epilogue thread
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(2 * OZ_SLOT_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
+            int stage = 0;
+            uint32_t phase = 0;
+            int issued[OZ_STG];
+            uint32_t issued_par[OZ_STG];
+            for (int s = 0; s < OZ_STG; ++s) issued[s] = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                const int nw = min(2, W - 2 * t);
+                for (int kk = 0; kk < nks; ++kk) {
+                    if (!mbar_wait(emp0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
+                    issued[stage] = 0;
+                    uint8_t* st = smem + stage * geo.stage;
+                    const uint32_t fb = ldf0 + 8 * stage;
+                    const uint32_t rb = (uint32_t)(min(8, n - 8 * kk) * o * 16);  // one walker's rows
+                    mbar_expect_tx(fb, (uint32_t)geo.b_bytes + nw * rb);
+                    tma_load_2d(smem_u32(st + OZ_A_BYTES), &tmB, 64 * kk, 0, fb);
+                    for (int wl = 0; wl < nw; ++wl)
+                        bulk_load(smem_u32(st + OZ_A_BYTES + geo.b_bytes + wl * 8 * o * 16),
+                                  walkers + ((size_t)(2 * t + wl) * n + 8 * kk) * o, rb, fb);
+                    issued[stage] = 1;
+                    issued_par[stage] = phase;
+                    if (++stage == OZ_STG) { stage = 0; phase ^= 1; }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+            }
+            // every copy this thread issued lands before the CTA exits
+            for (int s = 0; s < OZ_STG; ++s)
+                if (issued[s]) mbar_wait(ldf0 + 8 * s, issued_par[s], nullptr);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NB >> 3) << 17) |
+                                   ((uint32_t)(OZ_BM >> 4) << 24);
+            int stage = 0, slot = 0;
+            uint32_t phase = 0, slot_phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                for (int kk = 0; kk < nks; ++kk) {
+                    if (!mbar_wait(af0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(ldf0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    if (kk == 0 && !mbar_wait(tempty0 + 8 * slot, slot_phase ^ 1, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(smem + stage * geo.stage), b0 = a0 + OZ_A_BYTES;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        umma_bf16_i(tmem + slot * OZ_SLOT_COLS, desc_k128(a0 + 32 * k), desc_k128(b0 + 32 * k), idesc,
+                                    (kk | k) != 0);
+                    umma_commit(emp0 + 8 * stage);
+                    if (kk == nks - 1) {
+                        umma_commit(tfull0 + 8 * slot);
+                        if (++slot == 2) { slot = 0; slot_phase ^= 1; }
+                    }
+                    if (++stage == OZ_STG) { stage = 0; phase ^= 1; }
+                }
+            }
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+            }
+            umma_commit(drain);
+            mbar_wait(drain, 0, nullptr);
+        }
+    } else if (warp < OZ_EW0) {
+        // producers: row r of the tile, orbitals 4 h .. 4 h + 3 of each K step
+        const int p = threadIdx.x - 32 * OZ_PW0, r = p & (OZ_BM - 1), h = p >> 7;
+        const int wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
+        int stage = 0;
+        uint32_t phase = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            const int w = 2 * t + wl;
+            const bool valid = w < W && b < o;
+            int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
+            if (E == OZ_NONFINITE) E = 0;  // digits of no use: the epilogue writes nan for the row
+            for (int kk = 0; kk < nks; ++kk) {
+                if (!mbar_wait(ldf0 + 8 * stage, phase, abort_flag)) {
+                    atomicExch(err, 1);
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = smem + stage * geo.stage;
+                const double* wrow = (const double*)(st + OZ_A_BYTES + geo.b_bytes + wl * 8 * o * 16) + part;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int ii = 4 * h + u;
+                    const double x = (valid && 8 * kk + ii < n) ? wrow[2 * (ii * o + b)] : 0.0;
+                    const uint4 c = oz_chunk(x, E);
+                    const uint32_t dst = smem_u32(st) + r * 128 + ((ii ^ (r & 7)) << 4);
+                    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(c.x), "r"(c.y), "r"(c.z),
+                                 "r"(c.w)
+                                 : "memory");
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(af0 + 8 * stage);
+                if (++stage == OZ_STG) { stage = 0; phase ^= 1; }
+            }
+        }
+    } else {
+        // epilogue: this warp's 32 rows (lane quadrant q), half the trial orbitals
+        const int q = warp & 3, hh = (warp - OZ_EW0) >> 2, oe = o + (o & 1);
+        const int r = 32 * q + lane, wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
+        int slot = 0;
+        uint32_t slot_phase = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            if (!mbar_wait_inl(tfull0 + 8 * slot, slot_phase, abort_flag)) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const int w = 2 * t + wl;
+            const bool valid = w < W && b < o;
+            const int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
+            for (int a = hh * (oe / 2); a < (hh + 1) * (oe / 2); ++a) {
+                uint32_t v[8];
+                __syncwarp();
+                tmem_ld8(tmem + slot * OZ_SLOT_COLS + 8 * a + ((uint32_t)(32 * q) << 16), v);
+                if (valid && a < o) {
+                // Q0 = D_2 2^21 + D_3 2^14 + D_4 2^7 + D_5 and Q1 the same for D_6..9 (exact 64-bit
+                // integers), m = (Q0 2^-35 + Q1 2^-63) 2^(E + F) as a double-float pair
+                long long Q[2];
+#pragma unroll
+                for (int hq = 0; hq < 2; ++hq) {
+                    long long qv = 0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) qv = qv * 128 + (long long)__float2int_rn(__uint_as_float(v[4 * hq + u]));
+                    Q[hq] = qv;
+                }
+                float2 out;
+                if (E == OZ_NONFINITE) {
+                    out = make_float2(__int_as_float(0x7fc00000), 0.f);
+                } else {
+                    // Q0 = qh 2^21 + ql with qh, ql exact in fp32: (hi, lo) = two-sum of the two
+                    // exact terms, then the Q1 term (~2^-28 of Q0's range) into lo
+                    const long long q0 = Q[0];
+                    const long long qh = q0 >> 21, ql = q0 - (qh << 21);
+                    const int sc = E + fa[a];
+                    const float th = ldexpf((float)qh, sc - 14), tm = ldexpf((float)ql, sc - 35);
+                    const float hi = th + tm;
+                    const float bb = hi - th;
+                    const float e0 = (th - (hi - bb)) + (tm - bb);
+                    const float lo = e0 + ldexpf((float)Q[1], sc - 63);
+                    const float h2 = hi + lo;
+                    out = make_float2(h2, lo - (h2 - hi));
+                }
+                mout[(((size_t)w * o + a) * o + b) * 2 + part] = out;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(tempty0 + 8 * slot);
+            if (++slot == 2) { slot = 0; slot_phase ^= 1; }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * OZ_SLOT_COLS)
+                     : "memory");
+    }
+}
+
+DeviceOnce g_oz_smem;
+
+}  // namespace
 
 int launch_oz_split_c(int n, int o, const double2* mo, __nv_bfloat16* B, int* fa, cudaStream_t s) {
-    if (o > 64) return fail(AFQ_E_UNSUPPORTED, "ozaki m: nocc=%d > 64", o);
+    if (o > 32) return fail(AFQ_E_UNSUPPORTED, "ozaki m: nocc=%d > 32", o);
     const OzDims z = oz_dims(n, o);
-    k_oz_split_c<<<z.Nb, 256, 0, s>>>(n, o, mo, B, fa, z.nK, z.Kt);
+    k_oz_split_c<<<z.NB, 256, 0, s>>>(n, o, mo, B, fa, z.K);
     AFQ_LAUNCHED("k_oz_split_c");
     return AFQ_OK;
 }
 
-int launch_oz_split_w(int W, int n, int o, const double2* walkers, __nv_bfloat16* A, int* er, cudaStream_t s) {
+int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, int* er,
+                float2* m, int* err, cudaStream_t s) {
+    using namespace tc;
     if (W <= 0) return AFQ_OK;
     if (o > 32) return fail(AFQ_E_UNSUPPORTED, "ozaki m: nocc=%d > 32", o);
+    if (((uintptr_t)walkers) & 15) return fail(AFQ_E_INVALID_ARGUMENT, "ozaki m: walkers not 16-byte aligned");
     const OzDims z = oz_dims(n, o);
-    const size_t smem = (size_t)OZ_CH * o * sizeof(double2);
-    k_oz_split_w<<<W, 256, smem, s>>>(n, o, walkers, A, er, z.nK, z.Kt);
-    AFQ_LAUNCHED("k_oz_split_w");
+    const OzGeo g = oz_geo(o);
+    if (g.smem > OZ_SMEM_MAX) return fail(AFQ_E_UNSUPPORTED, "ozaki m: %d bytes of shared memory", g.smem);
+    k_oz_rowexp<<<W, 256, 0, s>>>(n, o, walkers, er);
+    AFQ_LAUNCHED("k_oz_rowexp");
+    AFQ_TRY(get_encode());
+    CUtensorMap mb;
+    AFQ_TRY(make_map(&mb, B, z.NB, z.K, z.K, z.NB));
+    int sms = 0;
+    AFQ_TRY(device_sms(&sms));
+    AFQ_TRY(raise_smem_once(g_oz_smem, k_oz_m, OZ_SMEM_MAX));
+    const int tiles = (W + 1) / 2, grid = tiles < sms ? tiles : sms;
+    k_oz_m<<<grid, OZ_THREADS, g.smem, s>>>(mb, W, n, o, walkers, er, fa, m, err);
+    AFQ_LAUNCHED("k_oz_m");
     return AFQ_OK;
 }
 

@@ -252,22 +252,9 @@ struct ExchOut {
     int nhalf = 0;   // column halves per row = 2 x column tiles
 };
 
-// Outputs of MODE 3: the recombination of the integer-digit product of
-// k_ozaki.cu.  Rows r = (walker, b, part) of the product, 8 columns per
-// trial orbital a (the digit sums D_d, d = 2..9, exact integers); per row
-//   m = 2^(E_r + F_a) sum_d D_d 2^(-7 d)
-// as a double-float pair at m[((w o + a) o + b) 2 + part].
-struct OzOut {
-    float2* m = nullptr;
-    const int* er = nullptr;  // per row: E_r, or OZ_NONFINITE
-    const int* fa = nullptr;  // per orbital: F_a
-    int o = 0;
-};
-
 // MODE 0: fp32 C.  MODE 1 (split): the two-piece bf16 split of each sum to
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
-// exchange contraction of each 32 x 32 block (ExchOut) instead of C.  MODE 3:
-// the digit recombination (OzOut) instead of C.
+// exchange contraction of each 32 x 32 block (ExchOut) instead of C.
 //
 // Each CTA loads its own A and B tiles with plain TMA copies.  Tile order:
 // with M tiles fastest (nfast = 0) the CTAs resident at one time work on one
@@ -279,8 +266,7 @@ template <int BNT, int MODE, int EWN>
 __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
-                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo, int nfast,
-                    OzOut oz) {
+                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo, int nfast) {
     using D = Drain<BNT, EWN>;
     static_assert(MODE != 2 || EWN == 8, "the exchange epilogue's transpose buffers are sized for eight warps");
     constexpr bool SPLIT = MODE == 1;
@@ -478,51 +464,6 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             }
             const int row = mb * BM + q * 32 + lane;
             const int col0 = nb * BNT + cb;
-            if constexpr (MODE == 3) {
-                // per orbital a: Q0 = D_2 2^21 + D_3 2^14 + D_4 2^7 + D_5 and Q1 the same for D_6..9
-                // (exact 64-bit integers), m = (Q0 2^-35 + Q1 2^-63) 2^(E + F) as a double-float pair
-                if (row < M) {
-                    const int o = oz.o, R = 2 * o;
-                    const int w = row / R, b = (row % R) >> 1, part = row & 1;
-                    const int E = oz.er[row];
-#pragma unroll
-                    for (int g = 0; g < CW / 8; ++g) {
-                        const int a = col0 / 8 + g;
-                        if (a >= o) break;
-                        long long Q[2];
-#pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            long long q = 0;
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const int j = 8 * g + 4 * h + u;
-                                const float v = (j & 1) ? acc[j / 2].y : acc[j / 2].x;
-                                q = q * 128 + (long long)__float2int_rn(v);
-                            }
-                            Q[h] = q;
-                        }
-                        float2 out;
-                        if (E == OZ_NONFINITE) {
-                            out = make_float2(__int_as_float(0x7fc00000), 0.f);
-                        } else {
-                            // Q0 = qh 2^21 + ql with qh, ql exact in fp32: (hi, lo) = two-sum of the
-                            // two exact terms, then the Q1 term (~2^-28 of Q0's range) into lo
-                            const long long q0 = Q[0];
-                            const long long qh = q0 >> 21, ql = q0 - (qh << 21);
-                            const int sc = E + oz.fa[a];
-                            const float th = ldexpf((float)qh, sc - 14), tm = ldexpf((float)ql, sc - 35);
-                            const float hi = th + tm;
-                            const float bb = hi - th;
-                            const float e0 = (th - (hi - bb)) + (tm - bb);
-                            const float lo = e0 + ldexpf((float)Q[1], sc - 63);
-                            const float h2 = hi + lo;
-                            out = make_float2(h2, lo - (h2 - hi));
-                        }
-                        oz.m[(((size_t)w * o + a) * o + b) * 2 + part] = out;
-                    }
-                }
-                continue;
-            }
             if (row < M && SPLIT) {
                 __nv_bfloat16* dh = Ch + (long long)row * ldc + col0;
                 __nv_bfloat16* dm = Cm + (long long)row * ldc + col0;
@@ -606,7 +547,7 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
 template <int BNT, int MODE, int EWN>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                         __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
-                        tc::ExchOut xo = tc::ExchOut{}, tc::OzOut oz = tc::OzOut{}) {
+                        tc::ExchOut xo = tc::ExchOut{}) {
     using namespace tc;
     static DeviceOnce smem_once;
     constexpr int SMEM = Drain<BNT, EWN>::SMEM + (MODE == 2 ? XT_BYTES : 0);
@@ -626,8 +567,8 @@ static int launch_drain(int M, int N, int K, const void* A, long long lda, const
     constexpr long long kL2Keep = 48LL << 20;
     const long long a_bytes = (long long)M * K * 2, b_bytes = (long long)N * K * 2;
     const int nfast = (a_bytes > kL2Keep && b_bytes <= kL2Keep) ? 1 : 0;
-    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo, nfast, oz);
-    AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : MODE == 3 ? "k_gemm_tn_drain(ozaki)" : "k_gemm_tn_drain");
+    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo, nfast);
+    AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }
 
@@ -668,23 +609,5 @@ int launch_tc_gemm_exchange(int nw, int G, int K, const void* A, long long lda, 
 }
 
 int exchange_halves(int G) { return 2 * ((32 * G + tc::EXCH_BNT - 1) / tc::EXCH_BNT); }
-
-// m = C^T W of every walker from the digit operands of k_ozaki.cu: M = W 2o
-// rows, N = 8 o columns, K = Kt; the whole K in one tensor-memory partial
-// (the digit sums are exact integers below 2^24).
-int launch_tc_gemm_oz(int W, int n, int o, const __nv_bfloat16* A, const __nv_bfloat16* B, const int* er,
-                      const int* fa, float2* m, int* err, cudaStream_t s) {
-    if (W <= 0) return AFQ_OK;
-    const OzDims z = oz_dims(n, o);
-    const int kt = z.Kt / tc::BK;
-    AFQ_TRY(drain_prologue(z.Kt, kt));
-    tc::OzOut oz;
-    oz.m = m;
-    oz.er = er;
-    oz.fa = fa;
-    oz.o = o;
-    return launch_drain<256, 3, 16>(W * z.rows, z.Nb, z.Kt, A, z.Kt, B, z.Kt, nullptr, nullptr, nullptr, 0, kt, err, s,
-                                    tc::ExchOut{}, oz);
-}
 
 }  // namespace afq
