@@ -553,6 +553,34 @@ __device__ __forceinline__ float4 zdf_rcp(float4 p) {  // 1 / (a + i b) = (a - i
     return make_float4(re.x, re.y, im.x, im.y);
 }
 
+// The same double-float operations on the (Re, Im) lanes of a complex value
+// at once with the paired fp32 instructions (f32x2): a value is a float4
+// (re hi, im hi, re lo, im lo) = heads h and tails l; results are bitwise
+// those of the scalar forms above (the same roundings in the same order).
+struct dfc {
+    float2 h, l;
+};
+__device__ __forceinline__ dfc dfc_of(float4 v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+__device__ __forceinline__ float4 dfc_f4(dfc v) { return make_float4(v.h.x, v.h.y, v.l.x, v.l.y); }
+__device__ __forceinline__ dfc dfc_add(dfc a, dfc b) {  // df_add on both lanes
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 s = __fadd2_rn(a.h, b.h);
+    const float2 bb = __ffma2_rn(a.h, m1, s);                                       // s - a
+    const float2 e1 = __ffma2_rn(__ffma2_rn(bb, m1, s), m1, a.h);                  // a - (s - bb)
+    const float2 e = __fadd2_rn(__fadd2_rn(e1, __ffma2_rn(bb, m1, b.h)), __fadd2_rn(a.l, b.l));
+    const float2 hs = __fadd2_rn(s, e);                                             // df_quick(s, e)
+    return {hs, __ffma2_rn(__ffma2_rn(s, m1, hs), m1, e)};
+}
+// (x.re x u.re, x.re x u.im) with the broadcast head x.re in (xh, xh), its
+// negation in nxh and its tail in xl: df_mul on both lanes.
+__device__ __forceinline__ dfc dfc_mul_b(float2 xh, float2 nxh, float2 xl, float2 uh, float2 ul) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 np = __fmul2_rn(nxh, uh);                                          // -p
+    const float2 e = __ffma2_rn(xh, ul, __ffma2_rn(xl, uh, __ffma2_rn(xh, uh, np)));
+    const float2 hs = __ffma2_rn(np, m1, e);                                        // p + e
+    return {hs, __ffma2_rn(__fadd2_rn(hs, np), m1, e)};                             // e - (hs - p)
+}
+
 template <int MA, bool STAGE_W, bool DF>
 __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, int o, const double2* __restrict__ mo,
                                                        const double2* __restrict__ walkers,
@@ -844,8 +872,8 @@ __global__ void __launch_bounds__(256, MA <= 4 ? 5 : 1) k_overlap_split(int n, i
 // (value, -row) keys, three in rotation), and Gauss-Jordan leaves each pivot
 // row unscaled (row k of the inverse is scaled by 1 / pivot_k at the end,
 // the multipliers carry the factor meanwhile).  Then G_half = W m^-1 in fp32
-// by all warps, W staged OG_CH rows a time, two rows by four columns a thread.
-constexpr int OG_CH = 64;  // rows of W per G_half staging chunk
+// by all warps, W staged OG_CH rows a time, one row by four columns a thread.
+constexpr int OG_CH = 32;  // rows of W per G_half staging chunk
 
 __device__ __forceinline__ unsigned long long piv_key(float v, int r) {  // v >= 0: its bits order as values
     return ((unsigned long long)__float_as_uint(v) << 32) | (unsigned)(0xffff - r);
@@ -855,7 +883,7 @@ __host__ __device__ constexpr int og_xs(int o) {  // float2 entries of [m | I], 
     return 2 * o * o > o * ((o + 3) & ~3) ? 2 * o * o : o * ((o + 3) & ~3);
 }
 __host__ __device__ constexpr int og_a16(int o) {  // 16-byte units of the region of m, later of staged W
-    return o * o > (OG_CH * (o | 1) + 1) / 2 ? o * o : (OG_CH * (o | 1) + 1) / 2;
+    return o * o > OG_CH * (o | 1) ? o * o : OG_CH * (o | 1);
 }
 __device__ __forceinline__ void group_bar(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
 
@@ -865,8 +893,8 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
                                                        double2* __restrict__ green_out) {
     extern __shared__ float4 smf[];
     const int o2 = 2 * o, ws = o | 1, IS = (o + 3) & ~3;
-    float4* md = smf;                       // o x o double-float m, LU in place
-    float2* wf = (float2*)smf;              // then OG_CH x ws staged fp32 rows of W
+    float4* md = smf;                       // o x o double-float m (re hi, im hi, re lo, im lo), LU in place
+    float4* wf = smf;                       // then OG_CH x ws staged fp32 rows of W as (re, re, im, im)
     float2* X = (float2*)(smf + og_a16(o)); // o x 2o fp32 [m | I], Gauss-Jordan in place
     float2* inv = X;                        // then o x IS: row a of m^-1
     __shared__ unsigned long long s_key[2][3];
@@ -877,9 +905,9 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
 
     const float4* mw = m_in + (size_t)w * o * o;
     for (int e = tid; e < o * o; e += blockDim.x) {
-        const float4 x = mw[e];
+        const float4 x = mw[e];  // (re hi, re lo, im hi, im lo)
         const int r = e / o, c = e - r * o;
-        md[e] = x;
+        md[e] = make_float4(x.x, x.z, x.y, x.w);
         X[r * o2 + c] = make_float2(x.x, x.z);
         X[r * o2 + o + c] = make_float2(r == c ? 1.f : 0.f, 0.f);
     }
@@ -888,7 +916,7 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
     __syncthreads();
     if (tid < o) {  // the pivot keys of step 0 (column 0; the same fp32 heads for both)
         const float4 x = md[tid * o];
-        const unsigned long long key = piv_key(fabsf(x.x) + fabsf(x.z), tid);
+        const unsigned long long key = piv_key(fabsf(x.x) + fabsf(x.y), tid);
         atomicMax(&s_key[0][0], key);
         atomicMax(&s_key[1][0], key);
     }
@@ -903,7 +931,8 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
             int* pn = s_perm[0][(k + 1) & 1];
             const int bi = piv_row(s_key[0][k % 3]);
             const int pr = pc[bi];
-            const float4 pk = md[pr * o + k];
+            const float4 pq = md[pr * o + k];
+            const float4 pk = make_float4(pq.x, pq.z, pq.y, pq.w);  // (re hi, re lo, im hi, im lo)
             // an exactly zero pivot: m is singular and det(m) is exactly 0 (as LAPACK's LU gives it)
             if (pk.x == 0.f && pk.y == 0.f && pk.z == 0.f && pk.w == 0.f) { zero = true; break; }
             if (tid == 0) {
@@ -916,11 +945,18 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
             if (r < o) {
                 const int p = r == bi ? pc[k] : pc[r];
                 if (q == 0) pn[r] = p;
-                const float4 l = zdf_mul(md[p * o + k], rpd);
+                const float4 lq = md[p * o + k];
+                const float4 l = zdf_mul(make_float4(lq.x, lq.z, lq.y, lq.w), rpd);
+                // -l broadcast: (-l.re, -l.re) and (l.im, -l.im), so that the two products sum to -l u
+                const float2 ah = make_float2(-l.x, -l.x), nah = make_float2(l.x, l.x), al = make_float2(-l.y, -l.y);
+                const float2 bh = make_float2(l.z, -l.z), nbh = make_float2(-l.z, l.z), bl = make_float2(l.w, -l.w);
                 for (int j = k + 1 + q; j < o; j += 4) {
-                    const float4 v = zdf_sub(md[p * o + j], zdf_mul(l, md[pr * o + j]));
-                    md[p * o + j] = v;
-                    if (j == k + 1) atomicMax(&s_key[0][(k + 1) % 3], piv_key(fabsf(v.x) + fabsf(v.z), r));
+                    const float4 u = md[pr * o + j];
+                    const dfc t = dfc_add(dfc_mul_b(ah, nah, al, make_float2(u.x, u.y), make_float2(u.z, u.w)),
+                                          dfc_mul_b(bh, nbh, bl, make_float2(u.y, u.x), make_float2(u.w, u.z)));
+                    const dfc v = dfc_add(dfc_of(md[p * o + j]), t);
+                    md[p * o + j] = dfc_f4(v);
+                    if (j == k + 1) atomicMax(&s_key[0][(k + 1) % 3], piv_key(fabsf(v.h.x) + fabsf(v.h.y), r));
                 }
             }
             group_bar(1);
@@ -979,55 +1015,53 @@ __global__ void __launch_bounds__(256, 5) k_overlap_oz(int n, int o, const float
         for (int e = tid; e < o * (IS - o); e += blockDim.x) inv[(e / (IS - o)) * IS + o + e % (IS - o)] = make_float2(0.f, 0.f);
     }
 
-    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out
+    // G_half[b, i] = sum_a W[i, a] inv[a, b] in fp32 -> split operand / green_out: a thread takes row il of
+    // a chunk and columns b0..b0+3; with W staged as (re, re, im, im) the products accumulate as pairs
+    //   A[b] += re W[i, a] inv[a, b],  B[b] += im W[i, a] inv[a, b]   (f32x2 fma, broadcast factors)
+    // and G_half[b, i] = (A.re - B.im, A.im + B.re).
     const double2* Wp = walkers + (size_t)w * n * o;
     __nv_bfloat16* re_row = split.ptr ? split.ptr + (size_t)w * split.ld : nullptr;
     __nv_bfloat16* im_row = split.ptr ? split.ptr + (size_t)(split.W + w) * split.ld : nullptr;
     double2* Gp = green_out ? green_out + (size_t)w * o * n : nullptr;
-    const int il = tid & 31, b0 = 4 * (tid >> 5);  // rows il and il + 32 of a chunk, columns b0..b0+3
+    const int il = tid & 31, b0 = 4 * (tid >> 5);
     for (int i0 = 0; i0 < n; i0 += OG_CH) {
         const int rows = min(OG_CH, n - i0);
         __syncthreads();
         for (int e = tid; e < rows * o; e += blockDim.x) {
             const double2 x = Wp[(size_t)i0 * o + e];
-            wf[(e / o) * ws + e % o] = make_float2(d2f_trunc(x.x), d2f_trunc(x.y));
+            const float xr = d2f_trunc(x.x), xi = d2f_trunc(x.y);
+            wf[(e / o) * ws + e % o] = make_float4(xr, xr, xi, xi);
         }
         __syncthreads();
         if (b0 >= o || il >= rows) continue;
-        const bool two = il + 32 < rows;
-        float2 a0[4], a1[4];
+        float2 A[4], B[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) a0[j] = a1[j] = make_float2(0.f, 0.f);
-        const float2* x0p = wf + il * ws;
-        const float2* x1p = wf + (two ? il + 32 : il) * ws;
-#pragma unroll 1
+        for (int j = 0; j < 4; ++j) A[j] = B[j] = make_float2(0.f, 0.f);
+        const float4* xp = wf + il * ws;
+#pragma unroll 2
         for (int a = 0; a < o; ++a) {
-            const float2 x0 = x0p[a], x1 = x1p[a];
+            const float4 x = xp[a];
             const float4 va = *(const float4*)(inv + a * IS + b0), vb = *(const float4*)(inv + a * IS + b0 + 2);
+            const float2 xr = make_float2(x.x, x.y), xi = make_float2(x.z, x.w);
             const float2 v[4] = {make_float2(va.x, va.y), make_float2(va.z, va.w), make_float2(vb.x, vb.y),
                                  make_float2(vb.z, vb.w)};
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                a0[j].x = fmaf(x0.x, v[j].x, a0[j].x); a0[j].x = fmaf(-x0.y, v[j].y, a0[j].x);
-                a0[j].y = fmaf(x0.x, v[j].y, a0[j].y); a0[j].y = fmaf(x0.y, v[j].x, a0[j].y);
-                a1[j].x = fmaf(x1.x, v[j].x, a1[j].x); a1[j].x = fmaf(-x1.y, v[j].y, a1[j].x);
-                a1[j].y = fmaf(x1.x, v[j].y, a1[j].y); a1[j].y = fmaf(x1.y, v[j].x, a1[j].y);
+                A[j] = __ffma2_rn(xr, v[j], A[j]);
+                B[j] = __ffma2_rn(xi, v[j], B[j]);
             }
         }
+        const int i = i0 + il;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int b = b0 + j;
-            if (b >= o) break;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1 && !two) break;
-                const int i = i0 + il + 32 * h;
-                const float2 g = h ? a1[j] : a0[j];
+            if (b < o) {
+                const float gr = A[j].x - B[j].y, gi = A[j].y + B[j].x;
                 if (re_row) {
-                    split_storef(re_row, split.S, b * n + i, g.x, true, split.sec);
-                    split_storef(im_row, split.S, b * n + i, g.y, true, split.sec);
+                    split_storef(re_row, split.S, b * n + i, gr, true, split.sec);
+                    split_storef(im_row, split.S, b * n + i, gi, true, split.sec);
                 }
-                if (Gp) Gp[(size_t)b * n + i] = make_double2(g.x, g.y);
+                if (Gp) Gp[(size_t)b * n + i] = make_double2(gr, gi);
             }
         }
     }

@@ -23,8 +23,8 @@
 // double-float m it replaces, given as a double-float pair.
 //
 // k_oz_m builds A itself: the walkers' rows are bulk-copied into shared
-// memory beside each B tile, eight producer warps cut them into digits and
-// write the 128-byte-swizzled A tile, one thread issues the MMAs, and eight
+// memory beside each B tile, sixteen producer warps cut them into digits and
+// write the 128-byte-swizzled A tile, one thread issues the MMAs, and four
 // epilogue warps recombine the digit sums from tensor memory.  A never goes
 // through HBM.
 #include "afq_internal.cuh"
@@ -60,20 +60,34 @@ __device__ __forceinline__ unsigned long long oz_fixed(double x, int E) {
     }
     return (unsigned long long)(X + OZ_OFF);
 }
-// digit s (1..7) of the offset value Y, as an exact fp32 integer
-__device__ __forceinline__ float oz_field(uint32_t v, int sh) {
-    return __int_as_float(0x4B000000 | ((v >> sh) & 127u)) - 8388672.f;  // (2^23 + field) - (2^23 + 64)
-}
 __device__ __forceinline__ uint32_t oz_bf2(float lo, float hi) {  // two small integers as a bf16 pair (exact)
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *(const uint32_t*)&v;
 }
-// Orbital i's eight K slots of an A row: w_1 .. w_7 and a zero.
-__device__ __forceinline__ uint4 oz_chunk(double x, int E) {
-    const unsigned long long Y = oz_fixed(x, E);
+// Orbital i's eight K slots of an A row (w_1 .. w_7 and a zero) from the two
+// words of x, with Ep = E + 1026, in 32-bit operations: the digits of |x| (of
+// |X| + OZ_OFF's base-128 fields f, each f - 64) times the sign of x, which
+// is again a balanced expansion (of X) with |digits| <= 64.  A digit is
+// fma(sign, 2^23 + f, -sign (2^23 + 64)), exact.
+__device__ __forceinline__ uint4 oz_chunk(uint32_t ulo, uint32_t uhi, int Ep) {
+    const int eb = (int)((uhi >> 20) & 0x7ffu), rs = Ep - eb;
+    uint32_t xl = 0, xh = 0;
+    if (eb != 0 && eb != 0x7ff && rs < 64) {
+        const uint32_t mh = (uhi & 0xfffffu) | 0x100000u;
+        if (rs < 32) {
+            xl = __funnelshift_r(ulo, mh, rs);
+            xh = mh >> rs;
+        } else {
+            xl = mh >> (rs - 32);
+        }
+    }
+    const unsigned long long Y = (((unsigned long long)xh << 32) | xl) + (unsigned long long)OZ_OFF;
     const uint32_t lo = (uint32_t)Y, hi = (uint32_t)(Y >> 28);
-    return make_uint4(oz_bf2(oz_field(hi, 14), oz_field(hi, 7)), oz_bf2(oz_field(hi, 0), oz_field(lo, 21)),
-                      oz_bf2(oz_field(lo, 14), oz_field(lo, 7)), oz_bf2(oz_field(lo, 0), 0.f));
+    const float sg = __int_as_float(0x3f800000u | (uhi & 0x80000000u)), c = -8388672.f * sg;
+#define OZ_F(v, sh) fmaf(sg, __int_as_float(0x4B000000u | (((v) >> (sh)) & 127u)), c)
+    return make_uint4(oz_bf2(OZ_F(hi, 14), OZ_F(hi, 7)), oz_bf2(OZ_F(hi, 0), OZ_F(lo, 21)),
+                      oz_bf2(OZ_F(lo, 14), OZ_F(lo, 7)), oz_bf2(OZ_F(lo, 0), 0.f));
+#undef OZ_F
 }
 __device__ __forceinline__ int oz_digit(double x, int E, int s) {  // w_s, s = 1..7
     const unsigned long long Y = oz_fixed(x, E);
@@ -124,12 +138,13 @@ __global__ void __launch_bounds__(256) k_oz_rowexp(int n, int o, const double2* 
 }
 
 constexpr int OZ_BM = 128;               // A rows a tile: two walkers of 64 rows (2 b + part, b < 32)
-constexpr int OZ_THREADS = 18 * 32;      // warp 0: copies, 1: MMA, 2-9: digits, 10-17: epilogue
-constexpr int OZ_PW0 = 2, OZ_EW0 = 10;   // first producer / epilogue warp
+constexpr int OZ_THREADS = 22 * 32;      // warp 0: copies, 1: MMA, 2-17: digits, 18-21: epilogue
+constexpr int OZ_PW0 = 2, OZ_EW0 = 18;   // first producer / epilogue warp
+constexpr int OZ_PWARPS = OZ_EW0 - OZ_PW0;
 constexpr int OZ_STG = 4;
 constexpr int OZ_A_BYTES = OZ_BM * 64 * 2;
 constexpr int OZ_SLOT_COLS = 256;        // tensor-memory columns between the two accumulators
-constexpr int OZ_SMEM_MAX = 227 * 1024;
+constexpr int OZ_SMEM_MAX = 226 * 1024;  // dynamic, beside the static shared memory
 
 struct OzGeo {
     int b_bytes, w_bytes, stage, smem;
@@ -148,6 +163,14 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                  "l"((unsigned long long)src), "r"(bytes), "r"(bar)
                  : "memory");
 }
+// L2 prefetch of bytes at src (16-byte aligned, a multiple of 16 bytes), 32 KB a request
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+    for (uint32_t off = 0; off < bytes; off += 32768u) {
+        const uint32_t len = min(32768u, bytes - off);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((unsigned long long)src + off), "r"(len)
+                     : "memory");
+    }
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
@@ -159,7 +182,7 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 
 // m of walkers 2 t, 2 t + 1 for the tiles t of this CTA (persistent).
 // Barriers a stage: ld_full (B tile and the walkers' rows landed), a_full
-// (the eight producer warps wrote the A tile), empty (the MMAs that read
+// (the producer warps wrote the A tile), empty (the MMAs that read
 // the stage finished).  Every wait is bounded; on a timeout the CTA raises
 // *err and every role unwinds (the copy thread waits, bounded, for its
 // copies, the MMA thread for its MMAs before the tensor memory is freed).
@@ -174,6 +197,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     uint64_t* bars = (uint64_t*)(smem + OZ_STG * geo.stage);
     uint32_t* tmem_slot = (uint32_t*)(bars + 3 * OZ_STG + 4 + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    __shared__ int s_fa[32];
     const uint32_t ldf0 = smem_u32(bars), af0 = smem_u32(bars + OZ_STG), emp0 = smem_u32(bars + 2 * OZ_STG);
     const uint32_t tfull0 = smem_u32(bars + 3 * OZ_STG), tempty0 = smem_u32(bars + 3 * OZ_STG + 2);
     const uint32_t drain = smem_u32(bars + 3 * OZ_STG + 4);
@@ -182,17 +206,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < OZ_STG; ++s) {
             mbar_init(ldf0 + 8 * s, 1);
-            mbar_init(af0 + 8 * s, 8);  // one arrival per producer warp
+            mbar_init(af0 + 8 * s, OZ_PWARPS);  // one arrival per producer warp
             mbar_init(emp0 + 8 * s, 1);
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, 256);  // every epilogue thread
+            mbar_init(tempty0 + 8 * a, 128);  // every epilogue thread
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (threadIdx.x < o) s_fa[threadIdx.x] = fa[threadIdx.x];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(2 * OZ_SLOT_COLS)
@@ -213,8 +238,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             uint32_t issued_par[OZ_STG];
             for (int s = 0; s < OZ_STG; ++s) issued[s] = 0;
             bool ok = true;
+            // the walkers' rows reach shared memory from L2: this tile's and, a tile ahead, the next one's
+            if (blockIdx.x < ntiles)
+                bulk_prefetch_l2(walkers + (size_t)2 * blockIdx.x * n * o,
+                                 (uint32_t)(min(2, W - 2 * (int)blockIdx.x) * n * o * 16));
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 const int nw = min(2, W - 2 * t);
+                if (t + (int)gridDim.x < ntiles) {
+                    const int tn = t + gridDim.x;
+                    bulk_prefetch_l2(walkers + (size_t)2 * tn * n * o, (uint32_t)(min(2, W - 2 * tn) * n * o * 16));
+                }
                 for (int kk = 0; kk < nks; ++kk) {
                     if (!mbar_wait(emp0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
@@ -248,8 +281,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             bool ok = true;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 for (int kk = 0; kk < nks; ++kk) {
-                    if (!mbar_wait(af0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
-                    if (!mbar_wait(ldf0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    // the producers waited for the copies of this stage before writing A
+                    if (!mbar_wait_inl(af0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait_inl(ldf0 + 8 * stage, phase, abort_flag)) { ok = false; break; }
                     if (kk == 0 && !mbar_wait(tempty0 + 8 * slot, slot_phase ^ 1, abort_flag)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t a0 = smem_u32(smem + stage * geo.stage), b0 = a0 + OZ_A_BYTES;
@@ -273,7 +307,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_wait(drain, 0, nullptr);
         }
     } else if (warp < OZ_EW0) {
-        // producers: row r of the tile, orbitals 4 h .. 4 h + 3 of each K step
+        // producers: row r of the tile, orbitals 2 h, 2 h + 1 of each K step
         const int p = threadIdx.x - 32 * OZ_PW0, r = p & (OZ_BM - 1), h = p >> 7;
         const int wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
         int stage = 0;
@@ -284,6 +318,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const bool valid = w < W && b < o;
             int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
             if (E == OZ_NONFINITE) E = 0;  // digits of no use: the epilogue writes nan for the row
+            const int Ep = E + 1026;
             for (int kk = 0; kk < nks; ++kk) {
                 if (!mbar_wait(ldf0 + 8 * stage, phase, abort_flag)) {
                     atomicExch(err, 1);
@@ -292,16 +327,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     break;
                 }
                 uint8_t* st = smem + stage * geo.stage;
-                const double* wrow = (const double*)(st + OZ_A_BYTES + geo.b_bytes + wl * 8 * o * 16) + part;
+                const uint2* wrow = (const uint2*)(st + OZ_A_BYTES + geo.b_bytes + wl * 8 * o * 16) + part;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int ii = 4 * h + u;
-                    const double x = (valid && 8 * kk + ii < n) ? wrow[2 * (ii * o + b)] : 0.0;
-                    const uint4 c = oz_chunk(x, E);
-                    const uint32_t dst = smem_u32(st) + r * 128 + ((ii ^ (r & 7)) << 4);
-                    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(c.x), "r"(c.y), "r"(c.z),
-                                 "r"(c.w)
-                                 : "memory");
+                for (int u = 0; u < 2; ++u) {
+                    const int ii = 2 * h + u;
+                    const uint2 x = (valid && 8 * kk + ii < n) ? wrow[2 * (ii * o + b)] : make_uint2(0u, 0u);
+                    *(uint4*)(st + r * 128 + ((ii ^ (r & 7)) << 4)) = oz_chunk(x.x, x.y, Ep);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
@@ -311,7 +342,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         }
     } else {
         // epilogue: this warp's 32 rows (lane quadrant q), half the trial orbitals
-        const int q = warp & 3, hh = (warp - OZ_EW0) >> 2, oe = o + (o & 1);
+        const int q = warp & 3;
         const int r = 32 * q + lane, wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
         int slot = 0;
         uint32_t slot_phase = 0;
@@ -325,39 +356,31 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const int w = 2 * t + wl;
             const bool valid = w < W && b < o;
             const int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
-            for (int a = hh * (oe / 2); a < (hh + 1) * (oe / 2); ++a) {
+            for (int a = 0; a < o; ++a) {
                 uint32_t v[8];
                 __syncwarp();
                 tmem_ld8(tmem + slot * OZ_SLOT_COLS + 8 * a + ((uint32_t)(32 * q) << 16), v);
-                if (valid && a < o) {
-                // Q0 = D_2 2^21 + D_3 2^14 + D_4 2^7 + D_5 and Q1 the same for D_6..9 (exact 64-bit
-                // integers), m = (Q0 2^-35 + Q1 2^-63) 2^(E + F) as a double-float pair
-                long long Q[2];
+                if (valid) {
+                    // the terms D_d 2^(-7 d) are exact in fp32 (|D_d| < 2^24); their sum as a
+                    // double-float pair by two-sums from the smallest, then scaled by 2^(E + F)
+                    float sm = __uint_as_float(v[7]) * 0x1p-63f, er2 = 0.f;
 #pragma unroll
-                for (int hq = 0; hq < 2; ++hq) {
-                    long long qv = 0;
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) qv = qv * 128 + (long long)__float2int_rn(__uint_as_float(v[4 * hq + u]));
-                    Q[hq] = qv;
-                }
-                float2 out;
-                if (E == OZ_NONFINITE) {
-                    out = make_float2(__int_as_float(0x7fc00000), 0.f);
-                } else {
-                    // Q0 = qh 2^21 + ql with qh, ql exact in fp32: (hi, lo) = two-sum of the two
-                    // exact terms, then the Q1 term (~2^-28 of Q0's range) into lo
-                    const long long q0 = Q[0];
-                    const long long qh = q0 >> 21, ql = q0 - (qh << 21);
-                    const int sc = E + fa[a];
-                    const float th = ldexpf((float)qh, sc - 14), tm = ldexpf((float)ql, sc - 35);
-                    const float hi = th + tm;
-                    const float bb = hi - th;
-                    const float e0 = (th - (hi - bb)) + (tm - bb);
-                    const float lo = e0 + ldexpf((float)Q[1], sc - 63);
-                    const float h2 = hi + lo;
-                    out = make_float2(h2, lo - (h2 - hi));
-                }
-                mout[(((size_t)w * o + a) * o + b) * 2 + part] = out;
+                    for (int d = 8; d >= 2; --d) {
+                        const float tt = __uint_as_float(v[d - 2]) * __int_as_float((127 - 7 * d) << 23);
+                        const float s2 = sm + tt, bb = s2 - sm;
+                        er2 += (sm - (s2 - bb)) + (tt - bb);
+                        sm = s2;
+                    }
+                    const float hi = sm + er2, lo = er2 - (hi - sm);
+                    float2 out;
+                    if (E == OZ_NONFINITE) {
+                        out = make_float2(__int_as_float(0x7fc00000), 0.f);
+                    } else {
+                        const int sc = E + s_fa[a];
+                        const float p2 = (unsigned)(sc + 126) < 253u ? __int_as_float((sc + 127) << 23) : ldexpf(1.f, sc);
+                        out = make_float2(hi * p2, lo * p2);
+                    }
+                    mout[(((size_t)w * o + a) * o + b) * 2 + part] = out;
                 }
             }
             tc_fence_before();
