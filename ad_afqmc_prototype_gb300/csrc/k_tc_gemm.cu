@@ -252,6 +252,25 @@ struct ExchOut {
     int nhalf = 0;   // column halves per row = 2 x column tiles
 };
 
+// Transpose, in each half-warp, of a 16 x 16 block of 32-bit words held one
+// row a lane (v[j] = word j of row `lane`) into one column a lane (v[r] =
+// word lane & 15 of row 16 (lane >> 4) + r): four butterfly stages, each
+// lane trading half of its words with lane ^ d.
+__device__ __forceinline__ void halfwarp_transpose16(uint32_t (&v)[16], int lane) {
+#pragma unroll
+    for (int d = 8; d >= 1; d >>= 1) {
+        const bool upper = (lane & d) != 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (j & d) continue;
+            const uint32_t send = upper ? v[j] : v[j | d];
+            const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, d);
+            if (upper) v[j] = recv;
+            else v[j | d] = recv;
+        }
+    }
+}
+
 // MODE 0: fp32 C.  MODE 1 (split): the two-piece bf16 split of each sum to
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
 // exchange contraction of each 32 x 32 block (ExchOut) instead of C.
@@ -464,6 +483,38 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             }
             const int row = mb * BM + q * 32 + lane;
             const int col0 = nb * BNT + cb;
+            if constexpr (SPLIT && CW == 64) {
+                // the warp's 32 rows x 64 columns of bf16 pairs (hi, mid) in 16-word halves, each
+                // transposed within the half-warps so that one store writes 64 contiguous bytes
+                // (two whole sectors) of each of two rows
+                if (vec && col0 + CW <= N && __activemask() == 0xffffffffu) {
+                    const int rw = mb * BM + q * 32 + 16 * (lane >> 4), wc = lane & 15;
+#pragma unroll
+                    for (int half = 0; half < 2; ++half) {
+                        uint32_t hv[16], mv[16];
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float2 a = acc[16 * half + j];
+                            const __nv_bfloat162 h = __floats2bfloat162_rn(a.x, a.y);
+                            const float2 hf = __bfloat1622float2(h);
+                            const __nv_bfloat162 m = __floats2bfloat162_rn(a.x - hf.x, a.y - hf.y);
+                            hv[j] = *(const uint32_t*)&h;
+                            mv[j] = *(const uint32_t*)&m;
+                        }
+                        halfwarp_transpose16(hv, lane);
+                        halfwarp_transpose16(mv, lane);
+                        const long long c = col0 + 32 * half + 2 * wc;
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) {
+                            if (rw + r < M) {
+                                __stcs((uint32_t*)(Ch + (long long)(rw + r) * ldc + c), hv[r]);
+                                __stcs((uint32_t*)(Cm + (long long)(rw + r) * ldc + c), mv[r]);
+                            }
+                        }
+                    }
+                    continue;
+                }
+            }
             if (row < M && SPLIT) {
                 __nv_bfloat16* dh = Ch + (long long)row * ldc + col0;
                 __nv_bfloat16* dm = Cm + (long long)row * ldc + col0;

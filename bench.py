@@ -133,9 +133,11 @@ def phase_work(n, o, G, W, trial_real=True, precision="fp64", n_terms=6):
     without the padding of its exchange-fused layout; the Taylor kernel's
     128 x N x 16 MMAs, N = norb rounded up to 16, two a K step (V's hi and mid
     pieces) over K = 2 N per V product and N per E - I product: 256 (4
-    n_terms + 4) N^2 per walker), the exchange step the bytes it must read.  The overlap,
-    Green's function and QR phases of the mixed forms run double-float
-    arithmetic on the fp32 pipe ("df32"): no algorithmic-flop roofline."""
+    n_terms + 4) N^2 per walker), the exchange step the bytes it must read.  The overlap
+    and Green's-function phases of the mixed forms form m = C^T W on the tensor
+    cores from integer digit slices and run the LU, the inverse and G_half on
+    the fp32 pipe; they and the QR (double-float arithmetic) are "df32": their
+    algorithmic flops are taken against the fp32 SIMT peak."""
     cm = 4 if trial_real else 8  # complex x real vs complex x complex multiply-add
     work = {
         "vbuild_gemm": (4.0 * G * n * n * W, "fp64"),
@@ -240,7 +242,10 @@ def roofline_for(phases, work, lib, steps, name=None, alg=None):
     out = {**common, "bound": ppipe, "achieved": round(achieved, 4), "peak": peak, "unit": "TFLOP/s",
            "frac": round(achieved / peak, 4) if peak else None, "peak_source": src,
            "work": "algorithmic flops (the reference's formulas, FP64-counted)"}
-    if pipe == "df32":
+    if pipe == "df32" and dname in ("overlap", "green"):
+        out["executed"] = ("m = C^T W as exact bf16 digit products on the tensor cores; LU (double-float) "
+                           "and inverse, G_half (fp32) on the fp32 pipe")
+    elif pipe == "df32":
         out["executed"] = "double-float (fp32 pairs) arithmetic on the fp32 pipe, ~10 instructions per flop"
     elif executed != algo:
         ex = executed * mult / (ms_block / 1000.0) / 1e12
