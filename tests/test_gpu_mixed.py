@@ -140,9 +140,11 @@ def test_mixed_block_energy_error_per_block(cuda, prec):
 
 
 def test_mixed_overlap_matches_binary64(cuda):
-    """The mixed forms form m = C^H W in double-float arithmetic (fp32 pairs,
-    ~2^-44): after a block of zero steps (QR, overlap, energy, comb) the
-    overlaps agree with the binary64 form's to 1e-10 relative."""
+    """The mixed forms form m = C^H W from exact integer digit products on the
+    tensor cores (nocc <= 32; double-float arithmetic beyond), ~2^-44 of the
+    entries' scale, and its LU in double-float: after a block of zero steps
+    (QR, overlap, energy, comb) the overlaps agree with the binary64 form's
+    to 1e-10 relative."""
     from ad_afqmc_prototype_gb300 import engine
     W = 64
     pa, pra, st = _setup("c4_n200_o30_g1000_w4096", W, "fp64", n_prop_steps=3)
@@ -157,6 +159,32 @@ def test_mixed_overlap_matches_binary64(cuda):
     engine.block(pb, z0b, y, 5, 100, zeta=0.5)
     assert engine.workspace_status() == 0
     rel = float(((x.overlaps - y.overlaps).abs() / x.overlaps.abs()).max().item())
+    assert rel < 1e-10, rel
+
+
+@pytest.mark.parametrize("n,o,G,W", [(45, 7, 60, 33), (12, 6, 48, 9), (100, 31, 200, 17), (37, 1, 40, 5),
+                                     (200, 30, 300, 3)])
+def test_tensor_core_overlap_shapes(cuda, n, o, G, W):
+    """The tensor-core m at ragged shapes: norb not a multiple of the eight
+    orbitals of a K step (a short last copy), nocc odd (a zero pad row pair in
+    B), an odd walker count (a last tile of one walker), nocc 1 and 31.
+    Overlaps after a block of zero steps against the binary64 form, 1e-10
+    relative."""
+    from ad_afqmc_prototype_gb300 import engine, synth
+    wl = synth.Workload(name=f"oz_n{n}_o{o}_g{G}", nbasis=n, nocc=o, nchol=G, n_walkers=W, n_steps=3, seed=7)
+    pa, pra, st = _setup(wl, W, "fp64", n_prop_steps=3)
+    pb, prb, _ = _setup(wl, W, "mixed_fast", n_prop_steps=3)
+    a = _dstate(st)
+    engine.block(pa, pra, a, 5, 0)  # move the walkers off the trial
+    z0a = pra.__class__(**{**pra.__dict__, "n_prop_steps": 0})
+    z0b = prb.__class__(**{**prb.__dict__, "n_prop_steps": 0})
+    x = engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)])
+    y = engine.DeviceState(*[t.clone() for t in (a.walkers, a.weights, a.overlaps, a.pop_shift, a.e_estimate)])
+    engine.block(pa, z0a, x, 5, 100, zeta=0.5)
+    engine.block(pb, z0b, y, 5, 100, zeta=0.5)
+    assert engine.workspace_status() == 0
+    rel = float(((x.overlaps - y.overlaps).abs() / x.overlaps.abs()).max().item())
+    print(f"n={n} o={o} W={W}: max relative overlap difference {rel:.3e}")
     assert rel < 1e-10, rel
 
 
