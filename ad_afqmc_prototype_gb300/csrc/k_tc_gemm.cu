@@ -275,17 +275,32 @@ __device__ __forceinline__ void halfwarp_transpose16(uint32_t (&v)[16], int lane
 // Ch (hi) and Cm (mid = bf16(c - hi)), same row stride ldc.  MODE 2: the
 // exchange contraction of each 32 x 32 block (ExchOut) instead of C.
 //
+// Tile order of the persistent schedule: order < 0, N tiles fastest; order =
+// gm > 0, M tiles fastest within groups of gm M tiles (all N tiles of a group
+// before the next group).
+__device__ __forceinline__ void drain_tile(int t, int mt, int nt, int order, int& mb, int& nb) {
+    if (order < 0) {
+        mb = t / nt;
+        nb = t % nt;
+        return;
+    }
+    const int g = t / (order * nt), r = t - g * order * nt, m0 = g * order, gsz = min(order, mt - m0);
+    mb = m0 + r % gsz;
+    nb = r / gsz;
+}
+
 // Each CTA loads its own A and B tiles with plain TMA copies.  Tile order:
-// with M tiles fastest (nfast = 0) the CTAs resident at one time work on one
-// or two N tiles, so a B tile is read from DRAM about once and served from L2
-// to the CTAs that share it, while A is re-read from L2 once per N tile; the
-// launcher picks N tiles fastest (nfast = 1) when A is the large operand and
-// B fits in L2.
+// with M tiles fastest the CTAs resident at one time work on one or two N
+// tiles, so a B tile is read from DRAM about once and served from L2 to the
+// CTAs that share it, while the group's A tiles are re-read from L2 once per
+// N tile; the launcher picks N tiles fastest when A is the large operand and
+// B fits in L2, and groups the M tiles when neither fits (each group's A then
+// stays in L2 beside the output stream, B is read once per group).
 template <int BNT, int MODE, int EWN>
 __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
     k_gemm_tn_drain(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     float* __restrict__ C, __nv_bfloat16* __restrict__ Ch, __nv_bfloat16* __restrict__ Cm, int M,
-                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo, int nfast) {
+                    int N, int K, long long ldc, int kd, int* __restrict__ err, ExchOut xo, int order) {
     using D = Drain<BNT, EWN>;
     static_assert(MODE != 2 || EWN == 8, "the exchange epilogue's transpose buffers are sized for eight warps");
     constexpr bool SPLIT = MODE == 1;
@@ -341,7 +356,8 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
             for (int s = 0; s < STG; ++s) issued[s] = 0;
             bool ok = true;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-                const int mb = nfast ? t / nt : t % mt, nb = nfast ? t % nt : t / mt;
+                int mb, nb;
+                drain_tile(t, mt, nt, order, mb, nb);
                 for (int kb = 0; kb < kt; ++kb) {
                     if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag)) { ok = false; break; }
                     issued[stage] = 0;
@@ -404,7 +420,8 @@ __global__ void __launch_bounds__(Drain<BNT, EWN>::THREADS, 1)
                                : (ldc % 4) == 0 && (((uintptr_t)C) & 15) == 0;
         bool ok = true;
         for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-            const int mb = nfast ? t / nt : t % mt, nb = nfast ? t % nt : t / mt;
+            int mb, nb;
+            drain_tile(t, mt, nt, order, mb, nb);
             float2 acc[CW / 2];
 #pragma unroll
             for (int j = 0; j < CW / 2; ++j) acc[j] = make_float2(0.f, 0.f);
@@ -598,7 +615,7 @@ int launch_tc_gemm_tn(int M, int N, int K, const void* A, long long lda, const v
 template <int BNT, int MODE, int EWN>
 static int launch_drain(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
                         __nv_bfloat16* Ch, __nv_bfloat16* Cm, long long ldc, int kd, int* err, cudaStream_t s,
-                        tc::ExchOut xo = tc::ExchOut{}) {
+                        tc::ExchOut xo = tc::ExchOut{}, int mgroup = 0) {
     using namespace tc;
     static DeviceOnce smem_once;
     constexpr int SMEM = Drain<BNT, EWN>::SMEM + (MODE == 2 ? XT_BYTES : 0);
@@ -614,11 +631,20 @@ static int launch_drain(int M, int N, int K, const void* A, long long lda, const
     // tile order: the operand re-read once per tile of the other should fit in
     // L2 beside the streams; if A does not and B does, N tiles run fastest (the
     // force-bias and energy GEMMs: full-size DRAM reads within 1.1x of the
-    // operands' bytes)
-    constexpr long long kL2Keep = 48LL << 20;
+    // operands' bytes); if neither does, M tiles run fastest in groups whose A
+    // tiles take at most kAGroup bytes (the V-build)
+    constexpr long long kL2Keep = 48LL << 20, kAGroup = 32LL << 20;
+    const int mt = (M + BM - 1) / BM;
     const long long a_bytes = (long long)M * K * 2, b_bytes = (long long)N * K * 2;
-    const int nfast = (a_bytes > kL2Keep && b_bytes <= kL2Keep) ? 1 : 0;
-    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo, nfast);
+    int order;
+    if (a_bytes > kL2Keep && b_bytes <= kL2Keep) {
+        order = -1;
+    } else {
+        const long long tile_a = (long long)BM * K * 2;
+        const int ng = (int)(((long long)mt * tile_a + kAGroup - 1) / kAGroup);
+        order = mgroup > 0 ? mgroup : (mt + ng - 1) / ng;
+    }
+    kern<<<grid, Drain<BNT, EWN>::THREADS, SMEM, s>>>(ma, mb, C, Ch, Cm, M, N, K, ldc, kd, err, xo, order);
     AFQ_LAUNCHED(MODE == 2 ? "k_gemm_tn_drain(exchange)" : "k_gemm_tn_drain");
     return AFQ_OK;
 }

@@ -36,7 +36,7 @@ SPLIT_SECTIONS = {"mixed": 6, "mixed_fast": 3}
 # DRAM bytes (read + write) per launch of a kernel, from one ncu capture of this bench's own command
 # (profiles/launches_block_c4_n200_o30_g1000_w4096_mixed_fast.md), keyed by (workload, precision,
 # walkers, phase); the roofline reports them beside the algorithmic bytes
-MEASURED_TRAFFIC = {("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "vbuild_gemm"): 1492193280 + 1410662400,
+MEASURED_TRAFFIC = {("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "vbuild_gemm"): 564473600 + 1283924736,
                     ("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "trotter"): 1741291520 + 368705536,
                     ("c4_n200_o30_g1000_w4096", "mixed_fast", 4096, "fb_gemm"): 368115712 + 19635200}
 
