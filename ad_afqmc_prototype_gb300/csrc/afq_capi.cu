@@ -129,7 +129,6 @@ struct StepWS {
     float2* csplit;     // n*o: trial orbitals as (hi, lo) fp32 pairs (double-float overlap)
     // m = C^T W on the tensor cores from integer digit slices (k_ozaki.cu), nocc <= 32
     __nv_bfloat16* ozB;  // NB x K: the trial's digit rows
-    int* ozE;            // W x 64: row exponents
     int* ozF;            // o: column exponents
     float2* ozM;         // W o o x 2: m as double-float pairs
 };
@@ -160,7 +159,6 @@ static StepWS layout_step(Arena& a, const afq_dims* d, int n_chunks) {
         if (oz_supported(d)) {
             const OzDims z = oz_dims((int)n, (int)o);
             s.ozB = a.take<__nv_bfloat16>((size_t)z.NB * z.K);
-            s.ozE = a.take<int>(64 * W);
             s.ozF = a.take<int>(64);
             s.ozM = a.take<float2>(W * o * o * 2);
         }
@@ -309,7 +307,7 @@ static int overlap_mixed(const afq_problem* pb, double2* walk, double2* ovl, Spl
     const double2* mo = (const double2*)pb->mo_coeff;
     if (ws.ozB) {
         AFQ_TRY(launch_oz_split_c(n, o, mo, ws.ozB, ws.ozF, s));
-        AFQ_TRY(launch_oz_m(W, n, o, walk, ws.ozB, ws.ozF, ws.ozE, ws.ozM, ws.status, s));
+        AFQ_TRY(launch_oz_m(W, n, o, walk, ws.ozB, ws.ozF, ws.ozM, ws.status, s));
         return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit, (const float4*)ws.ozM);
     }
     return launch_overlap_split(W, n, o, mo, walk, ovl, split, s, green_out, ws.csplit);

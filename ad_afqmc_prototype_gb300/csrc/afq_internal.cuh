@@ -381,9 +381,9 @@ constexpr int OZ_NONFINITE = 0x7fffffff;  // E_r of a row holding inf or nan
 OzDims oz_dims(int n, int o);
 // B (NB x K) and F_a (o) from the trial orbitals
 int launch_oz_split_c(int n, int o, const double2* mo, __nv_bfloat16* B, int* fa, cudaStream_t s);
-// m[((w o + a) o + b) 2 + part] (double-float pairs) from the walkers; er: W x 64 row exponents (scratch)
-int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, int* er,
-                float2* m, int* err, cudaStream_t s);
+// m[((w o + a) o + b) 2 + part] (double-float pairs) from the walkers
+int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, float2* m,
+                int* err, cudaStream_t s);
 int launch_split_c(int count, const double2* mo, float2* cs, cudaStream_t s);
 int launch_cholqr2(int W, int n, int o, const double2* win, double2* wout, double2* det_r, cudaStream_t s);
 // k_cv.cu, k_mlp.cu

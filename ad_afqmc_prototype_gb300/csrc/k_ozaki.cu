@@ -119,32 +119,15 @@ __global__ void __launch_bounds__(256) k_oz_split_c(int n, int o, const double2*
     }
 }
 
-// E_r of every row (walker, b, part) of A: er[w 64 + 2 b + part]; one CTA per
-// walker, four threads a row.
-__global__ void __launch_bounds__(256) k_oz_rowexp(int n, int o, const double2* __restrict__ walkers,
-                                                   int* __restrict__ er) {
-    __shared__ int s_e[4][64];
-    const int w = blockIdx.x, r = threadIdx.x & 63, ph = threadIdx.x >> 6, b = r >> 1;
-    const double* Wp = (const double*)(walkers + (size_t)w * n * o) + (r & 1);
-    int e = 0;
-    if (b < o)
-        for (int i = ph; i < n; i += 4) e = max(e, oz_ebits(Wp[2 * ((size_t)i * o + b)]));
-    s_e[ph][r] = e;
-    __syncthreads();
-    if (threadIdx.x < 64) {
-        const int m = max(max(s_e[0][r], s_e[1][r]), max(s_e[2][r], s_e[3][r]));
-        er[(size_t)w * 64 + r] = b >= o ? 0 : m == 0x7ff ? OZ_NONFINITE : m - 1020;
-    }
-}
-
 constexpr int OZ_BM = 128;               // A rows a tile: two walkers of 64 rows (2 b + part, b < 32)
-constexpr int OZ_THREADS = 22 * 32;      // warp 0: copies, 1: MMA, 2-17: digits, 18-21: epilogue
-constexpr int OZ_PW0 = 2, OZ_EW0 = 18;   // first producer / epilogue warp
+constexpr int OZ_THREADS = 26 * 32;      // warp 0: copies, 1: MMA, 2-17: digits, 18-21: epilogue, 22-25: E_r
+constexpr int OZ_PW0 = 2, OZ_EW0 = 18, OZ_XW0 = 22;  // first producer / epilogue / exponent warp
 constexpr int OZ_PWARPS = OZ_EW0 - OZ_PW0;
 constexpr int OZ_STG = 4;
 constexpr int OZ_A_BYTES = OZ_BM * 64 * 2;
 constexpr int OZ_SLOT_COLS = 256;        // tensor-memory columns between the two accumulators
-constexpr int OZ_SMEM_MAX = 226 * 1024;  // dynamic, beside the static shared memory
+// dynamic shared memory of the largest layout (nocc 32: B 32 KB, walker rows 8 KB a stage), beside ~1 KB static
+constexpr int OZ_SMEM_MAX = OZ_STG * (OZ_A_BYTES + 32 * 1024 + 8 * 1024) + 1024 + 256;
 
 struct OzGeo {
     int b_bytes, w_bytes, stage, smem;
@@ -183,24 +166,30 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 // m of walkers 2 t, 2 t + 1 for the tiles t of this CTA (persistent).
 // Barriers a stage: ld_full (B tile and the walkers' rows landed), a_full
 // (the producer warps wrote the A tile), empty (the MMAs that read
-// the stage finished).  Every wait is bounded; on a timeout the CTA raises
-// *err and every role unwinds (the copy thread waits, bounded, for its
-// copies, the MMA thread for its MMAs before the tensor memory is freed).
+// the stage finished).  The row scales E_r of a tile (two above the largest
+// binary64 exponent of the row, OZ_NONFINITE for a row holding inf or nan)
+// are found by four warps a tile ahead, into one of two shared slots: e_full
+// (written), e_empty (the producers and the epilogue have read them).
+// Every wait is bounded; on a timeout the CTA raises *err and every role
+// unwinds (the copy thread waits, bounded, for its copies, the MMA thread
+// for its MMAs before the tensor memory is freed).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_m(const __grid_constant__ CUtensorMap tmB, int W, int n, int o, const double2* __restrict__ walkers,
-           const int* __restrict__ er, const int* __restrict__ fa, float2* __restrict__ mout, int* __restrict__ err) {
+           const int* __restrict__ fa, float2* __restrict__ mout, int* __restrict__ err) {
     using namespace tc;
     const OzGeo geo = oz_geo(o);
     const int NB = 8 * (o + (o & 1)), nks = (n + 7) / 8, ntiles = (W + 1) / 2;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + OZ_STG * geo.stage);
-    uint32_t* tmem_slot = (uint32_t*)(bars + 3 * OZ_STG + 4 + 1);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 3 * OZ_STG + 4 + 1 + 4);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
     __shared__ int s_fa[32];
+    __shared__ int s_er[2][OZ_BM];
     const uint32_t ldf0 = smem_u32(bars), af0 = smem_u32(bars + OZ_STG), emp0 = smem_u32(bars + 2 * OZ_STG);
     const uint32_t tfull0 = smem_u32(bars + 3 * OZ_STG), tempty0 = smem_u32(bars + 3 * OZ_STG + 2);
     const uint32_t drain = smem_u32(bars + 3 * OZ_STG + 4);
+    const uint32_t exf0 = smem_u32(bars + 3 * OZ_STG + 5), exe0 = smem_u32(bars + 3 * OZ_STG + 7);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
@@ -214,6 +203,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_init(tempty0 + 8 * a, 128);  // every epilogue thread
         }
         mbar_init(drain, 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(exf0 + 8 * a, OZ_THREADS / 32 - OZ_XW0);        // one arrival per exponent warp
+            mbar_init(exe0 + 8 * a, OZ_PWARPS + (OZ_XW0 - OZ_EW0));  // producer and epilogue warps
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -313,11 +306,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         int stage = 0;
         uint32_t phase = 0;
         bool ok = true;
-        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+        for (int t = blockIdx.x, it = 0; ok && t < ntiles; t += gridDim.x, ++it) {
             const int w = 2 * t + wl;
             const bool valid = w < W && b < o;
-            int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
-            if (E == OZ_NONFINITE) E = 0;  // digits of no use: the epilogue writes nan for the row
+            if (!mbar_wait(exf0 + 8 * (it & 1), (it >> 1) & 1, abort_flag)) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                break;
+            }
+            int E = s_er[it & 1][r];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(exe0 + 8 * (it & 1));
+            if (!valid || E == OZ_NONFINITE) E = 0;  // digits of no use: the epilogue writes nan for the row
             const int Ep = E + 1026;
             for (int kk = 0; kk < nks; ++kk) {
                 if (!mbar_wait(ldf0 + 8 * stage, phase, abort_flag)) {
@@ -340,14 +340,46 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 if (++stage == OZ_STG) { stage = 0; phase ^= 1; }
             }
         }
+    } else if (warp >= OZ_XW0) {
+        // E_r of each row of the CTA's tiles, a tile ahead of the producers: row x of a tile by thread x,
+        // the largest biased exponent over the walker's orbitals (8-byte loads, a warp's lanes contiguous)
+        const int x = threadIdx.x - 32 * OZ_XW0, wl = x >> 6, b = (x & 63) >> 1, part = x & 1;
+        for (int t = blockIdx.x, it = 0; t < ntiles; t += gridDim.x, ++it) {
+            if (!mbar_wait(exe0 + 8 * (it & 1), ((it >> 1) & 1) ^ 1, abort_flag)) {
+                atomicExch(err, 1);
+                *abort_flag = 1;
+                break;
+            }
+            const int w = 2 * t + wl;
+            int e = 0;
+            if (w < W && b < o) {
+                const unsigned long long* Wq =
+                    (const unsigned long long*)(walkers + (size_t)w * n * o + b) + part;
+                int e1 = 0, e2 = 0, e3 = 0;
+                int i = 0;
+                for (; i + 4 <= n; i += 4) {
+                    e = max(e, (int)((Wq[2 * (size_t)i * o] >> 52) & 0x7ffu));
+                    e1 = max(e1, (int)((Wq[2 * (size_t)(i + 1) * o] >> 52) & 0x7ffu));
+                    e2 = max(e2, (int)((Wq[2 * (size_t)(i + 2) * o] >> 52) & 0x7ffu));
+                    e3 = max(e3, (int)((Wq[2 * (size_t)(i + 3) * o] >> 52) & 0x7ffu));
+                }
+                for (; i < n; ++i) e = max(e, (int)((Wq[2 * (size_t)i * o] >> 52) & 0x7ffu));
+                e = max(max(e, e1), max(e2, e3));
+                e = e == 0x7ff ? OZ_NONFINITE : e - 1020;
+            }
+            s_er[it & 1][x] = e;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(exf0 + 8 * (it & 1));
+        }
     } else {
         // epilogue: this warp's 32 rows (lane quadrant q), half the trial orbitals
         const int q = warp & 3;
         const int r = 32 * q + lane, wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
         int slot = 0;
         uint32_t slot_phase = 0;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            if (!mbar_wait_inl(tfull0 + 8 * slot, slot_phase, abort_flag)) {
+        for (int t = blockIdx.x, it = 0; t < ntiles; t += gridDim.x, ++it) {
+            if (!mbar_wait_inl(tfull0 + 8 * slot, slot_phase, abort_flag) ||
+                !mbar_wait_inl(exf0 + 8 * (it & 1), (it >> 1) & 1, abort_flag)) {
                 atomicExch(err, 1);
                 *abort_flag = 1;
                 break;
@@ -355,7 +387,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             tc_fence_after();
             const int w = 2 * t + wl;
             const bool valid = w < W && b < o;
-            const int E = valid ? er[(size_t)w * 64 + (r & 63)] : 0;
+            const int E = s_er[it & 1][r];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(exe0 + 8 * (it & 1));
             for (int a = 0; a < o; ++a) {
                 uint32_t v[8];
                 __syncwarp();
@@ -410,8 +444,8 @@ int launch_oz_split_c(int n, int o, const double2* mo, __nv_bfloat16* B, int* fa
     return AFQ_OK;
 }
 
-int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, int* er,
-                float2* m, int* err, cudaStream_t s) {
+int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16* B, const int* fa, float2* m,
+                int* err, cudaStream_t s) {
     using namespace tc;
     if (W <= 0) return AFQ_OK;
     if (o > 32) return fail(AFQ_E_UNSUPPORTED, "ozaki m: nocc=%d > 32", o);
@@ -419,8 +453,6 @@ int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16
     const OzDims z = oz_dims(n, o);
     const OzGeo g = oz_geo(o);
     if (g.smem > OZ_SMEM_MAX) return fail(AFQ_E_UNSUPPORTED, "ozaki m: %d bytes of shared memory", g.smem);
-    k_oz_rowexp<<<W, 256, 0, s>>>(n, o, walkers, er);
-    AFQ_LAUNCHED("k_oz_rowexp");
     AFQ_TRY(get_encode());
     CUtensorMap mb;
     AFQ_TRY(make_map(&mb, B, z.NB, z.K, z.K, z.NB));
@@ -428,7 +460,7 @@ int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16
     AFQ_TRY(device_sms(&sms));
     AFQ_TRY(raise_smem_once(g_oz_smem, k_oz_m, OZ_SMEM_MAX));
     const int tiles = (W + 1) / 2, grid = tiles < sms ? tiles : sms;
-    k_oz_m<<<grid, OZ_THREADS, g.smem, s>>>(mb, W, n, o, walkers, er, fa, m, err);
+    k_oz_m<<<grid, OZ_THREADS, g.smem, s>>>(mb, W, n, o, walkers, fa, m, err);
     AFQ_LAUNCHED("k_oz_m");
     return AFQ_OK;
 }
