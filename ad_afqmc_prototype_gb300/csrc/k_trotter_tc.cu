@@ -271,6 +271,9 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         const int L = 32 * q4 + lane, c = L >> 2, p = (L >> 1) & 1, q = L & 1;
         const bool valid = c < o;
         const float sg = q ? 1.f : -1.f;  // an A row's bottom half is sg times the other part
+        // the bottom half's pieces are the partner lane's (L ^ 1) pieces of its own half, times sg: a shuffle
+        // of the packed pair and a flip of both sign bits where sg < 0 (bf16 rounding is sign-symmetric)
+        const uint32_t sflip = q ? 0u : 0x80008000u;
         const int NC = N >> 2, nch = NC >> 2, j0 = (ew >> 2) * NC;  // columns j0 .. j0 + NC - 1, nch chunks of 4
         const uint32_t lf = (uint32_t)(32 * q4) << 16;
         const uint32_t tD = tmem + lf + (uint32_t)j0;
@@ -298,16 +301,15 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                 for (int cc = 0; cc < 2; ++cc) {
                     const int k = 2 * kb + cc;
                     if (k >= nch) break;
-                    float t[4], b[4];
+                    float t[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        t[u] = d2f_trunc(wv[4 * cc + u]);
-                        b[u] = sg * __shfl_xor_sync(0xffffffffu, t[u], 1);
-                    }
+                    for (int u = 0; u < 4; ++u) t[u] = d2f_trunc(wv[4 * cc + u]);
                     U[2 * k] = p ? t[1] : t[0];
                     U[2 * k + 1] = p ? t[3] : t[2];
-                    tmem_st2(tA + 2 * k, tt_piece2(t[0], t[1], p), tt_piece2(t[2], t[3], p));
-                    tmem_st2(tAb + 2 * k, tt_piece2(b[0], b[1], p), tt_piece2(b[2], b[3], p));
+                    const uint32_t t0 = tt_piece2(t[0], t[1], p), t1 = tt_piece2(t[2], t[3], p);
+                    tmem_st2(tA + 2 * k, t0, t1);
+                    tmem_st2(tAb + 2 * k, __shfl_xor_sync(0xffffffffu, t0, 1) ^ sflip,
+                             __shfl_xor_sync(0xffffffffu, t1, 1) ^ sflip);
                 }
             }
             tmem_wait_st();
@@ -358,7 +360,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                         U[2 * k] += p ? tq[1] : tq[0];
                         U[2 * k + 1] += p ? tq[3] : tq[2];
                         if (last) continue;
-                        float xq[4], xo[4];
+                        float xq[4];
                         if (x_is_u) {
 #pragma unroll
                             for (int i = 0; i < 2; ++i) {
@@ -367,19 +369,16 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                 xq[2 * i] = p ? other : mine;
                                 xq[2 * i + 1] = p ? mine : other;
                             }
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) xo[u] = sg * __shfl_xor_sync(0xffffffffu, xq[u], 1);
                         } else {
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                xq[u] = tq[u];
-                                xo[u] = -sk * yp[u];  // sg times the other part of T_r
-                            }
+                            for (int u = 0; u < 4; ++u) xq[u] = tq[u];
                         }
-                        tmem_st2(tA + 2 * k, valid ? tt_piece2(xq[0], xq[1], p) : 0u,
-                                 valid ? tt_piece2(xq[2], xq[3], p) : 0u);
-                        tmem_st2(tAb + 2 * k, valid ? tt_piece2(xo[0], xo[1], p) : 0u,
-                                 valid ? tt_piece2(xo[2], xo[3], p) : 0u);
+                        // the bottom half: sg times the other part (the partner's xq), as its pieces
+                        const uint32_t x0 = tt_piece2(xq[0], xq[1], p), x1 = tt_piece2(xq[2], xq[3], p);
+                        const uint32_t o0 = __shfl_xor_sync(0xffffffffu, x0, 1) ^ sflip;
+                        const uint32_t o1 = __shfl_xor_sync(0xffffffffu, x1, 1) ^ sflip;
+                        tmem_st2(tA + 2 * k, valid ? x0 : 0u, valid ? x1 : 0u);
+                        tmem_st2(tAb + 2 * k, valid ? o0 : 0u, valid ? o1 : 0u);
                     }
                 }
                 tc_fence_before();
