@@ -106,12 +106,13 @@ __device__ __forceinline__ void tmem_st2(uint32_t a, uint32_t v0, uint32_t v1) {
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Piece p of (a, b) as a bf16 pair (a in the low half): p = 0 the
-// round-to-nearest bf16 of each, p = 1 the bf16 of the remainder.
-__device__ __forceinline__ uint32_t tt_piece2(float a, float b, int p) {
+// round-to-nearest bf16 of each, p = 1 the bf16 of the remainder, as the
+// bf16 of fma(npf, h, (a, b)) with npf = -p (the remainder is exact; for p =
+// 0 the fma returns a and b themselves).
+__device__ __forceinline__ uint32_t tt_piece2(float a, float b, float2 npf) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 m = __floats2bfloat162_rn(a - hf.x, b - hf.y);
-    const __nv_bfloat162 x = p ? m : h;
+    const float2 r = __ffma2_rn(npf, __bfloat1622float2(h), make_float2(a, b));
+    const __nv_bfloat162 x = __floats2bfloat162_rn(r.x, r.y);
     return *(const uint32_t*)&x;
 }
 
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
         // the bottom half's pieces are the partner lane's (L ^ 1) pieces of its own half, times sg: a shuffle
         // of the packed pair and a flip of both sign bits where sg < 0 (bf16 rounding is sign-symmetric)
         const uint32_t sflip = q ? 0u : 0x80008000u;
+        const float2 npf = p ? make_float2(-1.f, -1.f) : make_float2(0.f, 0.f);
         const int NC = N >> 2, nch = NC >> 2, j0 = (ew >> 2) * NC;  // columns j0 .. j0 + NC - 1, nch chunks of 4
         const uint32_t lf = (uint32_t)(32 * q4) << 16;
         const uint32_t tD = tmem + lf + (uint32_t)j0;
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                     for (int u = 0; u < 4; ++u) t[u] = d2f_trunc(wv[4 * cc + u]);
                     U[2 * k] = p ? t[1] : t[0];
                     U[2 * k + 1] = p ? t[3] : t[2];
-                    const uint32_t t0 = tt_piece2(t[0], t[1], p), t1 = tt_piece2(t[2], t[3], p);
+                    const uint32_t t0 = tt_piece2(t[0], t[1], npf), t1 = tt_piece2(t[2], t[3], npf);
                     tmem_st2(tA + 2 * k, t0, t1);
                     tmem_st2(tAb + 2 * k, __shfl_xor_sync(0xffffffffu, t0, 1) ^ sflip,
                              __shfl_xor_sync(0xffffffffu, t1, 1) ^ sflip);
@@ -373,12 +375,12 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
 #pragma unroll
                             for (int u = 0; u < 4; ++u) xq[u] = tq[u];
                         }
-                        // the bottom half: sg times the other part (the partner's xq), as its pieces
-                        const uint32_t x0 = tt_piece2(xq[0], xq[1], p), x1 = tt_piece2(xq[2], xq[3], p);
-                        const uint32_t o0 = __shfl_xor_sync(0xffffffffu, x0, 1) ^ sflip;
-                        const uint32_t o1 = __shfl_xor_sync(0xffffffffu, x1, 1) ^ sflip;
-                        tmem_st2(tA + 2 * k, valid ? x0 : 0u, valid ? x1 : 0u);
-                        tmem_st2(tAb + 2 * k, valid ? o0 : 0u, valid ? o1 : 0u);
+                        // the bottom half: sg times the other part (the partner's xq), as its pieces.  The
+                        // rows of columns c >= nocc stay zero (zero walker entries, zero products).
+                        const uint32_t x0 = tt_piece2(xq[0], xq[1], npf), x1 = tt_piece2(xq[2], xq[3], npf);
+                        tmem_st2(tA + 2 * k, x0, x1);
+                        tmem_st2(tAb + 2 * k, __shfl_xor_sync(0xffffffffu, x0, 1) ^ sflip,
+                                 __shfl_xor_sync(0xffffffffu, x1, 1) ^ sflip);
                     }
                 }
                 tc_fence_before();
