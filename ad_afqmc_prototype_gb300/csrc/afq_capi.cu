@@ -327,7 +327,7 @@ static int step_mixed(const afq_problem* pb, const afq_params* p, const afq_stat
     const LowpBufs lb = layout_lowp(la, d);
     const double2* mo = (const double2*)pb->mo_coeff;
     double2* walk = (double2*)st->walkers;
-    AFQ_TRY(launch_split_c(n * o, mo, ws.csplit, s));
+    if (!ws.ozB) AFQ_TRY(launch_split_c(n * o, mo, ws.csplit, s));  // the double-float m (nocc > 32)
     // force bias: G_half split straight from the Green's function kernel
     if (!green_ready) {
         AFQ_PHASE("green", s);
