@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--walkers", type=int, default=0, help="override the workload's walker count")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-e2e-numa", dest="e2e_numa", action="store_false",
+                    help="leave the process affinity alone for the end-to-end line")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison block")
     ap.add_argument("--no-cv", action="store_true", help="skip the control-variate line")
@@ -771,11 +773,54 @@ def fma_peak(lib, fp64: bool):
     return _FMA_PEAK[fp64]
 
 
+def _parse_cpulist(text):
+    cpus = set()
+    for part in text.strip().split(","):
+        if not part:
+            continue
+        a, _, b = part.partition("-")
+        cpus.update(range(int(a), int(b or a) + 1))
+    return cpus
+
+
+def gpu_local_cpus(dev=0):
+    """Host CPUs of the NUMA node the GPU is attached to (sysfs), or None."""
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(dev)
+        addr = "%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        with open(f"/sys/bus/pci/devices/{addr}/numa_node") as f:
+            node = int(f.read())
+        if node < 0:
+            return None
+        with open(f"/sys/devices/system/node/node{node}/cpulist") as f:
+            return _parse_cpulist(f.read()) or None
+    except (AttributeError, OSError, ValueError, RuntimeError):
+        return None
+
+
 def run_e2e(args, env, afqmc_block, W):
     """The same metric through the public API with host buffers: each step
     copies walkers, weights and overlaps from pinned host memory, runs
     afqmc_block, and reads walkers, weights, overlaps and the block energy
-    back to pinned host memory."""
+    back to pinned host memory.  The process runs on the GPU's local NUMA
+    node meanwhile (when sysfs names one), so that the pinned buffers are
+    placed in the memory next to the GPU; the affinity is restored after."""
+    old = os.sched_getaffinity(0)
+    local = gpu_local_cpus() if args.e2e_numa else None
+    use = (local & old) if local else None
+    if use:
+        os.sched_setaffinity(0, use)
+    try:
+        out = _run_e2e(args, env, afqmc_block, W)
+    finally:
+        if use:
+            os.sched_setaffinity(0, old)
+    out["host_numa_local"] = bool(use)
+    return out
+
+
+def _run_e2e(args, env, afqmc_block, W):
     import torch
     st0 = env["state"]
     hw = torch.empty(st0.walkers.shape, dtype=torch.complex128, pin_memory=True)
