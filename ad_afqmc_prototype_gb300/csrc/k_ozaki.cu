@@ -18,15 +18,16 @@
 // tensor cores' fp32 sums are exact.  Then
 //   m = 2^(E_r + F_a) sum_{d=2..9} D_d 2^(-7 d)
 // with the terms s + t > 9 left out (each below 2^-51 of 2^(E_r + F_a) an
-// orbital) and the digits cut toward zero at 2^-49: m to ~2^-45 of the
-// product of the row's and the column's largest entries, the accuracy of the
-// double-float m it replaces, given as a double-float pair.
+// orbital) and the digits cut toward zero at 2^-49: m to ~2^-43 of the
+// product of the row's and the column's largest entries (sums over the
+// orbitals of errors ~2^-49 each), the accuracy class of the double-float m
+// it replaces, given as a double-float pair.
 //
 // k_oz_m builds A itself: the walkers' rows are bulk-copied into shared
 // memory beside each B tile, sixteen producer warps cut them into digits and
-// write the 128-byte-swizzled A tile, one thread issues the MMAs, and four
-// epilogue warps recombine the digit sums from tensor memory.  A never goes
-// through HBM.
+// write the 128-byte-swizzled A tile, one thread issues the MMAs, four
+// epilogue warps recombine the digit sums from tensor memory, and four more
+// warps find the next tile's row scales E_r.  A never goes through HBM.
 #include "afq_internal.cuh"
 #include "tc_common.cuh"
 
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             if (lane == 0) mbar_arrive(exf0 + 8 * (it & 1));
         }
     } else {
-        // epilogue: this warp's 32 rows (lane quadrant q), half the trial orbitals
+        // epilogue: this warp's 32 rows (lane quadrant q), every trial orbital
         const int q = warp & 3;
         const int r = 32 * q + lane, wl = r >> 6, b = (r & 63) >> 1, part = r & 1;
         int slot = 0;
