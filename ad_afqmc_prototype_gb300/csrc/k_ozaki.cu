@@ -450,6 +450,7 @@ int launch_oz_m(int W, int n, int o, const double2* walkers, const __nv_bfloat16
     using namespace tc;
     if (W <= 0) return AFQ_OK;
     if (o > 32) return fail(AFQ_E_UNSUPPORTED, "ozaki m: nocc=%d > 32", o);
+    if (n > 584) return fail(AFQ_E_UNSUPPORTED, "ozaki m: norb=%d > 584 (digit sums past 2^24)", n);
     if (((uintptr_t)walkers) & 15) return fail(AFQ_E_INVALID_ARGUMENT, "ozaki m: walkers not 16-byte aligned");
     const OzDims z = oz_dims(n, o);
     const OzGeo g = oz_geo(o);
