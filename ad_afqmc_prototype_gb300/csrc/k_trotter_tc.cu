@@ -331,6 +331,15 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                 const bool last = r == R - 1;
                 const bool x_is_u = !last && (r == 0 || r == R - 2);  // the next operand is U (W1, or out)
                 const bool term_is_y = r == 0 || last;                // the term added to U: Y, else T_r
+                // the middle products (T_r, r = 1 .. R - 3): each lane keeps its partner's (L ^ 1) share of
+                // U and forms the partner's part of T_r from its own Y, which needs no exchange of Y; U
+                // is swapped into that arrangement before them and back before product R - 2
+                const bool mid = !term_is_y && !x_is_u;
+                if (R >= 4 && (r == 1 || r == R - 2)) {
+#pragma unroll
+                    for (int m = 0; m < 2 * MAXCH; ++m) U[m] = __shfl_xor_sync(0xffffffffu, U[m], 1);
+                }
+                const float nsgsk = -sgsk;  // the partner's sg sk
 #pragma unroll
                 for (int kb = 0; kb < (MAXCH + 3) / 4; ++kb) {  // 16-column batches of the accumulator
                     if (4 * kb >= nch) break;
@@ -351,6 +360,23 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                     for (int cc = 0; cc < 4; ++cc) {
                         const int k = 4 * kb + cc;
                         if (k >= nch) break;
+                        if (mid) {
+                            float tp[4];  // the partner's own part of T_r
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const float y = __uint_as_float(v[4 * cc + u]);
+                                tp[u] = nsgsk * (y + __shfl_xor_sync(0xffffffffu, y, 2));
+                            }
+                            U[2 * k] += p ? tp[1] : tp[0];
+                            U[2 * k + 1] += p ? tp[3] : tp[2];
+                            // the top half is the partner's pieces of its tp (this lane's part of T_r),
+                            // the bottom half sg times this lane's tp
+                            const uint32_t x0 = tt_piece2(tp[0], tp[1], npf), x1 = tt_piece2(tp[2], tp[3], npf);
+                            tmem_st2(tA + 2 * k, __shfl_xor_sync(0xffffffffu, x0, 1),
+                                     __shfl_xor_sync(0xffffffffu, x1, 1));
+                            tmem_st2(tAb + 2 * k, x0 ^ sflip, x1 ^ sflip);
+                            continue;
+                        }
                         float yp[4], tq[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
