@@ -59,3 +59,13 @@ def test_roofline_binary64_form_keeps_fp64_phases(monkeypatch):
     assert r["kernel"] == "vbuild_gemm" and r["bound"] == "fp64" and r["peak"] == 1.25
     r = bench.roofline_for(phases, work, None, 2, name="overlap")
     assert r["kernel"] == "overlap" and r["bound"] == "fp64"
+
+
+def test_host_numa_helpers():
+    """The end-to-end line's NUMA helper parses sysfs cpulists and gives up
+    quietly where no GPU (or no sysfs entry) is found."""
+    assert bench._parse_cpulist("0-3,8,10-11\n") == {0, 1, 2, 3, 8, 10, 11}
+    assert bench._parse_cpulist("5") == {5}
+    assert bench._parse_cpulist("") == set()
+    got = bench.gpu_local_cpus()
+    assert got is None or (isinstance(got, set) and got)
